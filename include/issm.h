@@ -1,0 +1,299 @@
+/*
+ * issm.h — C ABI of libissm103.so, the sm_103a importance-sampling hot path.
+ *
+ * Every entry point is `extern "C"`, takes plain device pointers, element
+ * counts and a CUDA stream, never allocates caller-visible memory, never calls
+ * cudaDeviceSynchronize, and returns an int status:
+ *   0                       success
+ *   > 0                     a cudaError_t raised by a launch on the stream
+ *   < 0                     an argument error (ISSM_E_*)
+ * Sample-level numeric failures are NOT return errors: they are recorded in
+ * the caller's 3-word failure record exactly as the reference packs them
+ * (src/execution.jl:669-699, reason bits :758-767), so the reference's
+ * `_device_failure_snapshot` -> `SamplerExecutionError` path reads them as-is.
+ *
+ * Layouts follow the reference's column-major Julia arrays:
+ *   samples      d x N   sample i at x[i*d .. i*d+d-1]
+ *   locations    d x K   component k at loc[k*d ..]
+ *   factors      d x d x K, column-major lower-triangular L_k (zeros above)
+ *   counts/coefs K x R   column r is one round
+ * All float arrays of one call share the dtype given in the call (or in the
+ * bank); reductions that the reference accumulates in >= Float32 are kept in
+ * FP64 here and written to caller-provided FP64 device words.
+ *
+ * Threading: entry points are reentrant for distinct output/workspace
+ * buffers; a prepared sampler that owns them is non-reentrant
+ * (src/methods/importance_sampling.jl:105-116).
+ */
+#ifndef ISSM_H
+#define ISSM_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same object as cudaStream_t (struct CUstream_st*); NULL = legacy stream. */
+typedef struct CUstream_st *issm_stream_t;
+
+/* ---- status codes ------------------------------------------------------ */
+#define ISSM_OK                 0
+#define ISSM_E_NULL           (-1)   /* a required pointer is NULL            */
+#define ISSM_E_SIZE           (-2)   /* a size is negative or out of range    */
+#define ISSM_E_DTYPE          (-3)   /* unsupported dtype / dtype mismatch    */
+#define ISSM_E_KIND           (-4)   /* unknown family/scale/denominator kind */
+#define ISSM_E_ALL_ZERO       (-5)   /* every log weight is -Inf (AllZeroWeightsError, src/results.jl:133-144) */
+#define ISSM_E_UNSUPPORTED    (-6)   /* valid request this build does not run */
+#define ISSM_E_WORKSPACE      (-7)   /* workspace too small                   */
+#define ISSM_E_NOT_POSDEF     (-8)   /* Cholesky met a non-positive pivot     */
+
+/* ---- enums ------------------------------------------------------------- */
+#define ISSM_F32 0
+#define ISSM_F64 1
+
+#define ISSM_GAUSSIAN  0   /* GaussianFamily  src/proposals.jl:15            */
+#define ISSM_STUDENT_T 1   /* StudentTFamily  src/proposals.jl:17-20         */
+
+#define ISSM_SCALE_FACTOR    0  /* _FactorGaussianScale: L lower d x d      */
+#define ISSM_SCALE_DIAGONAL  1  /* _DiagonalGaussianScale: d scales         */
+#define ISSM_SCALE_SPHERICAL 2  /* _SphericalGaussianScale: 1 scale         */
+
+/* Denominator kinds (src/mis_execution.jl:30-65 and the term policies):     */
+#define ISSM_DENOM_FULL       0 /* all K slots, coef[k]   (_FullMixtureDenominator, src/methods/static_mis.jl:389-417;
+                                   _RealizedMixtureDenominator, src/mis_execution.jl:67-89) */
+#define ISSM_DENOM_GENERATING 1 /* generating slot only, coef 0 (_GeneratingDenominator, static_mis.jl:402-443) */
+#define ISSM_DENOM_PARTIAL    2 /* slots in the generating slot's group, coef[k] (_PartialMixtureDenominator) */
+#define ISSM_DENOM_PREFIX     3 /* slots 0..terms-1, coef[k] (_AMISMixtureDenominator, src/amis_execution.jl:12-35) */
+
+/* Contraction precision of the Mahalanobis term. */
+#define ISSM_PREC_NATIVE 0  /* SIMT in the bank dtype: the drop-in FP32/FP64 path */
+#define ISSM_PREC_TF32   1  /* tcgen05 kind::tf32, FP32 accumulate, centred inputs */
+#define ISSM_PREC_BF16   2  /* tcgen05 kind::f16 (bf16), FP32 accumulate, centred inputs */
+
+/* Failure reason bits (src/execution.jl:758-767, adaptive_gaussian_execution.jl:9) */
+#define ISSM_REASON_TARGET_NAN          0x0100u
+#define ISSM_REASON_TARGET_POS_INF      0x0200u
+#define ISSM_REASON_PROPOSAL_INVALID    0x0400u
+#define ISSM_REASON_GENERATED_NONFINITE 0x0800u
+#define ISSM_REASON_LOGWEIGHT_INVALID   0x1000u
+#define ISSM_REASON_DRAW_EXHAUSTED      0x0010u
+#define ISSM_REASON_MOMENT_FIT_INVALID  0x2000u
+
+/* A proposal bank packed as the reference's _PackedFactorBank /
+ * _PackedDiagonalBank (src/proposal_banks.jl:139-163). All float arrays have
+ * `dtype`. `dofs` is NULL for Gaussian banks; Student-t lognormalizers already
+ * include the per-slot Student-t log constant (src/proposals.jl:413-437).
+ * `range_risk` (optional, K bytes) marks slots whose factor exponent bound
+ * makes the Student-t density take the full-range radius
+ * (src/student_t_range.jl:35-36). */
+typedef struct issm_bank {
+    int32_t dim;           /* d >= 1                                     */
+    int32_t count;         /* K >= 1 active slots                        */
+    int32_t family;        /* ISSM_GAUSSIAN / ISSM_STUDENT_T             */
+    int32_t scale_kind;    /* ISSM_SCALE_*                               */
+    int32_t dtype;         /* ISSM_F32 / ISSM_F64                        */
+    int32_t reserved;
+    const void *locations;       /* d x K                                 */
+    const void *scales;          /* factor d x d x K | diag d x K | sph K */
+    const void *lognormalizers;  /* K                                     */
+    const void *dofs;            /* K or NULL                             */
+    const uint8_t *range_risk;   /* K or NULL                             */
+} issm_bank;
+
+typedef struct issm_denominator {
+    int32_t kind;                /* ISSM_DENOM_*                          */
+    int32_t terms;               /* PREFIX: number of leading slots       */
+    const void *logcoefficients; /* K, bank dtype (unused for GENERATING)  */
+    const int32_t *group_of_slot;/* PARTIAL: group id per slot            */
+} issm_denominator;
+
+/* ---- introspection ----------------------------------------------------- */
+/* Library version string, e.g. "issm103 1.0.0 sm_103a". */
+const char *issm_version(void);
+/* Human-readable message for a status code. */
+const char *issm_status_string(int status);
+
+/* ---- failure record (src/execution.jl:669-756) ------------------------- */
+/* Zero the 3-word record on the stream (replaces _reset_native_failure_scratch!,
+ * src/execution.jl:652-657). */
+int issm_failure_reset(uint64_t *failures, issm_stream_t stream);
+
+/* ---- device random streams (replace CUDA.RNG draws,
+ *      ext/ImportanceSamplersCUDAExt.jl:253-256) --------------------------- */
+/* Standard normals / U[0,1) uniforms from counter-based Philox-4x32-10 with
+ * Box-Muller; element i depends only on (seed, offset + i). */
+int issm_fill_normals(uint64_t seed, uint64_t offset, int64_t n, void *out,
+                      int32_t dtype, issm_stream_t stream);
+int issm_fill_uniforms(uint64_t seed, uint64_t offset, int64_t n, void *out,
+                       int32_t dtype, issm_stream_t stream);
+
+/* ---- assignment and draw ---------------------------------------------- */
+/* Static-MIS assignment: u' = (i + u_i)/N (stratified) or u_i (random), then
+ * the first slot with u' <= cdf[slot]. Replaces _static_mis_assignment_kernel!
+ * (src/static_mis_execution.jl:125-139; rule src/methods/static_mis.jl:171-211).
+ * Writes 0-based slots. */
+int issm_static_assign(const void *cdf, int32_t k, const void *uniforms,
+                       int64_t n, int32_t stratified, int32_t *slots,
+                       int32_t dtype, issm_stream_t stream);
+
+/* Draw x_i = mu_s + L_s * (m_i * n_i) for slot s = slots[i] (or `fixed_slot`
+ * when slots == NULL). Student-t banks compute the radial multiplier m_i from
+ * the buffered Marsaglia-Tsang gamma draw (8 attempts) on `radial_normals`
+ * and `radial_uniforms` with the given per-sample strides. Replaces
+ * _native_store_sample! (src/native_execution.jl:488-528),
+ * _scale_mis_normals_kernel! (:184-199) and _student_t_radial_multiplier
+ * (:153-180). Non-finite draws record ISSM_REASON_GENERATED_NONFINITE.
+ * `index_base` is added to the 0-based sample index before it is packed
+ * (1-based logical index = index_base + i + 1). */
+int issm_draw(const issm_bank *bank, const int32_t *slots, int32_t fixed_slot,
+              const void *normals, const void *radial_normals,
+              int32_t radial_normal_stride, const void *radial_uniforms,
+              int32_t radial_uniform_stride, int64_t n, void *samples,
+              uint64_t *failures, int64_t index_base, issm_stream_t stream);
+
+/* ---- balance-heuristic denominators ------------------------------------ */
+/* out_logden[i] = log sum_{k in terms(i)} exp(coef_k + log q_k(x_i)),
+ * out_generating[i] = log q_{slots[i]}(x_i) (optional). Records
+ * ISSM_REASON_PROPOSAL_INVALID when the generating density or the
+ * denominator is NaN or -Inf, and then writes -Inf.
+ * Replaces _mis_logdenominator_core (src/mis_execution.jl:30-65) over
+ * _packed_gaussian_logdensity! (src/native_execution.jl:346-384) and
+ * _radial_logdensity (src/proposals.jl:24-55). `precision` selects the SIMT
+ * path (NATIVE) or the tcgen05 contraction (TF32/BF16; factor-Gaussian and
+ * factor-Student-t banks, FP32 samples, d <= 64). */
+int issm_mixture_logdensity(const issm_bank *bank, const issm_denominator *den,
+                            const void *x, int64_t n, const int32_t *slots,
+                            int32_t fixed_slot, void *out_logden,
+                            void *out_generating, uint64_t *failures,
+                            int64_t index_base, int32_t precision,
+                            issm_stream_t stream);
+
+/* Fused static-MIS / DM-PMC round: draw + denominator + log weight.
+ * logw_i = logtarget_i - logden_i when `logtargets` is non-NULL; with
+ * logtargets == NULL the target is deferred (the reference's batch-target
+ * path, src/batched_targets.jl:70-77) and logw_i = -logden_i, finished later
+ * by issm_add_target_values. proposal_ids_out[i] = proposal_ids[slot] (or 0
+ * on failure). Replaces _mis_round_launch_kernel! (src/mis_execution.jl:674-720). */
+int issm_mis_round(const issm_bank *bank, const issm_denominator *den,
+                   const int32_t *slots, const void *normals,
+                   const void *radial_normals, int32_t radial_normal_stride,
+                   const void *radial_uniforms, int32_t radial_uniform_stride,
+                   const void *logtargets, int64_t n, void *samples,
+                   void *logweights, const int64_t *proposal_ids,
+                   int64_t *proposal_ids_out, uint64_t *failures,
+                   int32_t precision, issm_stream_t stream);
+
+/* Batch-target finish: logw_i += values_i, recording target NaN/+Inf and
+ * invalid log weights. Replaces _finish_batch_weights! (src/batched_targets.jl:204-214). */
+int issm_add_target_values(void *logweights, const void *values, int64_t n,
+                           int32_t dtype, uint64_t *failures,
+                           int64_t index_base, issm_stream_t stream);
+
+/* logw_i = logtarget_i - logden_i with the reference's invalid-weight check
+ * (_subtract_logweight, src/methods/importance_sampling.jl:1261-1266). */
+int issm_subtract_logweights(const void *logtargets, const void *logden,
+                             int64_t n, int32_t dtype, void *logweights,
+                             uint64_t *failures, int64_t index_base,
+                             issm_stream_t stream);
+
+/* ---- AMIS retrospective recurrence (src/amis_execution.jl) -------------- */
+/* Old samples: lognum_i <- logaddexp(lognum_i, logcounts[slot] + log q_slot(x_i)).
+ * Replaces _append_logmixture_kernel! (src/amis_execution.jl:37-71). */
+int issm_amis_append(const issm_bank *history, int32_t slot,
+                     const void *logcounts, const void *x, int64_t n,
+                     void *lognumerators, uint64_t *failures,
+                     int32_t precision, issm_stream_t stream);
+
+/* All samples of rounds 1..t: logw_i = logtarget_i - (lognum_i - logtotal)
+ * for round_ids[i] != 0. Replaces _form_amis_logweights_kernel!
+ * (src/amis_execution.jl:107-134). */
+int issm_amis_form(const void *logtargets, const void *lognumerators,
+                   const int64_t *round_ids, double logtotal, int64_t n,
+                   int32_t dtype, void *logweights, uint64_t *failures,
+                   issm_stream_t stream);
+
+/* ---- log-weight reductions (src/execution.jl:103-186, src/results.jl:6-36,560-626) */
+/* out[0..2] = (max, sum exp(l-max), sum exp(2(l-max))) in FP64 over n log
+ * weights, merged as _merge_logweight_moments. out is 3 FP64 device words.
+ * workspace: issm_reduce_workspace_bytes(n) bytes of device memory. */
+size_t issm_reduce_workspace_bytes(int64_t n);
+int issm_logweight_summary(const void *logweights, int64_t n, int32_t dtype,
+                           double *out, void *workspace, size_t workspace_bytes,
+                           issm_stream_t stream);
+
+/* w_i = exp(l_i - max) / S using a summary produced by
+ * issm_logweight_summary (device FP64 words). Replaces normalized_weights
+ * (src/results.jl:589-598) and _normalize_moment_weights! (adaptive_gaussian_execution.jl:207-247). */
+int issm_normalize(const void *logweights, int64_t n, int32_t dtype,
+                   const double *summary, void *weights, issm_stream_t stream);
+
+/* ---- resampling (src/resampling.jl) ------------------------------------ */
+/* Reference-compatible CDF: cdf = cumsum(exp(l - max)) / total in the
+ * logweight dtype (>= F32). Replaces _resampling_cdf! (src/resampling.jl:199-225). */
+int issm_resampling_cdf(const void *logweights, int64_t n, int32_t dtype,
+                        void *cdf, void *workspace, size_t workspace_bytes,
+                        issm_stream_t stream);
+/* Ancestors (1-based, as the reference) for given uniforms: first j with
+ * u < cdf[j] (strict), then the -Inf plateau repair. Replaces
+ * _select_resampling_ancestors_kernel! (src/resampling.jl:92-118). */
+int issm_resample_select(const void *cdf, const void *logweights, int64_t n,
+                         const void *uniforms, int64_t count, int32_t dtype,
+                         int64_t *ancestors, issm_stream_t stream);
+/* Deterministic multinomial / systematic resampling on an exact 64-bit
+ * fixed-point CDF of w_j = exp(l_j - max) (see docs); ancestors 1-based.
+ * Systematic uses one uniform u: u_i = (i + u)/count. */
+size_t issm_resample_workspace_bytes(int64_t n);
+int issm_resample_multinomial(const void *logweights, int64_t n, int32_t dtype,
+                              const double *uniforms, int64_t count,
+                              int64_t *ancestors, void *workspace,
+                              size_t workspace_bytes, issm_stream_t stream);
+int issm_resample_systematic(const void *logweights, int64_t n, int32_t dtype,
+                             double u, int64_t count, int64_t *ancestors,
+                             void *workspace, size_t workspace_bytes,
+                             issm_stream_t stream);
+/* dst[:, i] = src[:, ancestors[i]] (1-based ancestors). Replaces
+ * _gather_resampled_samples_kernel! (src/resampling.jl:160-164). */
+int issm_gather(const void *src, int32_t d, int64_t n_src,
+                const int64_t *ancestors, int64_t count, int32_t dtype,
+                void *dst, issm_stream_t stream);
+/* DM-PMC local resampling: one ancestor per proposal slot from that slot's
+ * contiguous run of `counts[slot]` samples, threshold u_slot * total with a
+ * strict < scan; ancestor 0 when the slot has no positive weight. Replaces
+ * _local_resample_locations_kernel! and the cooperative GPU variant
+ * (src/dm_pmc_execution.jl:80-265). */
+int issm_local_resample(const void *logweights, const int64_t *counts,
+                        int32_t k, const void *uniforms, const void *samples,
+                        int32_t d, int32_t dtype, int64_t *ancestors,
+                        void *destination, issm_stream_t stream);
+
+/* ---- adaptation moments (src/adaptive_gaussian_execution.jl:186-528) ---- */
+/* Weighted mean and covariance with normalised weights exp(l - max)/S taken
+ * from a device summary: mean = sum w x, cov = sum w (x-mean)(x-mean)^T, in
+ * FP64, accumulated about `shift` (d FP64 device words, e.g. the previous
+ * mean). Replaces _weighted_moments! (:268-273). workspace:
+ * issm_moments_workspace_bytes(n, d). */
+size_t issm_moments_workspace_bytes(int64_t n, int32_t d);
+int issm_weighted_moments(const void *x, int32_t d, int64_t n,
+                          const void *logweights, int32_t dtype,
+                          const double *summary, const double *shift,
+                          double *mean, double *cov, void *workspace,
+                          size_t workspace_bytes, issm_stream_t stream);
+/* Candidate fit: cov + ridge I with ridge = sqrt(eps(T)) tr(L_prev L_prev^T)
+ * * c_nu / d (src/adaptive_gaussian_execution.jl:283-301, src/execution.jl:188-194),
+ * FP64 Cholesky, Student-t scaling by sqrt((nu-2)/nu), lognormalizer and the
+ * validity rule (:475-528). Writes mean/factor/lognormalizer in `dtype` into
+ * the history slot pointers; records ISSM_REASON_MOMENT_FIT_INVALID at
+ * logical index `failure_index` on failure. `dof` <= 0 means Gaussian. */
+int issm_fit_factor(const double *mean, const double *cov, int32_t d,
+                    const void *previous_factor, double dof,
+                    double logconstant, int32_t dtype, void *out_location,
+                    void *out_factor, void *out_lognormalizer,
+                    uint64_t *failures, int64_t failure_index,
+                    issm_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ISSM_H */
