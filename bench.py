@@ -1,0 +1,303 @@
+"""Headline benchmark: AMIS weighted samples/s on the d = 64 Student-t
+workload (40 rounds x 50,000 samples, 2,000,000 retained weighted samples),
+through the public sampler API, with the log-Z and posterior-mean error
+reported beside the rate.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp32|tf32|bf16] [--impl gb300|reference]
+
+One step = one complete AMIS run (draw, target, retrospective
+balance-heuristic denominators, weights, summaries, weighted moments and FP64
+Cholesky fits for all 40 rounds) on device-resident problem data. `e2e`
+repeats the step through the same public API starting from host arrays
+(target and initial proposal copied in) and reading the run's summaries and
+posterior mean back. Under torchrun every rank runs an independent replica
+(the path has no cross-sample exchange), timed between barriers, max over ranks.
+`--impl reference` times the CPU restatement of the reference's threaded AMIS
+(FP64, all host cores) on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+D, ROUNDS, ROUND_SIZE, DOF = 64, 40, 50_000, 5.0
+CPU_ROUND_SIZE = 2_500
+WORKLOAD = "AMIS d=64, Student-t target (nu=5), 40 rounds x 50,000 samples, factor-Gaussian proposals"
+METRIC = "AMIS weighted samples/s at fixed logZ error"
+
+
+def problem(seed=20261203):
+    """Seeded synthetic C4 inputs: scale factor L (N(0, 0.3^2) below the
+    diagonal, 1 + |N(0,1)| on it), location 0, initial proposal N(0, 9 I)."""
+    rng = np.random.default_rng(seed)
+    L = np.tril(rng.normal(scale=0.3, size=(D, D)), -1) + np.diag(1.0 + np.abs(rng.normal(size=D)))
+    return np.zeros(D), L, np.zeros(D), 3.0 * np.eye(D)
+
+
+def read_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return float(p["hbm_gbs"]), float(p.get("bf16_tflops_sustained", p["bf16_tflops"])), "measured"
+    except Exception:
+        return 6800.0, 1700.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu_index = gpu_index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu_index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([v.strip() for v in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_info():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def cpu_amis_rate(threads=None, round_size=CPU_ROUND_SIZE, reps=1):
+    """Oracle AMIS (FP64, OpenMP on all host cores) on 40 rounds x round_size."""
+    from oracle import oracle as orc
+
+    if threads:
+        orc.set_threads(threads)
+    loc, L, p_loc, p_fac = problem()
+    tgt = orc.TargetView(orc.TARGET_STUDENT_T, D, a=loc, b=L, p0=DOF)
+    total = round_size * ROUNDS
+    normals = orc.philox_normals(11, 0, total * D)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        out = orc.amis_run(tgt, D, p_loc, p_fac, [round_size] * ROUNDS, normals)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    return total / best, orc.num_threads(), out
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+
+    orc.build()
+    for _ in range(args.warmup):
+        cpu_amis_rate(reps=1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, cores, out = cpu_amis_rate(reps=1)
+        times.append(time.perf_counter() - t0)
+    total = CPU_ROUND_SIZE * ROUNDS
+    value = total * len(times) / sum(times)
+    sample = f"40 rounds x {CPU_ROUND_SIZE} samples (d=64), FP64, one full AMIS run per step"
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "weighted samples/s",
+            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded C4 inputs)",
+            "config": {"workload": WORKLOAD, "sample": sample, "backend": "CPU oracle restatement (OpenMP)"},
+            "cpu_baseline": {"value": value, "unit": "weighted samples/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "weighted samples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "logz_error": float(abs(out["round_logz"][-1]))}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import torch
+
+    rank, world, local_rank = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local_rank if world > 1 else 0)
+    torch.cuda.set_device(dev)
+    import __graft_entry__ as ge
+
+    issm = ge.load_package()
+    issm.native.require()
+    precision = {"fp32": issm.native.PREC_NATIVE, "tf32": issm.native.PREC_TF32,
+                 "bf16": issm.native.PREC_BF16}[args.precision]
+    loc, L, p_loc, p_fac = problem()
+    target = issm.StudentTTarget(loc, L, DOF)
+    proposal = issm.FactorGaussian(p_loc.astype(np.float32), p_fac.astype(np.float32))
+    alg = issm.AMIS(proposal, rounds=ROUNDS, round_size=ROUND_SIZE)
+    sampler = issm.prepare_sampler(1234 + rank, target, alg, device=dev, precision=precision)
+
+    def step():
+        # each step restarts from the same initial proposal (no carried adaptation)
+        sampler.committed = tuple(t.clone() for t in sampler.initial) if hasattr(sampler, "initial") else \
+            sampler.committed
+        return issm.importance_sample_(sampler)
+
+    sampler.initial = tuple(t.clone() for t in sampler.committed)
+    launches0 = issm.native.lib().issm_kernel_launches()
+    for _ in range(max(args.warmup, 3)):
+        res = step()
+    torch.cuda.synchronize()
+    barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
+    stream = torch.cuda.current_stream()
+    with ClockSampler(dev.index) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        l0 = issm.native.lib().issm_kernel_launches()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        for _ in range(args.steps):
+            res = step()
+        end.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        l1 = issm.native.lib().issm_kernel_launches()
+    ms = start.elapsed_time(end) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    total = ROUNDS * ROUND_SIZE
+    value = total * world / (ms / 1e3)
+    logz = float(res.diagnostics["round_lognormalizers"][-1])
+    post_mean = issm.mean(res).cpu().numpy()
+
+    # per-kernel profile of one extra run (events on the launching stream)
+    sampler.profile = []
+    step()
+    torch.cuda.synchronize()
+    groups = {}
+    for name, s0, s1, nbytes in sampler.profile:
+        g = groups.setdefault(name, [0.0, 0, 0])
+        g[0] += s0.elapsed_time(s1)
+        g[1] += 1
+        g[2] += nbytes
+    sampler.profile = None
+    dominant = max(groups, key=lambda k: groups[k][0])
+    tms, cnt, nbytes = groups[dominant]
+    hbm, tflops, src = read_peaks()
+    achieved = (nbytes / cnt) / ((tms / cnt) / 1e3) / 1e9
+    share = {k: round(v[0] / sum(x[0] for x in groups.values()), 4) for k, v in groups.items()}
+
+    # e2e: host arrays in, summaries and posterior mean out, through the public API
+    def e2e_step():
+        tgt = issm.StudentTTarget(loc, L, DOF)
+        prop = issm.FactorGaussian(p_loc.astype(np.float32), p_fac.astype(np.float32))
+        smp = issm.prepare_sampler(99 + rank, tgt, issm.AMIS(prop, rounds=ROUNDS, round_size=ROUND_SIZE),
+                                   device=dev, precision=precision)
+        r = issm.importance_sample_(smp)
+        pm = issm.mean(r).cpu().numpy()
+        return r, pm
+
+    h2d = (D + D * D) * 4 * 2 + (D + D * D) * 4  # target (both dtypes bound lazily: float32) + proposal
+    h2d = (D + D * D) * 4 + (D + D * D) * 4
+    d2h = ROUNDS * 3 * 8 * 2 + D * 8 + 3 * 8
+    for _ in range(2):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(2, args.steps // 2)
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    if rank != 0:
+        return
+    cpu_value, cores, _ = cpu_amis_rate(reps=1)
+    line = {
+        "metric": METRIC, "value": value, "unit": "weighted samples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": {"fp32": "f32", "tf32": "tf32", "bf16": "bf16"}[args.precision],
+        "data": "synthetic (seeded C4 inputs)",
+        "config": {"workload": WORKLOAD, "d": D, "rounds": ROUNDS, "round_size": ROUND_SIZE,
+                   "precision": args.precision, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2: 512 MiB retained samples re-read every round"},
+        "accuracy": {"logz_hat": logz, "abs_logz_error": abs(logz), "posterior_mean_max_abs_error":
+                     float(np.max(np.abs(post_mean - loc)))},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "peak_source": f"{src} hbm_gbs", "traffic": None,
+                     "kernel_share": share},
+        "cpu_baseline": {"value": cpu_value, "unit": "weighted samples/s", "cores": cores, "kind": "port",
+                         "sample": f"40 rounds x {CPU_ROUND_SIZE} samples (d=64), FP64 oracle AMIS"},
+        "e2e": {"value": total * world / (e2e_ms / 1e3), "unit": "weighted samples/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+        "gpu_launches": int((l1 - l0) // args.steps),
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "bf16"])
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

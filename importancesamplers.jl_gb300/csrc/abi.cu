@@ -1,0 +1,305 @@
+// abi.cu — the extern "C" boundary of libissm103.so (declared in
+// include/issm.h). Validates arguments, maps them to the kernel entry points
+// and returns 0 / cudaError_t / ISSM_E_*; no exception crosses the ABI.
+#include <stdio.h>
+
+#include "issm_device.cuh"
+#include "issm_internal.h"
+
+#include <atomic>
+
+using namespace issm;
+
+namespace issm {
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace issm
+
+namespace {
+
+int check_bank(const issm_bank *b) {
+    if (!b || !b->locations || !b->scales || !b->lognormalizers) return ISSM_E_NULL;
+    if (b->dim < 1 || b->count < 1) return ISSM_E_SIZE;
+    if (b->dtype != ISSM_F32 && b->dtype != ISSM_F64) return ISSM_E_DTYPE;
+    if (b->family != ISSM_GAUSSIAN && b->family != ISSM_STUDENT_T) return ISSM_E_KIND;
+    if (b->scale_kind < ISSM_SCALE_FACTOR || b->scale_kind > ISSM_SCALE_SPHERICAL) return ISSM_E_KIND;
+    if (b->family == ISSM_STUDENT_T && !b->dofs) return ISSM_E_NULL;
+    return ISSM_OK;
+}
+
+int check_den(const issm_bank *b, const issm_denominator *den) {
+    if (!den) return ISSM_E_NULL;
+    switch (den->kind) {
+    case ISSM_DENOM_FULL:
+        return den->logcoefficients ? ISSM_OK : ISSM_E_NULL;
+    case ISSM_DENOM_GENERATING:
+        return ISSM_OK;
+    case ISSM_DENOM_PARTIAL:
+        return (den->logcoefficients && den->group_of_slot) ? ISSM_OK : ISSM_E_NULL;
+    case ISSM_DENOM_PREFIX:
+        if (!den->logcoefficients) return ISSM_E_NULL;
+        return (den->terms >= 1 && den->terms <= b->count) ? ISSM_OK : ISSM_E_SIZE;
+    }
+    return ISSM_E_KIND;
+}
+
+int check_dtype(int dtype) { return (dtype == ISSM_F32 || dtype == ISSM_F64) ? ISSM_OK : ISSM_E_DTYPE; }
+
+}  // namespace
+
+#define ISSM_TRY(expr)            \
+    do {                          \
+        int _st = (expr);         \
+        if (_st != 0) return _st; \
+    } while (0)
+
+extern "C" {
+
+const char *issm_version(void) { return "issm103 1.0.0 sm_103a"; }
+
+uint64_t issm_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+const char *issm_status_string(int status) {
+    switch (status) {
+    case ISSM_OK: return "success";
+    case ISSM_E_NULL: return "a required pointer is NULL";
+    case ISSM_E_SIZE: return "a size is negative or out of range";
+    case ISSM_E_DTYPE: return "unsupported or mismatched dtype";
+    case ISSM_E_KIND: return "unknown family, scale or denominator kind";
+    case ISSM_E_ALL_ZERO: return "normalized weights are undefined because all raw weights are zero";
+    case ISSM_E_UNSUPPORTED: return "request not supported by this build";
+    case ISSM_E_WORKSPACE: return "workspace too small";
+    case ISSM_E_NOT_POSDEF: return "covariance is not positive definite";
+    }
+    if (status > 0) return cudaGetErrorString((cudaError_t)status);
+    return "unknown status";
+}
+
+int issm_failure_reset(uint64_t *failures, issm_stream_t stream) {
+    if (!failures) return ISSM_E_NULL;
+    return failure_reset(failures, (cudaStream_t)stream);
+}
+
+int issm_fill_normals(uint64_t seed, uint64_t offset, int64_t n, void *out, int32_t dtype, issm_stream_t stream) {
+    if (n < 0) return ISSM_E_SIZE;
+    if (n > 0 && !out) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return fill_normals(seed, offset, n, out, dtype, (cudaStream_t)stream);
+}
+
+int issm_fill_uniforms(uint64_t seed, uint64_t offset, int64_t n, void *out, int32_t dtype, issm_stream_t stream) {
+    if (n < 0) return ISSM_E_SIZE;
+    if (n > 0 && !out) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return fill_uniforms(seed, offset, n, out, dtype, (cudaStream_t)stream);
+}
+
+int issm_static_assign(const void *cdf, int32_t k, const void *uniforms, int64_t n, int32_t stratified,
+                       int32_t *slots, int32_t dtype, issm_stream_t stream) {
+    if (n < 0 || k < 1) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!cdf || !uniforms || !slots) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return static_assign(cdf, k, uniforms, n, stratified, slots, dtype, (cudaStream_t)stream);
+}
+
+int issm_draw(const issm_bank *bank, const int32_t *slots, int32_t fixed_slot, const void *normals,
+              const void *radial_normals, int32_t radial_normal_stride, const void *radial_uniforms,
+              int32_t radial_uniform_stride, int64_t n, void *samples, uint64_t *failures, int64_t index_base,
+              issm_stream_t stream) {
+    ISSM_TRY(check_bank(bank));
+    if (n < 0) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!normals || !samples) return ISSM_E_NULL;
+    if (!slots && (fixed_slot < 0 || fixed_slot >= bank->count)) return ISSM_E_SIZE;
+    if (bank->family == ISSM_STUDENT_T && !radial_normals) return ISSM_E_NULL;
+    return simt_draw(bank, slots, fixed_slot, normals, radial_normals, radial_normal_stride, radial_uniforms,
+                     radial_uniform_stride, n, samples, failures, index_base, (cudaStream_t)stream);
+}
+
+int issm_mixture_logdensity(const issm_bank *bank, const issm_denominator *den, const void *x, int64_t n,
+                            const int32_t *slots, int32_t fixed_slot, void *out_logden, void *out_generating,
+                            uint64_t *failures, int64_t index_base, int32_t precision, issm_stream_t stream) {
+    ISSM_TRY(check_bank(bank));
+    ISSM_TRY(check_den(bank, den));
+    if (n < 0) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!x || !out_logden) return ISSM_E_NULL;
+    if (!slots && (fixed_slot < 0 || fixed_slot >= bank->count)) return ISSM_E_SIZE;
+    if (precision == ISSM_PREC_NATIVE)
+        return simt_mixture(bank, den, x, n, slots, fixed_slot, out_logden, out_generating, failures, index_base,
+                            (cudaStream_t)stream);
+    return ISSM_E_UNSUPPORTED;
+}
+
+int issm_mis_round(const issm_bank *bank, const issm_denominator *den, const int32_t *slots, const void *normals,
+                   const void *radial_normals, int32_t radial_normal_stride, const void *radial_uniforms,
+                   int32_t radial_uniform_stride, const void *logtargets, int64_t n, void *samples,
+                   void *logweights, const int64_t *proposal_ids, int64_t *proposal_ids_out, uint64_t *failures,
+                   int32_t precision, issm_stream_t stream) {
+    ISSM_TRY(check_bank(bank));
+    ISSM_TRY(check_den(bank, den));
+    if (n < 0) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!slots || !normals || !samples || !logweights) return ISSM_E_NULL;
+    if (bank->family == ISSM_STUDENT_T && !radial_normals) return ISSM_E_NULL;
+    if (precision != ISSM_PREC_NATIVE) return ISSM_E_UNSUPPORTED;
+    return simt_round(bank, den, slots, normals, radial_normals, radial_normal_stride, radial_uniforms,
+                      radial_uniform_stride, logtargets, n, samples, logweights, proposal_ids, proposal_ids_out,
+                      failures, (cudaStream_t)stream);
+}
+
+int issm_add_target_values(void *logweights, const void *values, int64_t n, int32_t dtype, uint64_t *failures,
+                           int64_t index_base, issm_stream_t stream) {
+    if (n < 0) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!logweights || !values) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return add_target_values(logweights, values, n, dtype, failures, index_base, (cudaStream_t)stream);
+}
+
+int issm_subtract_logweights(const void *logtargets, const void *logden, int64_t n, int32_t dtype,
+                             void *logweights, uint64_t *failures, int64_t index_base, issm_stream_t stream) {
+    if (n < 0) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!logtargets || !logden || !logweights) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return subtract_logweights(logtargets, logden, n, dtype, logweights, failures, index_base,
+                               (cudaStream_t)stream);
+}
+
+int issm_amis_append(const issm_bank *history, int32_t slot, const void *logcounts, const void *x, int64_t n,
+                     void *lognumerators, uint64_t *failures, int32_t precision, issm_stream_t stream) {
+    ISSM_TRY(check_bank(history));
+    if (n < 0 || slot < 0 || slot >= history->count) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!logcounts || !x || !lognumerators) return ISSM_E_NULL;
+    if (precision != ISSM_PREC_NATIVE) return ISSM_E_UNSUPPORTED;
+    return simt_append(history, slot, logcounts, x, n, lognumerators, failures, (cudaStream_t)stream);
+}
+
+int issm_amis_form(const void *logtargets, const void *lognumerators, const int64_t *round_ids, double logtotal,
+                   int64_t n, int32_t dtype, void *logweights, uint64_t *failures, issm_stream_t stream) {
+    if (n < 0) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!logtargets || !lognumerators || !logweights) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return amis_form(logtargets, lognumerators, round_ids, logtotal, n, dtype, logweights, failures,
+                     (cudaStream_t)stream);
+}
+
+size_t issm_reduce_workspace_bytes(int64_t n) { return reduce_workspace_bytes(n < 1 ? 1 : n); }
+
+int issm_logweight_summary(const void *logweights, int64_t n, int32_t dtype, double *out, void *workspace,
+                           size_t workspace_bytes, issm_stream_t stream) {
+    if (n < 1) return ISSM_E_SIZE;
+    if (!logweights || !out || !workspace) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return logweight_summary(logweights, n, dtype, out, workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+int issm_normalize(const void *logweights, int64_t n, int32_t dtype, const double *summary, void *weights,
+                   issm_stream_t stream) {
+    if (n < 1) return ISSM_E_SIZE;
+    if (!logweights || !summary || !weights) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return normalize(logweights, n, dtype, summary, weights, (cudaStream_t)stream);
+}
+
+int issm_resampling_cdf(const void *logweights, int64_t n, int32_t dtype, void *cdf, void *workspace,
+                        size_t workspace_bytes, issm_stream_t stream) {
+    if (n < 1) return ISSM_E_SIZE;
+    if (!logweights || !cdf || !workspace) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return resampling_cdf(logweights, n, dtype, cdf, workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+int issm_resample_select(const void *cdf, const void *logweights, int64_t n, const void *uniforms, int64_t count,
+                         int32_t dtype, int64_t *ancestors, issm_stream_t stream) {
+    if (n < 1 || count < 0) return ISSM_E_SIZE;
+    if (count == 0) return ISSM_OK;
+    if (!cdf || !logweights || !uniforms || !ancestors) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return resample_select(cdf, logweights, n, uniforms, count, dtype, ancestors, (cudaStream_t)stream);
+}
+
+size_t issm_resample_workspace_bytes(int64_t n) { return resample_workspace_bytes(n < 1 ? 1 : n); }
+
+int issm_resample_multinomial(const void *logweights, int64_t n, int32_t dtype, const double *uniforms,
+                              int64_t count, int64_t *ancestors, void *workspace, size_t workspace_bytes,
+                              issm_stream_t stream) {
+    if (n < 1 || count < 0 || n > ((int64_t)1 << 40)) return ISSM_E_SIZE;
+    if (!logweights || !workspace || (count > 0 && (!uniforms || !ancestors))) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return resample_fixed(logweights, n, dtype, uniforms, 0.0, 0, count, ancestors, workspace, workspace_bytes,
+                          (cudaStream_t)stream);
+}
+
+int issm_resample_systematic(const void *logweights, int64_t n, int32_t dtype, double u, int64_t count,
+                             int64_t *ancestors, void *workspace, size_t workspace_bytes, issm_stream_t stream) {
+    if (n < 1 || count < 0 || n > ((int64_t)1 << 40)) return ISSM_E_SIZE;
+    if (!(u >= 0.0 && u < 1.0)) return ISSM_E_SIZE;
+    if (!logweights || !workspace || (count > 0 && !ancestors)) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return resample_fixed(logweights, n, dtype, nullptr, u, 1, count, ancestors, workspace, workspace_bytes,
+                          (cudaStream_t)stream);
+}
+
+int issm_gather(const void *src, int32_t d, int64_t n_src, const int64_t *ancestors, int64_t count, int32_t dtype,
+                void *dst, issm_stream_t stream) {
+    if (d < 1 || n_src < 1 || count < 0) return ISSM_E_SIZE;
+    if (count == 0) return ISSM_OK;
+    if (!src || !ancestors || !dst) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return gather(src, d, n_src, ancestors, count, dtype, dst, (cudaStream_t)stream);
+}
+
+int issm_local_resample(const void *logweights, const int64_t *counts, int32_t k, const void *uniforms,
+                        const void *samples, int32_t d, int32_t dtype, int64_t *ancestors, void *destination,
+                        issm_stream_t stream) {
+    if (k < 0 || d < 1) return ISSM_E_SIZE;
+    if (k == 0) return ISSM_OK;
+    if (!logweights || !counts || !uniforms || !ancestors) return ISSM_E_NULL;
+    if (destination && !samples) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return local_resample(logweights, counts, k, uniforms, samples, d, dtype, ancestors, destination,
+                          (cudaStream_t)stream);
+}
+
+size_t issm_moments_workspace_bytes(int64_t n, int32_t d) { return moments_workspace_bytes(n < 1 ? 1 : n, d); }
+
+int issm_weighted_moments(const void *x, int32_t d, int64_t n, const void *logweights, int32_t dtype,
+                          const double *summary, const double *shift, double *mean, double *cov, void *workspace,
+                          size_t workspace_bytes, issm_stream_t stream) {
+    if (d < 1 || n < 1) return ISSM_E_SIZE;
+    if (d > 64) return ISSM_E_UNSUPPORTED;
+    if (!x || !logweights || !summary || !shift || !mean || !cov || !workspace) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return weighted_moments(x, d, n, logweights, dtype, summary, shift, mean, cov, workspace, workspace_bytes,
+                            (cudaStream_t)stream);
+}
+
+int issm_fit_factor(const double *mean, const double *cov, int32_t d, const void *previous_factor, double dof,
+                    double logconstant, int32_t dtype, void *out_location, void *out_factor,
+                    void *out_lognormalizer, uint64_t *failures, int64_t failure_index, issm_stream_t stream) {
+    if (d < 1) return ISSM_E_SIZE;
+    if (d > 64) return ISSM_E_UNSUPPORTED;
+    if (!mean || !cov || !previous_factor || !out_location || !out_factor || !out_lognormalizer)
+        return ISSM_E_NULL;
+    if (dof > 0.0 && !(dof > 2.0)) return ISSM_E_KIND;
+    ISSM_TRY(check_dtype(dtype));
+    return fit_factor(mean, cov, d, previous_factor, dof, logconstant, dtype, out_location, out_factor,
+                      out_lognormalizer, failures, failure_index, (cudaStream_t)stream);
+}
+
+int issm_target_logdensity(const issm_target *target, const void *x, int64_t n, void *out, issm_stream_t stream) {
+    if (!target) return ISSM_E_NULL;
+    if (n < 0 || target->dim < 1) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!x || !out) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(target->dtype));
+    if (target->kind < ISSM_TARGET_GAUSS_MIX || target->kind > ISSM_TARGET_QUADRATIC) return ISSM_E_KIND;
+    return target_logdensity(target, x, n, out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

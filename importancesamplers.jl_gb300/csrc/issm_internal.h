@@ -1,0 +1,72 @@
+// issm_internal.h — host-side entry points between the C ABI layer (abi.cu)
+// and the kernel translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/issm.h"
+
+namespace issm {
+
+int simt_mixture(const issm_bank *b, const issm_denominator *den, const void *x, int64_t n,
+                 const int32_t *slots, int32_t fixed_slot, void *out_logden, void *out_generating,
+                 uint64_t *failures, int64_t index_base, cudaStream_t stream);
+int simt_round(const issm_bank *b, const issm_denominator *den, const int32_t *slots, const void *normals,
+               const void *rn, int rn_stride, const void *ru, int ru_stride, const void *logtargets,
+               int64_t n, void *samples, void *logweights, const int64_t *proposal_ids,
+               int64_t *proposal_ids_out, uint64_t *failures, cudaStream_t stream);
+int simt_draw(const issm_bank *b, const int32_t *slots, int32_t fixed_slot, const void *normals,
+              const void *rn, int rn_stride, const void *ru, int ru_stride, int64_t n, void *samples,
+              uint64_t *failures, int64_t index_base, cudaStream_t stream);
+int simt_append(const issm_bank *b, int slot, const void *logcounts, const void *x, int64_t n, void *lognum,
+                uint64_t *failures, cudaStream_t stream);
+
+// reductions (reduce.cu)
+size_t reduce_workspace_bytes(int64_t n);
+int logweight_summary(const void *lw, int64_t n, int dtype, double *out, void *ws, size_t ws_bytes,
+                      cudaStream_t stream);
+int normalize(const void *lw, int64_t n, int dtype, const double *summary, void *w, cudaStream_t stream);
+int resampling_cdf(const void *lw, int64_t n, int dtype, void *cdf, void *ws, size_t ws_bytes,
+                   cudaStream_t stream);
+
+// resampling (resample.cu)
+size_t resample_workspace_bytes(int64_t n);
+int resample_select(const void *cdf, const void *lw, int64_t n, const void *u, int64_t count, int dtype,
+                    int64_t *anc, cudaStream_t stream);
+int resample_fixed(const void *lw, int64_t n, int dtype, const double *uniforms, double u, int systematic,
+                   int64_t count, int64_t *anc, void *ws, size_t ws_bytes, cudaStream_t stream);
+int gather(const void *src, int d, int64_t n_src, const int64_t *anc, int64_t count, int dtype, void *dst,
+           cudaStream_t stream);
+int local_resample(const void *lw, const int64_t *counts, int k, const void *u, const void *samples, int d,
+                   int dtype, int64_t *anc, void *dst, cudaStream_t stream);
+
+// moments and fit (moments.cu)
+size_t moments_workspace_bytes(int64_t n, int d);
+int weighted_moments(const void *x, int d, int64_t n, const void *lw, int dtype, const double *summary,
+                     const double *shift, double *mean, double *cov, void *ws, size_t ws_bytes,
+                     cudaStream_t stream);
+int fit_factor(const double *mean, const double *cov, int d, const void *prev, double dof, double logconst,
+               int dtype, void *out_loc, void *out_factor, void *out_lognorm, uint64_t *failures,
+               int64_t failure_index, cudaStream_t stream);
+
+// elementwise (elementwise.cu)
+int static_assign(const void *cdf, int k, const void *u, int64_t n, int stratified, int32_t *slots, int dtype,
+                  cudaStream_t stream);
+int add_target_values(void *lw, const void *values, int64_t n, int dtype, uint64_t *failures,
+                      int64_t index_base, cudaStream_t stream);
+int subtract_logweights(const void *lt, const void *ld, int64_t n, int dtype, void *lw, uint64_t *failures,
+                        int64_t index_base, cudaStream_t stream);
+int amis_form(const void *lt, const void *lnum, const int64_t *round_ids, double logtotal, int64_t n,
+              int dtype, void *lw, uint64_t *failures, cudaStream_t stream);
+int failure_reset(uint64_t *f, cudaStream_t stream);
+
+// built-in targets (targets.cu)
+int target_logdensity(const issm_target *t, const void *x, int64_t n, void *out, cudaStream_t stream);
+
+// random streams (rng.cu)
+int fill_normals(uint64_t seed, uint64_t offset, int64_t n, void *out, int dtype, cudaStream_t stream);
+int fill_uniforms(uint64_t seed, uint64_t offset, int64_t n, void *out, int dtype, cudaStream_t stream);
+
+}  // namespace issm

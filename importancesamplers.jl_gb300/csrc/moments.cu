@@ -1,0 +1,257 @@
+// moments.cu — weighted mean / covariance of the retained samples and the
+// FP64 candidate fit (ridge, Cholesky, Student-t scaling, lognormalizer).
+//
+// weighted_moments is a literal two-pass restatement of _weighted_moments!
+// (src/adaptive_gaussian_execution.jl:268-273): pass 1 the weighted mean about
+// `shift`, pass 2 the weighted covariance about that mean. Weights are
+// w_i = exp(l_i - max) / S from the device summary words. Each block stages a
+// tile of samples in shared memory (centred, in the sample dtype) and
+// accumulates its share of the d or d x d sums; per-block partials are summed
+// in FP64 by a second kernel. fit_factor runs in one CTA with the covariance
+// in shared memory (d <= 64).
+#include "issm_device.cuh"
+#include "issm_internal.h"
+
+namespace issm {
+
+constexpr int kMomThreads = 256;
+constexpr int kMomTile = 64;
+
+static int moment_blocks(int64_t n) {
+    int64_t b = (n + 2047) / 2048;
+    if (b > kSMs * 2) b = kSMs * 2;
+    return b < 1 ? 1 : (int)b;
+}
+
+size_t moments_workspace_bytes(int64_t n, int d) {
+    return sizeof(double) * ((size_t)moment_blocks(n) * (size_t)d * (size_t)d + (size_t)d * (size_t)d + 2 * (size_t)d + 16);
+}
+
+// pass: 0 -> partial[b][c] = sum w (x_c - shift_c); 1 -> partial[b][r + c d] = sum w z_r z_c
+template <typename T>
+__global__ void __launch_bounds__(kMomThreads) moments_partial_kernel(const T *__restrict__ x, int d, int64_t n,
+                                                                      const T *__restrict__ lw,
+                                                                      const double *__restrict__ summary,
+                                                                      const double *__restrict__ center, int pass,
+                                                                      double *__restrict__ partial) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *tile = reinterpret_cast<T *>(smem_raw);               // kMomTile x d (centred)
+    T *wt = tile + (size_t)kMomTile * d;                      // kMomTile weights
+    const T m = (T)summary[0];
+    const T inv = (T)(1.0 / summary[1]);
+    const int entries = pass == 0 ? d : d * d;
+    // each thread owns up to 16 entries of the output
+    T acc[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j] = T(0);
+    const int64_t per_block = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t lo = (int64_t)blockIdx.x * per_block;
+    const int64_t hi = min(n, lo + per_block);
+    for (int64_t t0 = lo; t0 < hi; t0 += kMomTile) {
+        const int cnt = (int)min((int64_t)kMomTile, hi - t0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < cnt * d; e += blockDim.x) {
+            const int s = e / d, c = e - s * d;
+            tile[e] = (T)((double)x[(t0 + s) * d + c] - center[c]);
+        }
+        for (int s = threadIdx.x; s < cnt; s += blockDim.x) {
+            const T w = dexp(lw[t0 + s] - m) * inv;
+            wt[s] = (pass == 1) ? w : w;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            const int e = threadIdx.x + j * kMomThreads;
+            if (e < entries) {
+                T a = acc[j];
+                if (pass == 0) {
+                    for (int s = 0; s < cnt; ++s) a += wt[s] * tile[s * d + e];
+                } else {
+                    const int r = e % d, c = e / d;
+                    for (int s = 0; s < cnt; ++s) a += wt[s] * tile[s * d + r] * tile[s * d + c];
+                }
+                acc[j] = a;
+            }
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const int e = threadIdx.x + j * kMomThreads;
+        if (e < entries) partial[(size_t)blockIdx.x * entries + e] = (double)acc[j];
+    }
+}
+
+// Sum block partials in FP64. pass 0: mean = center + S1 (weights sum to one);
+// pass 1: cov = S2 - s1 s1^T where s1 = sum w (x - mean) (nearly zero).
+__global__ void moments_finish_kernel(const double *__restrict__ partial, int blocks, int d, int pass,
+                                      const double *__restrict__ center, double *__restrict__ out,
+                                      const double *__restrict__ s1) {
+    const int entries = pass == 0 ? d : d * d;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < entries; e += gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int b = 0; b < blocks; ++b) acc += partial[(size_t)b * entries + e];
+        if (pass == 0) {
+            out[e] = center[e] + acc;
+        } else {
+            const int r = e % d, c = e / d;
+            out[e] = acc - (s1 ? s1[r] * s1[c] : 0.0);
+        }
+    }
+}
+
+// residual mean about the pass-1 mean, to correct pass 2
+__global__ void moments_residual_kernel(const double *__restrict__ partial, int blocks, int d,
+                                        double *__restrict__ s1) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d; e += gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int b = 0; b < blocks; ++b) acc += partial[(size_t)b * d + e];
+        s1[e] = acc;
+    }
+}
+
+template <typename T>
+static int moments_t(const T *x, int d, int64_t n, const T *lw, const double *summary, const double *shift,
+                     double *mean, double *cov, double *ws, cudaStream_t stream) {
+    const int blocks = moment_blocks(n);
+    double *partial = ws;
+    double *s1 = ws + (size_t)blocks * d * d;
+    const size_t smem = sizeof(T) * ((size_t)kMomTile * d + kMomTile);
+    if (d * d > 16 * kMomThreads) return ISSM_E_UNSUPPORTED;
+    auto kern = moments_partial_kernel<T>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    { kern<<<blocks, kMomThreads, smem, stream>>>(x, d, n, lw, summary, shift, 0, partial); note_launch(); }
+    { moments_finish_kernel<<<1, 256, 0, stream>>>(partial, blocks, d, 0, shift, mean, nullptr); note_launch(); }
+    { kern<<<blocks, kMomThreads, smem, stream>>>(x, d, n, lw, summary, mean, 1, partial); note_launch(); }
+    { moments_finish_kernel<<<(d * d + 255) / 256, 256, 0, stream>>>(partial, blocks, d, 1, mean, cov, nullptr); note_launch(); }
+    (void)s1;
+    return (int)cudaGetLastError();
+}
+
+int weighted_moments(const void *x, int d, int64_t n, const void *lw, int dtype, const double *summary,
+                     const double *shift, double *mean, double *cov, void *ws, size_t ws_bytes,
+                     cudaStream_t stream) {
+    if (ws_bytes < moments_workspace_bytes(n, d)) return ISSM_E_WORKSPACE;
+    if (dtype == ISSM_F32)
+        return moments_t<float>((const float *)x, d, n, (const float *)lw, summary, shift, mean, cov, (double *)ws,
+                                stream);
+    return moments_t<double>((const double *)x, d, n, (const double *)lw, summary, shift, mean, cov, (double *)ws,
+                             stream);
+}
+
+// ---- candidate fit ---------------------------------------------------------------
+// ridge = reg * tr(L_prev L_prev^T) * c_nu / d with the overflow fallback of
+// _factor_scale_aware_ridge (src/adaptive_gaussian_execution.jl:283-301);
+// right-looking Cholesky in FP64; factor *= sqrt(1/c_nu) for Student-t
+// (src/proposals.jl:73-80); zero upper triangle; lognormalizer and validity
+// (:493-528).
+template <typename T>
+__global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restrict__ mean,
+                                                         const double *__restrict__ cov, int d,
+                                                         const T *__restrict__ prev, double dof, double logconst,
+                                                         double reg, T *out_loc, T *out_factor, T *out_lognorm,
+                                                         uint64_t *failures, int64_t failure_index) {
+    extern __shared__ __align__(16) double A[];  // d x d column-major
+    __shared__ double red[256];
+    __shared__ int bad;
+    const double mult = dof > 0.0 ? dof / (dof - 2.0) : 1.0;
+    double tr = 0.0;
+    for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+        const int r = e % d, c = e / d;
+        if (r >= c) { const double v = (double)prev[e]; tr += v * v; }
+        A[e] = cov[e];
+    }
+    red[threadIdx.x] = tr;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    for (int off = 128; off > 0; off >>= 1) {
+        if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+        __syncthreads();
+    }
+    double ridge = reg * (red[0] * mult) / (double)d;
+    __syncthreads();
+    if (!isfinite(ridge)) {
+        double acc = 0.0;
+        if (reg != 0.0) {
+            const double sc = sqrt(reg) * sqrt(mult / (double)d);
+            for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+                const int r = e % d, c = e / d;
+                if (r >= c) { const double v = (double)prev[e] * sc; acc += v * v; }
+            }
+        }
+        red[threadIdx.x] = acc;
+        __syncthreads();
+        for (int off = 128; off > 0; off >>= 1) {
+            if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+            __syncthreads();
+        }
+        ridge = red[0];
+    }
+    for (int c = threadIdx.x; c < d; c += blockDim.x) A[c + c * d] += ridge;
+    __syncthreads();
+    for (int j = 0; j < d; ++j) {
+        if (threadIdx.x == 0) {
+            const double djj = A[j + j * d];
+            if (!(djj > 0.0) || !isfinite(djj)) bad = 1;
+            A[j + j * d] = sqrt(djj);
+        }
+        __syncthreads();
+        const double ljj = A[j + j * d];
+        for (int i = j + 1 + threadIdx.x; i < d; i += blockDim.x) A[i + j * d] /= ljj;
+        __syncthreads();
+        for (int e = threadIdx.x; e < (d - j - 1) * (d - j - 1); e += blockDim.x) {
+            const int i = j + 1 + e % (d - j - 1), c = j + 1 + e / (d - j - 1);
+            if (i >= c) A[i + c * d] -= A[i + j * d] * A[c + j * d];
+        }
+        __syncthreads();
+    }
+    const double f = dof > 0.0 ? sqrt(1.0 / mult) : 1.0;
+    for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+        const int r = e % d, c = e / d;
+        const double v = r >= c ? A[e] * f : 0.0;
+        out_factor[e] = (T)v;
+    }
+    for (int c = threadIdx.x; c < d; c += blockDim.x) out_loc[c] = (T)mean[c];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double logabsdet = 0.0;
+        bool valid = !bad;
+        for (int c = 0; c < d; ++c) {
+            const T lv = out_factor[c + c * d];
+            logabsdet += log(fabs((double)lv));
+            valid &= (bool)isfinite((double)out_loc[c]);
+        }
+        for (int e = 0; e < d * d; ++e) {
+            const int r = e % d, c = e / d;
+            if (r < c) continue;
+            const double v = (double)out_factor[e];
+            valid &= (bool)isfinite(v);
+            if (r == c) valid &= v > 0.0;
+        }
+        const double ln = dof > 0.0 ? logconst - logabsdet
+                                    : -0.5 * (double)d * log(2.0 * 3.14159265358979323846) - logabsdet;
+        *out_lognorm = (T)ln;
+        valid &= (bool)isfinite((double)(T)ln);
+        if (!valid) record_failure(failures, failure_index, 0, ISSM_REASON_MOMENT_FIT_INVALID);
+    }
+}
+
+int fit_factor(const double *mean, const double *cov, int d, const void *prev, double dof, double logconst,
+               int dtype, void *out_loc, void *out_factor, void *out_lognorm, uint64_t *failures,
+               int64_t failure_index, cudaStream_t stream) {
+    if (d > 64) return ISSM_E_UNSUPPORTED;
+    const size_t smem = sizeof(double) * (size_t)d * d;
+    if (dtype == ISSM_F32) {
+        const double reg = sqrt((double)FLT_EPSILON);
+        { fit_factor_kernel<float><<<1, 256, smem, stream>>>(mean, cov, d, (const float *)prev, dof, logconst, reg,
+                                                           (float *)out_loc, (float *)out_factor,
+                                                           (float *)out_lognorm, failures, failure_index); note_launch(); }
+    } else {
+        const double reg = sqrt(DBL_EPSILON);
+        { fit_factor_kernel<double><<<1, 256, smem, stream>>>(mean, cov, d, (const double *)prev, dof, logconst,
+                                                            reg, (double *)out_loc, (double *)out_factor,
+                                                            (double *)out_lognorm, failures, failure_index); note_launch(); }
+    }
+    return (int)cudaGetLastError();
+}
+
+}  // namespace issm

@@ -1,0 +1,176 @@
+// reduce.cu — log-weight reductions (HBM-bound, one read of the log weights).
+//
+// logweight_summary: single pass; each thread keeps an online (max, S, S2)
+// with S = sum exp(l - max) computed in the weight dtype and accumulated in
+// FP64; warps and blocks merge with the reference's rescaling rule
+// (_merge_logweight_moments, src/execution.jl:166-173); the last block to
+// finish merges the per-block partials, so one launch yields the final three
+// FP64 words with no host round trip.
+// resampling_cdf: exp(l - max) in the weight dtype, an FP64 three-phase scan,
+// and cdf = prefix / total rounded to the weight dtype
+// (_resampling_cdf!, src/resampling.jl:199-225).
+#include "issm_device.cuh"
+#include "issm_internal.h"
+#include "scan.cuh"
+
+namespace issm {
+
+struct Moments3 {
+    double m, s, s2;
+};
+
+__device__ __forceinline__ Moments3 merge3(Moments3 a, Moments3 b) {
+    if (a.s == 0.0) return b;
+    if (b.s == 0.0) return a;
+    double M = fmax(a.m, b.m);
+    double l = exp(a.m - M), r = exp(b.m - M);
+    return Moments3{M, l * a.s + r * b.s, (l * l) * a.s2 + (r * r) * b.s2};
+}
+
+__device__ __forceinline__ Moments3 shfl3(Moments3 v, int off) {
+    return Moments3{__shfl_down_sync(0xffffffffu, v.m, off), __shfl_down_sync(0xffffffffu, v.s, off),
+                    __shfl_down_sync(0xffffffffu, v.s2, off)};
+}
+
+__device__ Moments3 block_merge3(Moments3 v) {
+    __shared__ Moments3 warp_part[32];
+    for (int off = 16; off > 0; off >>= 1) v = merge3(v, shfl3(v, off));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_part[warp] = v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    if (warp == 0) {
+        v = lane < nw ? warp_part[lane] : Moments3{-INFINITY, 0.0, 0.0};
+        for (int off = 16; off > 0; off >>= 1) v = merge3(v, shfl3(v, off));
+    }
+    return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, int64_t n, double *out,
+                                                      Moments3 *partials, unsigned int *counter) {
+    T m = -num<T>::inf();
+    double s = 0.0, s2 = 0.0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const T l = lw[i];
+        if (l == -num<T>::inf()) continue;
+        if (l > m) {
+            if (m != -num<T>::inf()) {
+                const double r = (double)dexp(m - l);
+                s *= r;
+                s2 *= r * r;
+            }
+            m = l;
+        }
+        const double e = (double)dexp(l - m);
+        s += e;
+        s2 += e * e;
+    }
+    Moments3 v{(double)m, s, s2};
+    v = block_merge3(v);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = v;
+        __threadfence();
+        unsigned int done = atomicAdd(counter, 1u);
+        last = (done == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    Moments3 acc{-INFINITY, 0.0, 0.0};
+    const volatile double *pv = reinterpret_cast<const volatile double *>(partials);
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        acc = merge3(acc, Moments3{pv[3 * b], pv[3 * b + 1], pv[3 * b + 2]});
+    acc = block_merge3(acc);
+    if (threadIdx.x == 0) {
+        out[0] = acc.s == 0.0 ? -INFINITY : acc.m;
+        out[1] = acc.s;
+        out[2] = acc.s2;
+        *counter = 0u;
+    }
+}
+
+static int summary_blocks(int64_t n) {
+    int64_t b = (n + 256 * 8 - 1) / (256 * 8);
+    if (b > kSMs * 8) b = kSMs * 8;
+    return b < 1 ? 1 : (int)b;
+}
+
+// Workspace layout shared by the summary and the CDF:
+//   [0, 4)      completion counter of the summary kernel
+//   [128, 152)  summary words written by resampling_cdf
+//   [256, ...)  per-block summary partials, later reused as scan tile sums
+size_t reduce_workspace_bytes(int64_t n) {
+    size_t a = sizeof(Moments3) * (size_t)(kSMs * 8);
+    size_t tiles = (size_t)((n + kScanTile - 1) / kScanTile) + 1;
+    size_t b = sizeof(double) * tiles;
+    return 256 + (a > b ? a : b);
+}
+
+static int summary_launch(const void *lw, int64_t n, int dtype, double *out, void *ws, cudaStream_t stream) {
+    unsigned int *counter = (unsigned int *)ws;
+    Moments3 *partials = (Moments3 *)((char *)ws + 256);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), stream);
+    if (e != cudaSuccess) return (int)e;
+    const int blocks = summary_blocks(n);
+    if (dtype == ISSM_F32)
+        { summary_kernel<float><<<blocks, 256, 0, stream>>>((const float *)lw, n, out, partials, counter); note_launch(); }
+    else
+        { summary_kernel<double><<<blocks, 256, 0, stream>>>((const double *)lw, n, out, partials, counter); note_launch(); }
+    return (int)cudaGetLastError();
+}
+
+int logweight_summary(const void *lw, int64_t n, int dtype, double *out, void *ws, size_t ws_bytes,
+                      cudaStream_t stream) {
+    if (ws_bytes < reduce_workspace_bytes(n)) return ISSM_E_WORKSPACE;
+    return summary_launch(lw, n, dtype, out, ws, stream);
+}
+
+template <typename T>
+__global__ void normalize_kernel(const T *__restrict__ lw, int64_t n, const double *__restrict__ summary,
+                                 T *__restrict__ w) {
+    const T m = (T)summary[0];
+    const T inv = (T)(1.0 / summary[1]);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        w[i] = dexp(lw[i] - m) * inv;
+}
+
+int normalize(const void *lw, int64_t n, int dtype, const double *summary, void *w, cudaStream_t stream) {
+    const int blocks = grid_for(n, 256, 4);
+    if (dtype == ISSM_F32)
+        { normalize_kernel<float><<<blocks, 256, 0, stream>>>((const float *)lw, n, summary, (float *)w); note_launch(); }
+    else
+        { normalize_kernel<double><<<blocks, 256, 0, stream>>>((const double *)lw, n, summary, (double *)w); note_launch(); }
+    return (int)cudaGetLastError();
+}
+
+// ---- reference-compatible CDF ------------------------------------------------
+template <typename T> struct ExpWeight {
+    const T *lw;
+    const double *summary;
+    __device__ double operator()(int64_t i) const { return (double)dexp(lw[i] - (T)summary[0]); }
+};
+
+template <typename T> struct CdfWrite {
+    T *cdf;
+    __device__ void operator()(int64_t i, double prefix, double total) const { cdf[i] = (T)(prefix / total); }
+};
+
+int resampling_cdf(const void *lw, int64_t n, int dtype, void *cdf, void *ws, size_t ws_bytes,
+                   cudaStream_t stream) {
+    if (ws_bytes < reduce_workspace_bytes(n)) return ISSM_E_WORKSPACE;
+    double *summary = (double *)((char *)ws + 128);
+    int st = summary_launch(lw, n, dtype, summary, ws, stream);
+    if (st) return st;
+    double *scan_ws = (double *)((char *)ws + 256);
+    if (dtype == ISSM_F32)
+        return scan_apply<double>(n, ExpWeight<float>{(const float *)lw, summary}, CdfWrite<float>{(float *)cdf},
+                                  scan_ws, stream);
+    return scan_apply<double>(n, ExpWeight<double>{(const double *)lw, summary}, CdfWrite<double>{(double *)cdf},
+                              scan_ws, stream);
+}
+
+}  // namespace issm

@@ -1,0 +1,173 @@
+"""ctypes binding of libissm103.so (include/issm.h).
+
+This is the only route from Python to the GPU kernels. There is no CPU
+fallback: if the library or a CUDA device is missing, `require()` raises.
+Tensors are passed as raw device pointers; the current torch stream is used
+unless a stream is given.
+"""
+import ctypes as C
+import os
+
+import torch
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBRARY = os.path.join(HERE, "libissm103.so")
+
+F32, F64 = 0, 1
+GAUSSIAN, STUDENT_T = 0, 1
+SCALE_FACTOR, SCALE_DIAGONAL, SCALE_SPHERICAL = 0, 1, 2
+DENOM_FULL, DENOM_GENERATING, DENOM_PARTIAL, DENOM_PREFIX = 0, 1, 2, 3
+PREC_NATIVE, PREC_TF32, PREC_BF16 = 0, 1, 2
+
+REASON_TARGET_NAN = 0x0100
+REASON_TARGET_POS_INF = 0x0200
+REASON_PROPOSAL_INVALID = 0x0400
+REASON_GENERATED_NONFINITE = 0x0800
+REASON_LOGWEIGHT_INVALID = 0x1000
+REASON_DRAW_EXHAUSTED = 0x0010
+REASON_MOMENT_FIT_INVALID = 0x2000
+
+E_ALL_ZERO = -5
+
+
+class NativeError(RuntimeError):
+    def __init__(self, status, where):
+        self.status = status
+        msg = _lib.issm_status_string(status).decode() if _lib is not None else str(status)
+        super().__init__(f"{where}: {msg} (status {status})")
+
+
+class Bank(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("count", C.c_int32), ("family", C.c_int32),
+                ("scale_kind", C.c_int32), ("dtype", C.c_int32), ("reserved", C.c_int32),
+                ("locations", C.c_void_p), ("scales", C.c_void_p), ("lognormalizers", C.c_void_p),
+                ("dofs", C.c_void_p), ("range_risk", C.c_void_p)]
+
+
+class Denominator(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("terms", C.c_int32), ("logcoefficients", C.c_void_p),
+                ("group_of_slot", C.c_void_p)]
+
+
+class Target(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("dim", C.c_int32), ("count", C.c_int32), ("dtype", C.c_int32),
+                ("a", C.c_void_p), ("b", C.c_void_p), ("c", C.c_void_p), ("p0", C.c_double), ("p1", C.c_double)]
+
+
+TARGET_GAUSS_MIX, TARGET_STUDENT_T, TARGET_LINREG, TARGET_LOGISTIC, TARGET_STD_NORMAL, TARGET_QUADRATIC = range(6)
+
+# (name, restype, argtypes) for every entry point of include/issm.h
+_p, _i32, _i64, _u64, _d, _sz = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_double, C.c_size_t
+_bank, _den = C.POINTER(Bank), C.POINTER(Denominator)
+SIGNATURES = [
+    ("issm_version", C.c_char_p, []),
+    ("issm_status_string", C.c_char_p, [C.c_int]),
+    ("issm_kernel_launches", C.c_uint64, []),
+    ("issm_failure_reset", C.c_int, [_p, _p]),
+    ("issm_fill_normals", C.c_int, [_u64, _u64, _i64, _p, _i32, _p]),
+    ("issm_fill_uniforms", C.c_int, [_u64, _u64, _i64, _p, _i32, _p]),
+    ("issm_static_assign", C.c_int, [_p, _i32, _p, _i64, _i32, _p, _i32, _p]),
+    ("issm_draw", C.c_int, [_bank, _p, _i32, _p, _p, _i32, _p, _i32, _i64, _p, _p, _i64, _p]),
+    ("issm_mixture_logdensity", C.c_int, [_bank, _den, _p, _i64, _p, _i32, _p, _p, _p, _i64, _i32, _p]),
+    ("issm_mis_round", C.c_int, [_bank, _den, _p, _p, _p, _i32, _p, _i32, _p, _i64, _p, _p, _p, _p, _p,
+                                 _i32, _p]),
+    ("issm_add_target_values", C.c_int, [_p, _p, _i64, _i32, _p, _i64, _p]),
+    ("issm_subtract_logweights", C.c_int, [_p, _p, _i64, _i32, _p, _p, _i64, _p]),
+    ("issm_amis_append", C.c_int, [_bank, _i32, _p, _p, _i64, _p, _p, _i32, _p]),
+    ("issm_amis_form", C.c_int, [_p, _p, _p, _d, _i64, _i32, _p, _p, _p]),
+    ("issm_reduce_workspace_bytes", _sz, [_i64]),
+    ("issm_logweight_summary", C.c_int, [_p, _i64, _i32, _p, _p, _sz, _p]),
+    ("issm_normalize", C.c_int, [_p, _i64, _i32, _p, _p, _p]),
+    ("issm_resampling_cdf", C.c_int, [_p, _i64, _i32, _p, _p, _sz, _p]),
+    ("issm_resample_select", C.c_int, [_p, _p, _i64, _p, _i64, _i32, _p, _p]),
+    ("issm_resample_workspace_bytes", _sz, [_i64]),
+    ("issm_resample_multinomial", C.c_int, [_p, _i64, _i32, _p, _i64, _p, _p, _sz, _p]),
+    ("issm_resample_systematic", C.c_int, [_p, _i64, _i32, _d, _i64, _p, _p, _sz, _p]),
+    ("issm_gather", C.c_int, [_p, _i32, _i64, _p, _i64, _i32, _p, _p]),
+    ("issm_local_resample", C.c_int, [_p, _p, _i32, _p, _p, _i32, _i32, _p, _p, _p]),
+    ("issm_moments_workspace_bytes", _sz, [_i64, _i32]),
+    ("issm_weighted_moments", C.c_int, [_p, _i32, _i64, _p, _i32, _p, _p, _p, _p, _p, _sz, _p]),
+    ("issm_fit_factor", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _p, _p, _p, _p, _i64, _p]),
+    ("issm_target_logdensity", C.c_int, [C.POINTER(Target), _p, _i64, _p, _p]),
+]
+
+_lib = None
+
+
+def library_path():
+    return LIBRARY
+
+
+def load():
+    """Load libissm103.so and declare every entry point (raises if absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIBRARY):
+        raise RuntimeError(
+            f"libissm103.so is not built at {LIBRARY}; run __graft_entry__.build() (needs nvcc)")
+    lib = C.CDLL(LIBRARY)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def require():
+    """Fail loudly unless the native library and a CUDA device are usable."""
+    load()
+    if not torch.cuda.is_available():
+        raise RuntimeError("a CUDA device is required: the importance-sampling path has no CPU fallback")
+
+
+def lib():
+    return load()
+
+
+def dtype_code(dtype):
+    if dtype == torch.float32:
+        return F32
+    if dtype == torch.float64:
+        return F64
+    raise TypeError(f"unsupported dtype {dtype}; use float32 or float64")
+
+
+def ptr(t):
+    if t is None:
+        return None
+    if isinstance(t, int):
+        return t
+    return t.data_ptr()
+
+
+def stream_ptr(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def check(status, where):
+    if status != 0:
+        raise NativeError(status, where)
+
+
+def call(name, *args):
+    fn = getattr(lib(), name)
+    st = fn(*args)
+    check(st, name)
+    return st
+
+
+_workspaces = {}
+
+
+def workspace(nbytes, device=None, tag="default"):
+    """A cached device scratch buffer of at least nbytes (per device, per tag)."""
+    device = device or torch.device("cuda", torch.cuda.current_device())
+    key = (str(device), tag)
+    buf = _workspaces.get(key)
+    if buf is None or buf.numel() < nbytes:
+        buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+        _workspaces[key] = buf
+    return buf

@@ -1,0 +1,230 @@
+"""Tensor-level wrappers over the C ABI: each function takes torch CUDA
+tensors, checks shapes, and calls one libissm103.so entry point on the current
+stream. Results stay on the device."""
+import ctypes
+
+import torch
+
+from . import native
+
+_U = native
+
+
+def _dt(t):
+    return native.dtype_code(t.dtype)
+
+
+def _s(stream=None):
+    return native.stream_ptr(stream)
+
+
+def new_failures(device):
+    return torch.zeros(3, dtype=torch.int64, device=device)
+
+
+def denominator(kind, coef=None, terms=0, groups=None):
+    d = native.Denominator(kind, int(terms), native.ptr(coef), native.ptr(groups))
+    d._keep = (coef, groups)
+    return d
+
+
+def fill_normals(n, dtype, device, seed, offset=0, out=None):
+    out = torch.empty(int(n), dtype=dtype, device=device) if out is None else out
+    native.call("issm_fill_normals", int(seed) & (2 ** 64 - 1), int(offset), int(n), native.ptr(out),
+                native.dtype_code(dtype), _s())
+    return out
+
+
+def fill_uniforms(n, dtype, device, seed, offset=0, out=None):
+    out = torch.empty(int(n), dtype=dtype, device=device) if out is None else out
+    native.call("issm_fill_uniforms", int(seed) & (2 ** 64 - 1), int(offset), int(n), native.ptr(out),
+                native.dtype_code(dtype), _s())
+    return out
+
+
+def static_assign(cdf, uniforms, stratified=True, out=None):
+    n = uniforms.numel()
+    out = torch.empty(n, dtype=torch.int32, device=uniforms.device) if out is None else out
+    native.call("issm_static_assign", native.ptr(cdf), cdf.numel(), native.ptr(uniforms), n, int(stratified),
+                native.ptr(out), _dt(cdf), _s())
+    return out
+
+
+def draw(bank, normals, n, slots=None, fixed_slot=0, radial_normals=None, rn_stride=0, radial_uniforms=None,
+         ru_stride=0, failures=None, index_base=0, out=None, bank_ref=None):
+    out = torch.empty(int(n), bank.d, dtype=bank.dtype, device=normals.device) if out is None else out
+    native.call("issm_draw", bank_ref or bank.ref(), native.ptr(slots), int(fixed_slot), native.ptr(normals),
+                native.ptr(radial_normals), int(rn_stride), native.ptr(radial_uniforms), int(ru_stride), int(n),
+                native.ptr(out), native.ptr(failures), int(index_base), _s())
+    return out
+
+
+def mixture_logdensity(bank, den, x, slots=None, fixed_slot=0, failures=None, generating=False, index_base=0,
+                       precision=native.PREC_NATIVE, out=None, bank_ref=None):
+    n = x.shape[0]
+    out = torch.empty(n, dtype=bank.dtype, device=x.device) if out is None else out
+    gen = torch.empty(n, dtype=bank.dtype, device=x.device) if generating else None
+    native.call("issm_mixture_logdensity", bank_ref or bank.ref(), ctypes.byref(den), native.ptr(x), n,
+                native.ptr(slots), int(fixed_slot), native.ptr(out), native.ptr(gen), native.ptr(failures),
+                int(index_base), int(precision), _s())
+    return (out, gen) if generating else out
+
+
+def mis_round(bank, den, slots, normals, logtargets=None, radial_normals=None, rn_stride=0, radial_uniforms=None,
+              ru_stride=0, failures=None, precision=native.PREC_NATIVE, samples=None, logweights=None,
+              proposal_ids_out=None):
+    n = slots.numel()
+    dev = slots.device
+    samples = torch.empty(n, bank.d, dtype=bank.dtype, device=dev) if samples is None else samples
+    logweights = torch.empty(n, dtype=bank.dtype, device=dev) if logweights is None else logweights
+    pid = torch.empty(n, dtype=torch.int64, device=dev) if proposal_ids_out is None else proposal_ids_out
+    native.call("issm_mis_round", bank.ref(), ctypes.byref(den), native.ptr(slots), native.ptr(normals),
+                native.ptr(radial_normals), int(rn_stride), native.ptr(radial_uniforms), int(ru_stride),
+                native.ptr(logtargets), n, native.ptr(samples), native.ptr(logweights),
+                native.ptr(bank.proposal_ids), native.ptr(pid), native.ptr(failures), int(precision), _s())
+    return samples, logweights, pid
+
+
+def add_target_values(logweights, values, failures=None, index_base=0):
+    native.call("issm_add_target_values", native.ptr(logweights), native.ptr(values), logweights.numel(),
+                _dt(logweights), native.ptr(failures), int(index_base), _s())
+    return logweights
+
+
+def subtract_logweights(logtargets, logden, failures=None, index_base=0, out=None):
+    out = torch.empty_like(logtargets) if out is None else out
+    native.call("issm_subtract_logweights", native.ptr(logtargets), native.ptr(logden), logtargets.numel(),
+                _dt(logtargets), native.ptr(out), native.ptr(failures), int(index_base), _s())
+    return out
+
+
+def amis_append(history_ref, slot, logcounts, x, lognum, failures=None, precision=native.PREC_NATIVE):
+    native.call("issm_amis_append", history_ref, int(slot), native.ptr(logcounts), native.ptr(x), x.shape[0],
+                native.ptr(lognum), native.ptr(failures), int(precision), _s())
+    return lognum
+
+
+def amis_form(logtargets, lognum, logtotal, logweights, round_ids=None, failures=None):
+    native.call("issm_amis_form", native.ptr(logtargets), native.ptr(lognum), native.ptr(round_ids),
+                float(logtotal), logtargets.numel(), _dt(logtargets), native.ptr(logweights), native.ptr(failures),
+                _s())
+    return logweights
+
+
+def logweight_summary(logweights, out=None):
+    n = logweights.numel()
+    out = torch.empty(3, dtype=torch.float64, device=logweights.device) if out is None else out
+    nb = native.lib().issm_reduce_workspace_bytes(n)
+    ws = native.workspace(nb, logweights.device, "reduce")
+    native.call("issm_logweight_summary", native.ptr(logweights), n, _dt(logweights), native.ptr(out),
+                native.ptr(ws), ws.numel(), _s())
+    return out
+
+
+def normalize(logweights, summary, out=None):
+    out = torch.empty_like(logweights) if out is None else out
+    native.call("issm_normalize", native.ptr(logweights), logweights.numel(), _dt(logweights), native.ptr(summary),
+                native.ptr(out), _s())
+    return out
+
+
+def resampling_cdf(logweights, out=None):
+    n = logweights.numel()
+    out = torch.empty_like(logweights) if out is None else out
+    nb = native.lib().issm_reduce_workspace_bytes(n)
+    ws = native.workspace(nb, logweights.device, "cdf")
+    native.call("issm_resampling_cdf", native.ptr(logweights), n, _dt(logweights), native.ptr(out), native.ptr(ws),
+                ws.numel(), _s())
+    return out
+
+
+def resample_select(cdf, logweights, uniforms, out=None):
+    count = uniforms.numel()
+    out = torch.empty(count, dtype=torch.int64, device=cdf.device) if out is None else out
+    native.call("issm_resample_select", native.ptr(cdf), native.ptr(logweights), cdf.numel(), native.ptr(uniforms),
+                count, _dt(cdf), native.ptr(out), _s())
+    return out
+
+
+def resample_multinomial(logweights, uniforms, out=None):
+    n = logweights.numel()
+    count = uniforms.numel()
+    out = torch.empty(count, dtype=torch.int64, device=logweights.device) if out is None else out
+    nb = native.lib().issm_resample_workspace_bytes(n)
+    ws = native.workspace(nb, logweights.device, "resample")
+    native.call("issm_resample_multinomial", native.ptr(logweights), n, _dt(logweights), native.ptr(uniforms),
+                count, native.ptr(out), native.ptr(ws), ws.numel(), _s())
+    return out
+
+
+def resample_systematic(logweights, u, count, out=None):
+    n = logweights.numel()
+    out = torch.empty(int(count), dtype=torch.int64, device=logweights.device) if out is None else out
+    nb = native.lib().issm_resample_workspace_bytes(n)
+    ws = native.workspace(nb, logweights.device, "resample")
+    native.call("issm_resample_systematic", native.ptr(logweights), n, _dt(logweights), float(u), int(count),
+                native.ptr(out), native.ptr(ws), ws.numel(), _s())
+    return out
+
+
+def gather(src, ancestors, out=None):
+    d = src.shape[1] if src.dim() == 2 else 1
+    count = ancestors.numel()
+    shape = (count, d) if src.dim() == 2 else (count,)
+    out = torch.empty(shape, dtype=src.dtype, device=src.device) if out is None else out
+    native.call("issm_gather", native.ptr(src), d, src.shape[0], native.ptr(ancestors), count, _dt(src),
+                native.ptr(out), _s())
+    return out
+
+
+def local_resample(logweights, counts, uniforms, samples=None, ancestors=None, destination=None):
+    k = counts.numel()
+    d = samples.shape[1] if samples is not None else 1
+    anc = torch.empty(k, dtype=torch.int64, device=logweights.device) if ancestors is None else ancestors
+    if samples is not None and destination is None:
+        destination = torch.empty(k, d, dtype=samples.dtype, device=samples.device)
+    native.call("issm_local_resample", native.ptr(logweights), native.ptr(counts), k, native.ptr(uniforms),
+                native.ptr(samples), d, _dt(logweights), native.ptr(anc), native.ptr(destination), _s())
+    return anc, destination
+
+
+def weighted_moments(x, logweights, summary, shift, mean=None, cov=None):
+    n, d = x.shape
+    dev = x.device
+    mean = torch.empty(d, dtype=torch.float64, device=dev) if mean is None else mean
+    cov = torch.empty(d, d, dtype=torch.float64, device=dev) if cov is None else cov
+    nb = native.lib().issm_moments_workspace_bytes(n, d)
+    ws = native.workspace(nb, dev, "moments")
+    native.call("issm_weighted_moments", native.ptr(x), d, n, native.ptr(logweights), _dt(x), native.ptr(summary),
+                native.ptr(shift), native.ptr(mean), native.ptr(cov), native.ptr(ws), ws.numel(), _s())
+    return mean, cov
+
+
+def fit_factor(mean, cov, previous_factor, out_location, out_factor, out_lognorm, dof=0.0, logconstant=0.0,
+               failures=None, failure_index=0):
+    d = mean.numel()
+    native.call("issm_fit_factor", native.ptr(mean), native.ptr(cov), d, native.ptr(previous_factor), float(dof),
+                float(logconstant), _dt(out_factor), native.ptr(out_location), native.ptr(out_factor),
+                native.ptr(out_lognorm), native.ptr(failures), int(failure_index), _s())
+
+
+def target_logdensity(target_struct, x, out=None):
+    n = x.shape[0]
+    out = torch.empty(n, dtype=x.dtype, device=x.device) if out is None else out
+    native.call("issm_target_logdensity", ctypes.byref(target_struct), native.ptr(x), n, native.ptr(out), _s())
+    return out
+
+
+def decode_failure(words):
+    """_decode_native_failure (src/execution.jl:701-717) on the 3-word record."""
+    w = [int(v) & (2 ** 64 - 1) for v in words]
+
+    def dec(count, packed):
+        if count == 0:
+            return dict(count=0, first_logical_index=0, first_block=0, reason_bits=0)
+        inv_index = (packed >> 32) & 0xFFFFFFFF
+        inv_block = (packed >> 16) & 0xFFFF
+        return dict(count=count, first_logical_index=(0xFFFFFFFF - inv_index + 1) & 0xFFFFFFFF,
+                    first_block=(0xFFFF - inv_block + 1) & 0xFFFF, reason_bits=packed & 0xFFFF)
+
+    return dec(w[0], w[1]), dec(1 if w[2] else 0, w[2])

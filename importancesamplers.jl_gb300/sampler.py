@@ -1,0 +1,465 @@
+"""prepare_sampler / importance_sample! / importance_sample
+(src/methods/importance_sampling.jl:357-440, 857-935).
+
+A prepared sampler owns every device buffer of its method, its counter-based
+random stream and per-round failure records. A whole call is a host-driven
+sequence of stream-ordered launches with no synchronisation until the end,
+where the per-round summaries and failure words are read back in one copy.
+The reference instead synchronises after nearly every launch
+(src/mis_execution.jl:840) and reads scalars every round.
+"""
+import math
+from fractions import Fraction
+
+import numpy as np
+import torch
+
+from . import native, ops
+from .bank import DeviceHistory, pack
+from .methods import (AMIS, NPMC, DeterministicMixturePMC, GlobalResampling, ImportanceSampling, LocalResampling,
+                      PartialDeterministicMixture, RandomMixture, StandardMIS)
+from .proposals import STUDENT_T
+from .results import (AMISRoundError, DMPMCRoundError, NPMCRoundError, SamplerExecutionError, WeightedSamples,
+                      phase_of)
+
+GAMMA_DRAW_ATTEMPTS = 8
+
+
+class SamplerBusyError(RuntimeError):
+    """A prepared sampler is non-reentrant (src/methods/importance_sampling.jl:105-116)."""
+
+
+def _radial_strides(dofs):
+    """_radial_normal_stride / _radial_uniform_stride over a packed family
+    (src/proposal_banks.jl:205-223)."""
+    if dofs is None:
+        return 0, 0
+    rn = max(1 if float(v) == 1.0 else GAMMA_DRAW_ATTEMPTS for v in dofs)
+    ru = max(0 if float(v) == 1.0 else GAMMA_DRAW_ATTEMPTS + (1 if float(v) < 2 else 0) for v in dofs)
+    return rn, ru
+
+
+def compile_partial_denominator(bank, ids, logmasses, groups):
+    """_compile_partial_denominator (src/methods/static_mis.jl:241-303):
+    group id per active slot and each member's log mass within its group."""
+    nprop = len(bank.proposals)
+    seen = [False] * nprop
+    slot_of = {pid: s for s, pid in enumerate(ids)}
+    group_of_slot = [0] * len(ids)
+    coef = np.zeros(len(ids), dtype=logmasses.dtype)
+    g = 0
+    for group in groups:
+        if len(group) == 0:
+            raise ValueError("partial-MIS groups cannot be empty")
+        members = []
+        for pid in group:
+            if isinstance(pid, bool) or not isinstance(pid, (int, np.integer)):
+                raise ValueError("partial-MIS proposal IDs must be integers")
+            if not 1 <= pid <= nprop:
+                raise ValueError(f"partial-MIS proposal ID {pid} is out of range")
+            if seen[pid - 1]:
+                raise ValueError(f"partial-MIS proposal ID {pid} appears more than once")
+            seen[pid - 1] = True
+            if pid in slot_of:
+                members.append(slot_of[pid])
+        if not members:
+            continue
+        g += 1
+        lm = [float(logmasses[s]) for s in members]
+        mx = max(lm)
+        glog = mx + math.log(sum(math.exp(v - mx) for v in lm))
+        for s in members:
+            group_of_slot[s] = g
+            coef[s] = logmasses[s] - logmasses.dtype.type(glog)
+    if not all(seen):
+        raise ValueError("partial-MIS groups must include every proposal ID exactly once")
+    return np.array(group_of_slot, dtype=np.int32), coef
+
+
+def deterministic_allocation_plan(active_masses, schedule):
+    """_deterministic_allocation_plan (src/population_preparation.jl:266-367):
+    exact largest-remainder counts with rotating tie order, contiguous
+    assignments per slot, and log(count / round_size) coefficients."""
+    exact = [Fraction(float(m)) for m in active_masses]
+    total = sum(exact)
+    exact = [m / total for m in exact]
+    k = len(exact)
+    rounds = len(schedule)
+    counts = np.zeros((k, rounds), dtype=np.int64)
+    for r, size in enumerate(schedule):
+        quota = [m * size for m in exact]
+        c = [math.floor(q) for q in quota]
+        rem = [q - f for q, f in zip(quota, c)]
+        remaining = size - sum(c)
+        if not 0 <= remaining < k:
+            raise RuntimeError("invalid DM-PMC allocation remainder")
+        first_tie = r % k  # mod1(round, K) with 1-based rounds -> 0-based slot r % K
+        order = sorted(range(k), key=lambda s: (-rem[s], (s - first_tie) % k))
+        for s in order[:remaining]:
+            c[s] += 1
+        if not all(v > 0 for v in c):
+            raise ValueError(f"round {r + 1} of size {size} cannot allocate at least one sample to every "
+                             "positive-mass proposal")
+        counts[:, r] = c
+    offsets = np.concatenate([[0], np.cumsum(schedule)])
+    return counts, offsets
+
+
+class _Span:
+    """CUDA events around one launch group on the current stream (profiling)."""
+
+    def __init__(self, sampler, name, nbytes):
+        self.sampler, self.name, self.nbytes = sampler, name, nbytes
+
+    def __enter__(self):
+        if self.sampler.profile is not None:
+            self.start = torch.cuda.Event(enable_timing=True)
+            self.start.record()
+        return self
+
+    def __exit__(self, *exc):
+        if self.sampler.profile is not None:
+            end = torch.cuda.Event(enable_timing=True)
+            end.record()
+            self.sampler.profile.append((self.name, self.start, end, self.nbytes))
+        return False
+
+
+class PreparedSampler:
+    def __init__(self, seed, target, algorithm, device, precision):
+        self.profile = None  # list of (name, start, end, algorithmic bytes) when profiling
+        self.seed = int(seed) & (2 ** 64 - 1)
+        self.offset = 0
+        self.target = target
+        self.algorithm = algorithm
+        self.device = device
+        self.precision = precision
+        self.busy = False
+        self.calls = 0
+
+    # counter-based stream: disjoint (seed, offset) ranges per draw
+    def normals(self, n, dtype):
+        out = ops.fill_normals(n, dtype, self.device, self.seed, self.offset)
+        self.offset += int(n) + 8
+        return out
+
+    def uniforms(self, n, dtype):
+        out = ops.fill_uniforms(n, dtype, self.device, self.seed, self.offset)
+        self.offset += int(n) + 8
+        return out
+
+
+def prepare_sampler(seed, target, algorithm, device="cuda", precision=native.PREC_NATIVE):
+    """prepare_sampler(rng, logtarget, alg) with the device applied: packs the
+    proposal(s) and allocates every buffer on the device."""
+    native.require()
+    device = torch.device(device)
+    s = PreparedSampler(seed, target, algorithm, device, precision)
+    if isinstance(algorithm, ImportanceSampling):
+        _prepare_static(s)
+    elif isinstance(algorithm, (AMIS, NPMC)):
+        _prepare_moment(s)
+    elif isinstance(algorithm, DeterministicMixturePMC):
+        _prepare_dmpmc(s)
+    else:
+        raise TypeError(f"{type(algorithm).__name__} is not supported")
+    return s
+
+
+def importance_sample_(sampler):
+    """importance_sample!(sampler): one complete run; raises on failures."""
+    if sampler.busy:
+        raise SamplerBusyError("prepared sampler is already running")
+    sampler.busy = True
+    try:
+        alg = sampler.algorithm
+        if isinstance(alg, ImportanceSampling):
+            return _run_static(sampler)
+        if isinstance(alg, (AMIS, NPMC)):
+            return _run_moment(sampler)
+        return _run_dmpmc(sampler)
+    finally:
+        sampler.busy = False
+        sampler.calls += 1
+
+
+def importance_sample(seed, target, algorithm, device="cuda", precision=native.PREC_NATIVE):
+    return importance_sample_(prepare_sampler(seed, target, algorithm, device, precision))
+
+
+# ---- static MIS ------------------------------------------------------------------
+def _prepare_static(s):
+    alg = s.algorithm
+    db = pack(alg.bank, s.device)
+    s.bank = db
+    s.dtype = db.dtype
+    scheme = alg.mis_scheme
+    if isinstance(scheme, StandardMIS):
+        s.den = ops.denominator(native.DENOM_GENERATING)
+    elif isinstance(scheme, PartialDeterministicMixture):
+        grp, coef = compile_partial_denominator(alg.bank, db.host_ids, db.host_logmasses, scheme.groups)
+        s.den = ops.denominator(native.DENOM_PARTIAL, torch.tensor(coef, device=s.device),
+                                groups=torch.tensor(grp, device=s.device))
+    else:
+        s.den = ops.denominator(native.DENOM_FULL, db.logmasses)
+    s.stratified = not isinstance(scheme, RandomMixture)
+    dofs = None if db.dofs is None else db.dofs.cpu().numpy()
+    s.rn_stride, s.ru_stride = _radial_strides(dofs)
+    s.bound_target = s.target.bind(s.device, db.dtype)
+
+
+def _raise_failures(words, error=None, rnd=None):
+    fail, _ = ops.decode_failure(words)
+    if fail["count"] == 0:
+        return
+    cause = SamplerExecutionError(phase_of(fail["reason_bits"]), fail["first_logical_index"], fail["reason_bits"],
+                                  fail["count"])
+    if error is None:
+        raise cause
+    raise error(rnd, cause.phase, cause)
+
+
+def _radial_buffers(s, n, dtype):
+    rn = s.normals(n * s.rn_stride, dtype) if s.rn_stride else None
+    ru = s.uniforms(n * s.ru_stride, dtype) if s.ru_stride else None
+    return rn, ru
+
+
+def _run_static(s):
+    alg, db = s.algorithm, s.bank
+    n, d, dt = alg.nsamples, db.d, db.dtype
+    fail = ops.new_failures(s.device)
+    u = s.uniforms(n, dt)
+    slots = ops.static_assign(db.cdf, u, s.stratified)
+    normals = s.normals(n * d, dt)
+    rn, ru = _radial_buffers(s, n, dt)
+    samples, lw, pid = ops.mis_round(db, s.den, slots, normals, None, rn, s.rn_stride, ru, s.ru_stride, fail,
+                                     s.precision)
+    values = s.bound_target.evaluate(samples)
+    ops.add_target_values(lw, values, fail)
+    _raise_failures(fail.cpu().numpy())
+    scheme = type(alg.mis_scheme).__name__
+    return WeightedSamples(samples, lw, provenance={"proposal_id": pid},
+                           diagnostics={"method": "importance_sampling", "mis_scheme": scheme,
+                                        "nsamples": n, "failures": 0})
+
+
+# ---- AMIS / NPMC ------------------------------------------------------------------
+def _prepare_moment(s):
+    alg = s.algorithm
+    p = alg.proposal
+    s.proposal = p
+    s.dtype = torch.float32 if p.dtype == np.float32 else torch.float64
+    s.rounds = alg.rounds
+    s.schedule = list(alg.round_size)
+    s.offsets = np.concatenate([[0], np.cumsum(s.schedule)])
+    s.history = DeviceHistory.allocate(p, s.rounds, s.device)
+    s.logcounts = torch.tensor(np.log(np.array(s.schedule, dtype=np.float64)), dtype=s.dtype, device=s.device)
+    total = int(s.offsets[-1])
+    d = p.dimension
+    dev, dt = s.device, s.dtype
+    s.samples = torch.empty(total, d, dtype=dt, device=dev)
+    s.logtargets = torch.empty(total, dtype=dt, device=dev)
+    s.lognum = torch.empty(total, dtype=dt, device=dev)
+    s.logweights = torch.empty(total, dtype=dt, device=dev)
+    s.summaries = torch.zeros(s.rounds, 3, dtype=torch.float64, device=dev)
+    s.round_failures = torch.zeros(s.rounds, 3, dtype=torch.int64, device=dev)
+    s.mean = torch.zeros(d, dtype=torch.float64, device=dev)
+    s.cov = torch.zeros(d, d, dtype=torch.float64, device=dev)
+    s.shift = torch.zeros(d, dtype=torch.float64, device=dev)
+    s.cand_loc = torch.zeros(d, dtype=dt, device=dev)
+    s.cand_factor = torch.zeros(d, d, dtype=dt, device=dev)
+    s.cand_lognorm = torch.zeros(1, dtype=dt, device=dev)
+    s.committed = (s.history.locations[0].clone(), s.history.scales[0].clone(), s.history.lognormalizers[0].clone())
+    dofs = None if p.family != STUDENT_T else [float(p.dof)]
+    s.rn_stride, s.ru_stride = _radial_strides(dofs)
+    s.bound_target = s.target.bind(s.device, dt)
+    s.round_ids = torch.repeat_interleave(torch.arange(1, s.rounds + 1, device=dev),
+                                          torch.tensor(s.schedule, device=dev))
+
+
+def _run_moment(s):
+    is_npmc = isinstance(s.algorithm, NPMC)
+    h = s.history
+    d, dt = h.d, h.dtype
+    loc0, fac0, ln0 = s.committed
+    h.locations[0].copy_(loc0)
+    h.scales[0].copy_(fac0)
+    h.lognormalizers[0].copy_(ln0)
+    s.round_failures.zero_()
+    for t in range(s.rounds):
+        n_old, n_new = int(s.offsets[t]), int(s.schedule[t])
+        n_tot = n_old + n_new
+        fail = s.round_failures[t]
+        view = h.view(t + 1)
+        es = h.scales.element_size()
+        with _Span(s, "draw", n_new * d * es * 2):
+            normals = s.normals(n_new * d, dt)
+            rn, ru = _radial_buffers(s, n_new, dt)
+            x_new = s.samples[n_old:n_tot]
+            ops.draw(h, normals, n_new, fixed_slot=t, radial_normals=rn, rn_stride=s.rn_stride,
+                     radial_uniforms=ru, ru_stride=s.ru_stride, failures=fail, out=x_new, bank_ref=view)
+        with _Span(s, "target", n_new * (d + 1) * es):
+            s.bound_target.evaluate(x_new, out=s.logtargets[n_old:n_tot])
+        if is_npmc:
+            den = ops.denominator(native.DENOM_GENERATING)
+            lq = ops.mixture_logdensity(h, den, x_new, fixed_slot=t, failures=fail, out=s.lognum[n_old:n_tot],
+                                        bank_ref=view, precision=s.precision)
+            ops.subtract_logweights(s.logtargets[n_old:n_tot], lq, fail, out=s.logweights[n_old:n_tot])
+            lw_fit = _npmc_clipped(s.logweights[n_old:n_tot])
+            x_fit = x_new
+            ops.logweight_summary(s.logweights[n_old:n_tot], out=s.summaries[t])
+            fit_summary = ops.logweight_summary(lw_fit)
+        else:
+            if n_old > 0:
+                with _Span(s, "amis_append", n_old * (d + 2) * es):
+                    ops.amis_append(view, t, s.logcounts, s.samples[:n_old], s.lognum[:n_old], fail, s.precision)
+            den = ops.denominator(native.DENOM_PREFIX, s.logcounts, terms=t + 1)
+            with _Span(s, "mixture_new", n_new * (d + 1) * es + (t + 1) * d * d * es):
+                ops.mixture_logdensity(h, den, x_new, fixed_slot=t, failures=fail, out=s.lognum[n_old:n_tot],
+                                       bank_ref=view, precision=s.precision)
+            with _Span(s, "form_summary", n_tot * 4 * es):
+                ops.amis_form(s.logtargets[:n_tot], s.lognum[:n_tot], math.log(n_tot), s.logweights[:n_tot],
+                              failures=fail)
+                lw_fit = s.logweights[:n_tot]
+                x_fit = s.samples[:n_tot]
+                fit_summary = ops.logweight_summary(lw_fit, out=s.summaries[t])
+        with _Span(s, "moments", 2 * x_fit.shape[0] * (d + 1) * es):
+            s.shift.copy_(h.locations[t])
+            ops.weighted_moments(x_fit, lw_fit, fit_summary, s.shift, s.mean, s.cov)
+        last = t + 1 == s.rounds
+        out_loc = s.cand_loc if last else h.locations[t + 1]
+        out_fac = s.cand_factor if last else h.scales[t + 1]
+        out_ln = s.cand_lognorm if last else h.lognormalizers[t + 1:t + 2]
+        with _Span(s, "fit", 3 * d * d * 8):
+            ops.fit_factor(s.mean, s.cov, h.scales[t], out_loc, out_fac, out_ln, dof=h.dof,
+                           logconstant=h.logconstant, failures=fail, failure_index=n_tot + 1)
+    words = s.round_failures.cpu().numpy()
+    summaries = s.summaries.cpu().numpy()
+    err = NPMCRoundError if is_npmc else AMISRoundError
+    for t in range(s.rounds):
+        if words[t][0] != 0:
+            _raise_failures(words[t], err, t + 1)
+    total = int(s.offsets[-1])
+    ess = np.zeros(s.rounds)
+    logz = np.zeros(s.rounds)
+    for t in range(s.rounds):
+        m, sm, s2 = summaries[t]
+        n_t = int(s.schedule[t]) if is_npmc else int(s.offsets[t + 1])
+        ess[t] = 0.0 if sm == 0 else sm * sm / s2
+        logz[t] = -np.inf if sm == 0 else m + np.log(sm) - np.log(n_t)
+    s.committed = (s.cand_loc.clone(), s.cand_factor.clone(), s.cand_lognorm[0].clone())
+    diagnostics = {"method": "npmc" if is_npmc else "amis", "rounds": s.rounds, "round_sizes": list(s.schedule),
+                   "round_ess": ess, "round_lognormalizers": logz, "target_evaluations": total,
+                   "proposal_evaluations": total if is_npmc else s.rounds * total, "failures": 0}
+    return WeightedSamples(s.samples.clone(), s.logweights.clone(), provenance={"round": s.round_ids.clone()},
+                           diagnostics=diagnostics)
+
+
+def _npmc_clipped(lw):
+    """Clip the isqrt(n) largest log weights to the (n - isqrt(n) + 1)-th order
+    statistic (src/npmc_execution.jl:29-42)."""
+    n = lw.numel()
+    k = n - math.isqrt(n) + 1
+    threshold = torch.kthvalue(lw, k).values
+    return torch.minimum(lw, threshold)
+
+
+def current_proposal(sampler):
+    """The committed (learned) proposal of a moment sampler as host arrays."""
+    loc, fac, ln = sampler.committed
+    return loc.cpu().numpy(), fac.cpu().numpy().T.copy(), float(ln)
+
+
+# ---- DM-PMC ------------------------------------------------------------------------
+def _prepare_dmpmc(s):
+    alg = s.algorithm
+    db = pack(alg.bank, s.device)
+    s.bank = db
+    s.dtype = db.dtype
+    s.schedule = list(alg.round_size)
+    active = np.array([alg.bank.masses[i - 1] for i in db.host_ids])
+    counts, offsets = deterministic_allocation_plan(active, s.schedule)
+    s.counts_host, s.offsets = counts, offsets
+    s.counts = torch.tensor(counts.T.copy(), device=s.device)  # rounds x K
+    rounds = len(s.schedule)
+    s.rounds = rounds
+    s.slots = []
+    s.coefs = []
+    for r in range(rounds):
+        sl = np.repeat(np.arange(db.count, dtype=np.int32), counts[:, r])
+        s.slots.append(torch.tensor(sl, device=s.device))
+        coef = np.log(counts[:, r].astype(np.float64) / float(s.schedule[r]))
+        s.coefs.append(torch.tensor(coef, dtype=db.dtype, device=s.device))
+    s.committed_locations = db.locations.clone()
+    dofs = None if db.dofs is None else db.dofs.cpu().numpy()
+    s.rn_stride, s.ru_stride = _radial_strides(dofs)
+    s.bound_target = s.target.bind(s.device, db.dtype)
+    total = int(offsets[-1])
+    s.summaries = torch.zeros(rounds, 3, dtype=torch.float64, device=s.device)
+    s.round_failures = torch.zeros(rounds, 3, dtype=torch.int64, device=s.device)
+    s.samples = torch.empty(total, db.d, dtype=db.dtype, device=s.device)
+    s.logweights = torch.empty(total, dtype=db.dtype, device=s.device)
+    s.proposal_ids = torch.empty(total, dtype=torch.int64, device=s.device)
+    # locations in force during each round and the uniforms each resampling
+    # step consumed (device-side provenance, read only by diagnostics)
+    s.location_history = torch.empty(rounds, db.count, db.d, dtype=db.dtype, device=s.device)
+    s.resample_uniform_history = [None] * rounds
+
+
+def _run_dmpmc(s):
+    db = s.bank
+    d, dt = db.d, db.dtype
+    db.locations.copy_(s.committed_locations)
+    s.round_failures.zero_()
+    local = isinstance(s.algorithm.resampling, LocalResampling)
+    for r in range(s.rounds):
+        lo, hi = int(s.offsets[r]), int(s.offsets[r + 1])
+        n = hi - lo
+        fail = s.round_failures[r]
+        s.location_history[r].copy_(db.locations)
+        normals = s.normals(n * d, dt)
+        rn, ru = _radial_buffers(s, n, dt)
+        den = ops.denominator(native.DENOM_FULL, s.coefs[r])
+        x, lw, pid = ops.mis_round(db, den, s.slots[r], normals, None, rn, s.rn_stride, ru, s.ru_stride, fail,
+                                   s.precision, samples=s.samples[lo:hi], logweights=s.logweights[lo:hi],
+                                   proposal_ids_out=s.proposal_ids[lo:hi])
+        s.bound_target.evaluate(x, out=_scratch(s, n, dt))
+        ops.add_target_values(lw, s._scratch[:n], fail)
+        ops.logweight_summary(lw, out=s.summaries[r])
+        if local:
+            u = s.uniforms(db.count, dt)
+            _, dst = ops.local_resample(lw, s.counts[r], u, x)
+        else:
+            u = s.uniforms(db.count, torch.float64)
+            anc = ops.resample_multinomial(lw, u)
+            dst = ops.gather(x, anc)
+        s.resample_uniform_history[r] = u
+        db.locations.copy_(dst)
+    words = s.round_failures.cpu().numpy()
+    summaries = s.summaries.cpu().numpy()
+    for r in range(s.rounds):
+        if words[r][0] != 0:
+            _raise_failures(words[r], DMPMCRoundError, r + 1)
+        if summaries[r][1] == 0.0:
+            from .results import AllZeroWeightsError
+
+            raise DMPMCRoundError(r + 1, "resampling", AllZeroWeightsError())
+    ess = np.array([sm[1] ** 2 / sm[2] for sm in summaries])
+    logz = np.array([sm[0] + np.log(sm[1]) - np.log(s.schedule[r]) for r, sm in enumerate(summaries)])
+    s.committed_locations = db.locations.clone()
+    round_ids = torch.repeat_interleave(torch.arange(1, s.rounds + 1, device=s.device),
+                                        torch.tensor(s.schedule, device=s.device))
+    return WeightedSamples(s.samples.clone(), s.logweights.clone(),
+                           provenance={"round": round_ids, "proposal_id": s.proposal_ids.clone()},
+                           diagnostics={"method": "deterministic_mixture_pmc", "rounds": s.rounds,
+                                        "round_sizes": list(s.schedule), "round_ess": ess,
+                                        "round_lognormalizers": logz,
+                                        "resampling": "local" if local else "global", "failures": 0})
+
+
+def _scratch(s, n, dt):
+    buf = getattr(s, "_scratch", None)
+    if buf is None or buf.numel() < n:
+        s._scratch = torch.empty(n, dtype=dt, device=s.device)
+    return s._scratch[:n]

@@ -114,6 +114,8 @@ typedef struct issm_denominator {
 const char *issm_version(void);
 /* Human-readable message for a status code. */
 const char *issm_status_string(int status);
+/* Number of kernels this library has launched in this process (all threads). */
+uint64_t issm_kernel_launches(void);
 
 /* ---- failure record (src/execution.jl:669-756) ------------------------- */
 /* Zero the 3-word record on the stream (replaces _reset_native_failure_scratch!,
@@ -292,6 +294,30 @@ int issm_fit_factor(const double *mean, const double *cov, int32_t d,
                     void *out_factor, void *out_lognormalizer,
                     uint64_t *failures, int64_t failure_index,
                     issm_stream_t stream);
+
+/* ---- built-in batch targets ------------------------------------------------
+ * Native equivalents of the batch callbacks the benchmark workloads pass to
+ * LogTarget(...; batch=...) (src/targets.jl:65-76, src/batched_targets.jl:54-114):
+ *   STD_NORMAL  N(0, I)                              (normalised)
+ *   QUADRATIC   -|x - a|^2 / p0                      (a: d)
+ *   GAUSS_MIX   equal-weight N(a_j, I), j < count    (a: d x count; normalised)
+ *   STUDENT_T   t_nu(a, b b^T), nu = p0, p1 = log constant - log|b|  (b: d x d)
+ *   LINREG      N(y | X beta, p0^2 I) N(beta | 0, p1 I)  (X: count x d, y: count)
+ *   LOGISTIC    Bernoulli-logit(y | X beta) N(beta | 0, p1 I)                    */
+#define ISSM_TARGET_GAUSS_MIX  0
+#define ISSM_TARGET_STUDENT_T  1
+#define ISSM_TARGET_LINREG     2
+#define ISSM_TARGET_LOGISTIC   3
+#define ISSM_TARGET_STD_NORMAL 4
+#define ISSM_TARGET_QUADRATIC  5
+typedef struct issm_target {
+    int32_t kind, dim, count, dtype;
+    const void *a, *b, *c;
+    double p0, p1;
+} issm_target;
+/* out[i] = log target(x_i) for n samples (d x n, target dtype). */
+int issm_target_logdensity(const issm_target *target, const void *x, int64_t n,
+                           void *out, issm_stream_t stream);
 
 #ifdef __cplusplus
 }

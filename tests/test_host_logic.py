@@ -1,0 +1,128 @@
+"""Host-side logic of the package (no GPU): proposal constants, bank
+metadata, DM-PMC allocation plans and partial-MIS compilation, checked against
+the reference's golden vectors and the oracle."""
+import math
+
+import numpy as np
+import pytest
+
+
+def test_student_t_logconstant_matches_oracle(issm, orc):
+    for dof in (0.3, 1.0, 2.5, 5.0, 31.0, 40.0, 1e6):
+        for d in (1, 2, 3, 5, 16, 64):
+            assert issm.student_t_logconstant(dof, d) == pytest.approx(orc.student_t_logconstant(dof, d),
+                                                                       rel=1e-14, abs=1e-12)
+
+
+def test_student_t_logconstant_against_lgamma(issm):
+    for dof in (1.5, 5.0, 12.0):
+        for d in (1, 3, 4, 9):
+            exact = math.lgamma((dof + d) / 2) - math.lgamma(dof / 2) - d / 2 * math.log(dof * math.pi)
+            assert issm.student_t_logconstant(dof, d) == pytest.approx(exact, rel=1e-12)
+
+
+def test_proposal_validation(issm):
+    with pytest.raises(ValueError):
+        issm.FactorGaussian(np.zeros(2), np.array([[1.0, 0.5], [0.0, 1.0]]))
+    with pytest.raises(ValueError):
+        issm.SphericalGaussian(np.zeros(2), -1.0)
+    with pytest.raises(TypeError):
+        issm.FactorGaussian(np.zeros(2, dtype=np.float32), np.eye(2))
+    with pytest.raises(ValueError):
+        issm.ProposalBank([])
+    with pytest.raises(ValueError):
+        issm.ProposalBank([issm.SphericalGaussian(0.0, 1.0)], [0.0])
+
+
+def test_gaussian_lognormalizer(issm, golden):
+    c = golden["packed_factor_primitives"]
+    p = issm.FactorGaussian(np.array(c["location"]), np.array(c["factor"]))
+    assert float(p.lognormalizer) == pytest.approx(-math.log(2 * math.pi) - math.log(2.0), rel=1e-15)
+
+
+def test_bank_metadata_sorted_stably_by_mass(issm):
+    props = [issm.SphericalGaussian(float(i), 1.0) for i in range(1, 5)]
+    bank = issm.ProposalBank(props, [1, 3, 2, 0])
+    ids, logm, cdf = bank.active_metadata()
+    assert ids == [1, 3, 2]
+    assert cdf[-1] == 1.0
+    assert np.allclose(np.exp(logm), [1 / 6, 2 / 6, 3 / 6])
+    ties = issm.ProposalBank(props[:3], [1, 1, 1]).active_metadata()[0]
+    assert ties == [1, 2, 3]
+
+
+def test_dm_pmc_allocation_oracle(issm, golden):
+    c = golden["dm_pmc_allocation"]
+    props = [issm.SphericalGaussian(float(i), 1.0) for i in range(1, 5)]
+    bank = issm.ProposalBank(props, c["masses"])
+    ids, _, _ = bank.active_metadata()
+    assert ids == c["active_ids"]
+    active = [bank.masses[i - 1] for i in ids]
+    counts, offsets = issm.deterministic_allocation_plan(active, c["schedule"])
+    by_id = np.zeros((4, 3), dtype=np.int64)
+    for s, pid in enumerate(ids):
+        by_id[pid - 1] = counts[s]
+    assert by_id.tolist() == c["counts_by_id"]
+    assert (offsets + 1).tolist() == c["offsets"]
+
+
+def test_dm_pmc_rotating_ties(issm, golden):
+    c = golden["dm_pmc_rotating_ties"]
+    counts, _ = issm.deterministic_allocation_plan(c["masses"], c["schedule"])
+    assert counts.tolist() == c["counts"]
+
+
+def test_dm_pmc_large_float32_counts(issm, golden):
+    c = golden["dm_pmc_large_f32_counts"]
+    counts, _ = issm.deterministic_allocation_plan(np.float32(c["masses_f32"]), [c["round_size"]] * 2)
+    assert counts[:, 0].tolist() == c["first_round"]
+    assert counts[:, 1].tolist() == c["second_round"]
+
+
+def test_dm_pmc_uncovered_proposal_rejected(issm):
+    with pytest.raises(ValueError):
+        issm.deterministic_allocation_plan([100.0, 1.0, 1.0], [10])
+
+
+def test_partial_denominator_compile(issm):
+    from issm.sampler import compile_partial_denominator
+
+    props = [issm.SphericalGaussian(float(i), 1.0) for i in range(4)]
+    bank = issm.ProposalBank(props, [1.0, 2.0, 3.0, 4.0])
+    ids, logm, _ = bank.active_metadata()
+    grp, coef = compile_partial_denominator(bank, ids, logm, [[1, 2], [3, 4]])
+    # slots are ordered by mass: ids [1, 2, 3, 4]
+    assert grp.tolist() == [1, 1, 2, 2]
+    assert np.allclose(np.exp(coef), [1 / 3, 2 / 3, 3 / 7, 4 / 7])
+    with pytest.raises(ValueError):
+        compile_partial_denominator(bank, ids, logm, [[1, 2], [3]])
+    with pytest.raises(ValueError):
+        compile_partial_denominator(bank, ids, logm, [[1, 1], [2, 3, 4]])
+
+
+def test_schedules(issm):
+    p = issm.SphericalGaussian(0.0, 1.0)
+    assert issm.AMIS(p, rounds=3, round_size=5).round_size == [5, 5, 5]
+    assert issm.AMIS(p, rounds=2, round_size=[2, 3]).round_size == [2, 3]
+    with pytest.raises(ValueError):
+        issm.AMIS(p, rounds=2, round_size=[2])
+    with pytest.raises(ValueError):
+        issm.AMIS(issm.SphericalStudentT(2.0, 0.0, 1.0), rounds=2, round_size=2)
+
+
+def test_failure_decoding(issm):
+    idx, block, reason = 37, 0, 0x0400
+    packed = (((0xFFFFFFFF - idx + 1) & 0xFFFFFFFF) << 32) | (((0xFFFF - block + 1) & 0xFFFF) << 16) | reason
+    fail, draw = issm.ops.decode_failure([2, packed, 0])
+    assert fail == dict(count=2, first_logical_index=37, first_block=0, reason_bits=0x0400)
+    assert draw["count"] == 0
+
+
+def test_no_cpu_fallback(issm):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("has a GPU")
+    with pytest.raises(RuntimeError):
+        issm.prepare_sampler(0, issm.StandardNormalTarget(1),
+                             issm.ImportanceSampling(issm.SphericalGaussian(np.zeros(1), 1.0), nsamples=8))
