@@ -176,7 +176,8 @@ def run_gb300(args):
     loc, L, p_loc, p_fac = problem()
     target = issm.StudentTTarget(loc, L, DOF)
     proposal = issm.FactorGaussian(p_loc.astype(np.float32), p_fac.astype(np.float32))
-    alg = issm.AMIS(proposal, rounds=ROUNDS, round_size=ROUND_SIZE)
+    rounds, round_size = args.rounds, args.round_size
+    alg = issm.AMIS(proposal, rounds=rounds, round_size=round_size)
     sampler = issm.prepare_sampler(1234 + rank, target, alg, device=dev, precision=precision)
 
     def step():
@@ -186,7 +187,6 @@ def run_gb300(args):
         return issm.importance_sample_(sampler)
 
     sampler.initial = tuple(t.clone() for t in sampler.committed)
-    launches0 = issm.native.lib().issm_kernel_launches()
     for _ in range(max(args.warmup, 3)):
         res = step()
     torch.cuda.synchronize()
@@ -210,7 +210,7 @@ def run_gb300(args):
         t = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    total = ROUNDS * ROUND_SIZE
+    total = rounds * round_size
     value = total * world / (ms / 1e3)
     logz = float(res.diagnostics["round_lognormalizers"][-1])
     post_mean = issm.mean(res).cpu().numpy()
@@ -236,38 +236,46 @@ def run_gb300(args):
     def e2e_step():
         tgt = issm.StudentTTarget(loc, L, DOF)
         prop = issm.FactorGaussian(p_loc.astype(np.float32), p_fac.astype(np.float32))
-        smp = issm.prepare_sampler(99 + rank, tgt, issm.AMIS(prop, rounds=ROUNDS, round_size=ROUND_SIZE),
+        smp = issm.prepare_sampler(99 + rank, tgt, issm.AMIS(prop, rounds=rounds, round_size=round_size),
                                    device=dev, precision=precision)
         r = issm.importance_sample_(smp)
         pm = issm.mean(r).cpu().numpy()
         return r, pm
 
-    h2d = (D + D * D) * 4 * 2 + (D + D * D) * 4  # target (both dtypes bound lazily: float32) + proposal
+    # bytes copied per step: target location + scale factor and proposal location + factor
+    # (float32) in; per-round summary and failure words, the posterior mean and its
+    # summary out
     h2d = (D + D * D) * 4 + (D + D * D) * 4
-    d2h = ROUNDS * 3 * 8 * 2 + D * 8 + 3 * 8
-    for _ in range(2):
-        e2e_step()
-    torch.cuda.synchronize()
-    barrier()
-    t0 = time.perf_counter()
-    e2e_steps = max(2, args.steps // 2)
-    for _ in range(e2e_steps):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    d2h = rounds * 3 * 8 * 2 + D * 8 + 3 * 8
+    e2e_ms = float("nan")
+    if not args.quick:
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        e2e_steps = max(2, args.steps // 2)
+        for _ in range(e2e_steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / e2e_steps
     if world > 1:
         t = torch.tensor([e2e_ms], device=dev)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_ms = float(t.item())
     if rank != 0:
         return
-    cpu_value, cores, _ = cpu_amis_rate(reps=1)
+    cpu_value, cores = None, None
+    if not args.quick:
+        cpu_value, cores, _ = cpu_amis_rate(reps=1)
     line = {
         "metric": METRIC, "value": value, "unit": "weighted samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": {"fp32": "f32", "tf32": "tf32", "bf16": "bf16"}[args.precision],
         "data": "synthetic (seeded C4 inputs)",
-        "config": {"workload": WORKLOAD, "d": D, "rounds": ROUNDS, "round_size": ROUND_SIZE,
+        "config": {"workload": WORKLOAD if (rounds, round_size) == (ROUNDS, ROUND_SIZE) else
+                   f"AMIS d=64, Student-t target (nu=5), {rounds} rounds x {round_size} samples (reduced case)",
+                   "d": D, "rounds": rounds, "round_size": round_size,
                    "precision": args.precision, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2: 512 MiB retained samples re-read every round"},
         "accuracy": {"logz_hat": logz, "abs_logz_error": abs(logz), "posterior_mean_max_abs_error":
@@ -292,6 +300,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "bf16"])
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--rounds", type=int, default=ROUNDS)
+    ap.add_argument("--round-size", type=int, default=ROUND_SIZE)
+    ap.add_argument("--quick", action="store_true", help="skip the e2e and CPU-baseline legs (profiling runs)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

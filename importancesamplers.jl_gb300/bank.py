@@ -131,10 +131,12 @@ def pack_proposals(proposals, device, dtype=None):
         if kind == FACTOR:
             rr = torch.tensor([1 if factor_range_risk(p.exponent_bound(), dt) else 0 for p in proposals],
                               dtype=torch.uint8, device=device)
+    # torch.tensor keeps numpy strides; the kernels read raw C-order memory
     return DeviceBank(d, k, native.STUDENT_T if first.family == STUDENT_T else native.GAUSSIAN,
                       _scale_kind_code(kind), tdt,
-                      torch.tensor(loc, device=device), torch.tensor(sc, device=device),
-                      torch.tensor(lnorm, device=device), dofs, rr)
+                      torch.tensor(np.ascontiguousarray(loc), device=device).contiguous(),
+                      torch.tensor(np.ascontiguousarray(sc), device=device).contiguous(),
+                      torch.tensor(np.ascontiguousarray(lnorm), device=device).contiguous(), dofs, rr)
 
 
 def pack(bank, device):

@@ -158,6 +158,15 @@ int issm_add_target_values(void *logweights, const void *values, int64_t n, int3
     return add_target_values(logweights, values, n, dtype, failures, index_base, (cudaStream_t)stream);
 }
 
+int issm_check_target_values(const void *values, int64_t n, int32_t dtype, int64_t *round_ids,
+                             uint64_t *failures, int64_t index_base, issm_stream_t stream) {
+    if (n < 0) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!values) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return check_target_values(values, n, dtype, round_ids, failures, index_base, (cudaStream_t)stream);
+}
+
 int issm_subtract_logweights(const void *logtargets, const void *logden, int64_t n, int32_t dtype,
                              void *logweights, uint64_t *failures, int64_t index_base, issm_stream_t stream) {
     if (n < 0) return ISSM_E_SIZE;

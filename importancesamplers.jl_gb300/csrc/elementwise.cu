@@ -129,6 +129,36 @@ int amis_form(const void *lt, const void *lnum, const int64_t *round_ids, double
     return (int)cudaGetLastError();
 }
 
+// Target validity for targets evaluated outside the sampling kernel: a NaN or
+// +Inf value is recorded (_native_target_reason, src/execution.jl:769-773) and
+// the sample leaves the round (its round id becomes 0, as the reference's
+// _gaussian_round_launch_kernel! leaves it, src/mis_execution.jl:722-771).
+template <typename T>
+__global__ void check_targets_kernel(const T *__restrict__ v, int64_t n, int64_t *round_ids, uint64_t *failures,
+                                     int64_t index_base) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint16_t r = target_reason(v[i]);
+        if (r) {
+            record_failure(failures, index_base + i + 1, 0, r);
+            if (round_ids) round_ids[i] = 0;
+        }
+    }
+}
+
+int check_target_values(const void *values, int64_t n, int dtype, int64_t *round_ids, uint64_t *failures,
+                        int64_t index_base, cudaStream_t stream) {
+    if (n <= 0) return 0;
+    const int blocks = grid_for(n, 256, 4);
+    if (dtype == ISSM_F32)
+        { check_targets_kernel<float><<<blocks, 256, 0, stream>>>((const float *)values, n, round_ids, failures,
+                                                                  index_base); note_launch(); }
+    else
+        { check_targets_kernel<double><<<blocks, 256, 0, stream>>>((const double *)values, n, round_ids, failures,
+                                                                   index_base); note_launch(); }
+    return (int)cudaGetLastError();
+}
+
 int failure_reset(uint64_t *f, cudaStream_t stream) {
     return (int)cudaMemsetAsync(f, 0, 3 * sizeof(uint64_t), stream);
 }

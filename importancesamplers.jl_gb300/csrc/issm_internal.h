@@ -61,6 +61,8 @@ int subtract_logweights(const void *lt, const void *ld, int64_t n, int dtype, vo
 int amis_form(const void *lt, const void *lnum, const int64_t *round_ids, double logtotal, int64_t n,
               int dtype, void *lw, uint64_t *failures, cudaStream_t stream);
 int failure_reset(uint64_t *f, cudaStream_t stream);
+int check_target_values(const void *values, int64_t n, int dtype, int64_t *round_ids, uint64_t *failures,
+                        int64_t index_base, cudaStream_t stream);
 
 // built-in targets (targets.cu)
 int target_logdensity(const issm_target *t, const void *x, int64_t n, void *out, cudaStream_t stream);

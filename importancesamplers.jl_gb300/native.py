@@ -73,6 +73,7 @@ SIGNATURES = [
                                  _i32, _p]),
     ("issm_add_target_values", C.c_int, [_p, _p, _i64, _i32, _p, _i64, _p]),
     ("issm_subtract_logweights", C.c_int, [_p, _p, _i64, _i32, _p, _p, _i64, _p]),
+    ("issm_check_target_values", C.c_int, [_p, _i64, _i32, _p, _p, _i64, _p]),
     ("issm_amis_append", C.c_int, [_bank, _i32, _p, _p, _i64, _p, _p, _i32, _p]),
     ("issm_amis_form", C.c_int, [_p, _p, _p, _d, _i64, _i32, _p, _p, _p]),
     ("issm_reduce_workspace_bytes", _sz, [_i64]),
@@ -139,6 +140,8 @@ def ptr(t):
         return None
     if isinstance(t, int):
         return t
+    if not t.is_contiguous():
+        raise ValueError("tensors passed to libissm103.so must be contiguous (raw column-major layouts)")
     return t.data_ptr()
 
 

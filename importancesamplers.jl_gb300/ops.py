@@ -91,6 +91,11 @@ def add_target_values(logweights, values, failures=None, index_base=0):
     return logweights
 
 
+def check_target_values(values, round_ids=None, failures=None, index_base=0):
+    native.call("issm_check_target_values", native.ptr(values), values.numel(), _dt(values), native.ptr(round_ids),
+                native.ptr(failures), int(index_base), _s())
+
+
 def subtract_logweights(logtargets, logden, failures=None, index_base=0, out=None):
     out = torch.empty_like(logtargets) if out is None else out
     native.call("issm_subtract_logweights", native.ptr(logtargets), native.ptr(logden), logtargets.numel(),

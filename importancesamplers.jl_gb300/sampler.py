@@ -274,8 +274,9 @@ def _prepare_moment(s):
     dofs = None if p.family != STUDENT_T else [float(p.dof)]
     s.rn_stride, s.ru_stride = _radial_strides(dofs)
     s.bound_target = s.target.bind(s.device, dt)
-    s.round_ids = torch.repeat_interleave(torch.arange(1, s.rounds + 1, device=dev),
-                                          torch.tensor(s.schedule, device=dev))
+    s.round_ids_init = torch.repeat_interleave(torch.arange(1, s.rounds + 1, device=dev),
+                                               torch.tensor(s.schedule, device=dev)).contiguous()
+    s.round_ids = s.round_ids_init.clone()
 
 
 def _run_moment(s):
@@ -287,6 +288,7 @@ def _run_moment(s):
     h.scales[0].copy_(fac0)
     h.lognormalizers[0].copy_(ln0)
     s.round_failures.zero_()
+    s.round_ids.copy_(s.round_ids_init)
     for t in range(s.rounds):
         n_old, n_new = int(s.offsets[t]), int(s.schedule[t])
         n_tot = n_old + n_new
@@ -301,6 +303,7 @@ def _run_moment(s):
                      radial_uniforms=ru, ru_stride=s.ru_stride, failures=fail, out=x_new, bank_ref=view)
         with _Span(s, "target", n_new * (d + 1) * es):
             s.bound_target.evaluate(x_new, out=s.logtargets[n_old:n_tot])
+            ops.check_target_values(s.logtargets[n_old:n_tot], s.round_ids[n_old:n_tot], fail)
         if is_npmc:
             den = ops.denominator(native.DENOM_GENERATING)
             lq = ops.mixture_logdensity(h, den, x_new, fixed_slot=t, failures=fail, out=s.lognum[n_old:n_tot],
@@ -320,7 +323,7 @@ def _run_moment(s):
                                        bank_ref=view, precision=s.precision)
             with _Span(s, "form_summary", n_tot * 4 * es):
                 ops.amis_form(s.logtargets[:n_tot], s.lognum[:n_tot], math.log(n_tot), s.logweights[:n_tot],
-                              failures=fail)
+                              round_ids=s.round_ids[:n_tot], failures=fail)
                 lw_fit = s.logweights[:n_tot]
                 x_fit = s.samples[:n_tot]
                 fit_summary = ops.logweight_summary(lw_fit, out=s.summaries[t])

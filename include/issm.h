@@ -193,6 +193,14 @@ int issm_add_target_values(void *logweights, const void *values, int64_t n,
                            int32_t dtype, uint64_t *failures,
                            int64_t index_base, issm_stream_t stream);
 
+/* Record NaN / +Inf target values of a batch target (_native_target_reason,
+ * src/execution.jl:769-773) and, when round_ids is given, set the failed
+ * samples' round id to 0 so later stages skip them, as the reference's round
+ * kernel leaves them (src/mis_execution.jl:722-771). */
+int issm_check_target_values(const void *values, int64_t n, int32_t dtype,
+                             int64_t *round_ids, uint64_t *failures,
+                             int64_t index_base, issm_stream_t stream);
+
 /* logw_i = logtarget_i - logden_i with the reference's invalid-weight check
  * (_subtract_logweight, src/methods/importance_sampling.jl:1261-1266). */
 int issm_subtract_logweights(const void *logtargets, const void *logden,

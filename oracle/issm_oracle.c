@@ -464,13 +464,24 @@ double orc_target_logdensity(const orc_target *t, const double *x) {
 }
 
 /* src/execution.jl:103-186: (max, S, S2) and the summary. */
+/* Sums are compensated (Neumaier) so that the oracle stays accurate to a few
+ * ulps at any n: a plain sequential sum drops the many terms far below one
+ * ulp of the running total. */
 void orc_logweight_summary(const double *lw, int64_t n, double out[3]) {
     double m = -INFINITY;
     for (int64_t i = 0; i < n; ++i) if (lw[i] > m) m = lw[i];
-    double s = 0.0, s2 = 0.0;
+    double s = 0.0, s2 = 0.0, cs = 0.0, cs2 = 0.0;
     if (m != -INFINITY)
-        for (int64_t i = 0; i < n; ++i) { double w = exp(lw[i] - m); s += w; s2 += w * w; }
-    out[0] = m; out[1] = s; out[2] = s2;
+        for (int64_t i = 0; i < n; ++i) {
+            double w = exp(lw[i] - m), w2 = w * w;
+            double t = s + w;
+            cs += fabs(s) >= fabs(w) ? (s - t) + w : (w - t) + s;
+            s = t;
+            t = s2 + w2;
+            cs2 += fabs(s2) >= fabs(w2) ? (s2 - t) + w2 : (w2 - t) + s2;
+            s2 = t;
+        }
+    out[0] = m; out[1] = s + cs; out[2] = s2 + cs2;
 }
 
 /* src/results.jl:589-598 */

@@ -283,7 +283,9 @@ def test_summary_full_size_properties(issm, cuda):
     a = issm.ops.logweight_summary(lw).cpu().numpy()
     b = issm.ops.logweight_summary(lw[torch.randperm(n, device=cuda, generator=g)]).cpu().numpy()
     c = issm.ops.logweight_summary(lw + 7.0).cpu().numpy()
-    assert a[0] == b[0] and a[1] == pytest.approx(b[1], rel=1e-12) and a[2] == pytest.approx(b[2], rel=1e-12)
+    # FP32 exponentials are taken about per-thread running maxima, so the
+    # grouping changes them at the 1e-7 level; the FP64 sums add nothing more.
+    assert a[0] == b[0] and a[1] == pytest.approx(b[1], rel=1e-6) and a[2] == pytest.approx(b[2], rel=1e-6)
     assert c[0] == pytest.approx(a[0] + 7.0, rel=1e-7)
     assert c[1] == pytest.approx(a[1], rel=1e-5)
 
