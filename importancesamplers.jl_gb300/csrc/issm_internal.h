@@ -67,6 +67,10 @@ int check_target_values(const void *values, int64_t n, int dtype, int64_t *round
 // built-in targets (targets.cu)
 int target_logdensity(const issm_target *t, const void *x, int64_t n, void *out, cudaStream_t stream);
 
+// tensor-core self-test (tc_selftest.cu)
+int tc_gemm_selftest(const float *a, const float *b, float *c, int n, int k, int kind, int *status,
+                     cudaStream_t stream);
+
 // random streams (rng.cu)
 int fill_normals(uint64_t seed, uint64_t offset, int64_t n, void *out, int dtype, cudaStream_t stream);
 int fill_uniforms(uint64_t seed, uint64_t offset, int64_t n, void *out, int dtype, cudaStream_t stream);

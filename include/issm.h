@@ -327,6 +327,18 @@ typedef struct issm_target {
 int issm_target_logdensity(const issm_target *target, const void *x, int64_t n,
                            void *out, issm_stream_t stream);
 
+/* ---- tensor-core self-test ------------------------------------------------
+ * No counterpart in the reference: a one-CTA tcgen05 GEMM
+ * C[128 x n] = A[128 x k] B[n x k]^T (row-major FP32 in and out; inputs rounded
+ * to bf16 when kind = ISSM_PREC_BF16 or read as tf32 when kind = ISSM_PREC_TF32)
+ * that pins the shared-memory and instruction descriptor encodings used by
+ * the tensor-core kernels. n in {16, 32, ..., 256}; k a multiple of 16 (bf16)
+ * or 8 (tf32), k <= 64. *status (device int, zeroed by the caller) becomes 1
+ * if the MMA completion wait timed out. */
+int issm_tc_selftest(const float *a, const float *b, float *c, int32_t n,
+                     int32_t k, int32_t kind, int32_t *status,
+                     issm_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
