@@ -132,6 +132,57 @@ int issm_mixture_logdensity(const issm_bank *bank, const issm_denominator *den, 
     return ISSM_E_UNSUPPORTED;
 }
 
+size_t issm_tc_workspace_bytes(int32_t k, int32_t d) {
+    return tc_workspace_bytes(k < 1 ? 1 : k, d < 1 ? 1 : d) + 64;
+}
+
+static int tc_args_ok(const issm_bank *bank, int precision) {
+    if (precision != ISSM_PREC_TF32 && precision != ISSM_PREC_BF16) return ISSM_E_KIND;
+    if (bank->dtype != ISSM_F32 || bank->scale_kind != ISSM_SCALE_FACTOR || bank->dim > 64) return ISSM_E_UNSUPPORTED;
+    return ISSM_OK;
+}
+
+int issm_mixture_logdensity_ws(const issm_bank *bank, const issm_denominator *den, const void *x, int64_t n,
+                               const int32_t *slots, int32_t fixed_slot, void *out_logden, void *out_generating,
+                               uint64_t *failures, int64_t index_base, int32_t precision, void *workspace,
+                               size_t workspace_bytes, issm_stream_t stream) {
+    if (precision == ISSM_PREC_NATIVE)
+        return issm_mixture_logdensity(bank, den, x, n, slots, fixed_slot, out_logden, out_generating, failures,
+                                       index_base, precision, stream);
+    ISSM_TRY(check_bank(bank));
+    ISSM_TRY(check_den(bank, den));
+    ISSM_TRY(tc_args_ok(bank, precision));
+    if (n < 0) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!x || !out_logden || !workspace) return ISSM_E_NULL;
+    if (slots == nullptr && (fixed_slot < 0 || fixed_slot >= bank->count)) return ISSM_E_SIZE;
+    if (slots != nullptr) return ISSM_E_UNSUPPORTED;  // tensor form centres on one fixed slot
+    if (workspace_bytes < issm_tc_workspace_bytes(bank->count, bank->dim)) return ISSM_E_WORKSPACE;
+    const int last = den->kind == ISSM_DENOM_PREFIX ? den->terms - 1 : bank->count - 1;
+    int *err = (int *)((char *)workspace + workspace_bytes - 64);
+    return tc_mixture(bank, den, 0, 0, last, x, n, slots, fixed_slot,
+                      den->kind == ISSM_DENOM_GENERATING ? nullptr : den->logcoefficients, out_logden,
+                      out_generating, nullptr, failures, index_base, precision, workspace, workspace_bytes - 64,
+                      err, (cudaStream_t)stream);
+}
+
+int issm_amis_append_ws(const issm_bank *history, int32_t slot, const void *logcounts, const void *x, int64_t n,
+                        void *lognumerators, uint64_t *failures, int32_t precision, void *workspace,
+                        size_t workspace_bytes, issm_stream_t stream) {
+    if (precision == ISSM_PREC_NATIVE)
+        return issm_amis_append(history, slot, logcounts, x, n, lognumerators, failures, precision, stream);
+    ISSM_TRY(check_bank(history));
+    ISSM_TRY(tc_args_ok(history, precision));
+    if (n < 0 || slot < 0 || slot >= history->count) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!logcounts || !x || !lognumerators || !workspace) return ISSM_E_NULL;
+    if (workspace_bytes < issm_tc_workspace_bytes(history->count, history->dim)) return ISSM_E_WORKSPACE;
+    int *err = (int *)((char *)workspace + workspace_bytes - 64);
+    return tc_mixture(history, nullptr, 1, slot, slot, x, n, nullptr, slot, logcounts, nullptr, nullptr,
+                      lognumerators, failures, 0, precision, workspace, workspace_bytes - 64, err,
+                      (cudaStream_t)stream);
+}
+
 int issm_mis_round(const issm_bank *bank, const issm_denominator *den, const int32_t *slots, const void *normals,
                    const void *radial_normals, int32_t radial_normal_stride, const void *radial_uniforms,
                    int32_t radial_uniform_stride, const void *logtargets, int64_t n, void *samples,
@@ -275,7 +326,29 @@ int issm_local_resample(const void *logweights, const int64_t *counts, int32_t k
                           (cudaStream_t)stream);
 }
 
-size_t issm_moments_workspace_bytes(int64_t n, int32_t d) { return moments_workspace_bytes(n < 1 ? 1 : n, d); }
+size_t issm_moments_workspace_bytes(int64_t n, int32_t d) {
+    const size_t a = moments_workspace_bytes(n < 1 ? 1 : n, d < 1 ? 1 : d);
+    const size_t b = moments_tc_workspace_bytes(n < 1 ? 1 : n);
+    return (a > b ? a : b) + 64;
+}
+
+int issm_weighted_moments_ws(const void *x, int32_t d, int64_t n, const void *logweights, int32_t dtype,
+                             const double *summary, const double *shift, double *mean, double *cov,
+                             int32_t precision, void *workspace, size_t workspace_bytes, issm_stream_t stream) {
+    if (d < 1 || n < 1) return ISSM_E_SIZE;
+    if (d > 64) return ISSM_E_UNSUPPORTED;
+    if (!x || !logweights || !summary || !shift || !mean || !cov || !workspace) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    if (workspace_bytes < issm_moments_workspace_bytes(n, d)) return ISSM_E_WORKSPACE;
+    if (precision == ISSM_PREC_NATIVE)
+        return weighted_moments(x, d, n, logweights, dtype, summary, shift, mean, cov, workspace,
+                                workspace_bytes - 64, (cudaStream_t)stream);
+    if (precision != ISSM_PREC_TF32 && precision != ISSM_PREC_BF16) return ISSM_E_KIND;
+    if (dtype != ISSM_F32) return ISSM_E_UNSUPPORTED;
+    int *err = (int *)((char *)workspace + workspace_bytes - 64);
+    return moments_tc(x, d, n, logweights, summary, shift, mean, cov, precision, workspace, workspace_bytes - 64,
+                      err, (cudaStream_t)stream);
+}
 
 int issm_weighted_moments(const void *x, int32_t d, int64_t n, const void *logweights, int32_t dtype,
                           const double *summary, const double *shift, double *mean, double *cov, void *workspace,

@@ -67,6 +67,18 @@ int check_target_values(const void *values, int64_t n, int dtype, int64_t *round
 // built-in targets (targets.cu)
 int target_logdensity(const issm_target *t, const void *x, int64_t n, void *out, cudaStream_t stream);
 
+// tensor-core mixture density (mixture_tc.cu)
+size_t tc_workspace_bytes(int k, int d);
+int tc_mixture(const issm_bank *bk, const issm_denominator *den, int mode, int first, int last, const void *x,
+               int64_t n, const int32_t *slots, int fixed_slot, const void *coef, void *out_logden,
+               void *out_generating, void *lognum, uint64_t *failures, int64_t index_base, int precision, void *ws,
+               size_t ws_bytes, int *error, cudaStream_t stream);
+
+// tensor-core weighted moments (moments_tc.cu)
+size_t moments_tc_workspace_bytes(int64_t n);
+int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *summary, const double *shift,
+               double *mean, double *cov, int precision, void *ws, size_t ws_bytes, int *error, cudaStream_t stream);
+
 // tensor-core self-test (tc_selftest.cu)
 int tc_gemm_selftest(const float *a, const float *b, float *c, int n, int k, int kind, int *status,
                      cudaStream_t stream);

@@ -1,0 +1,201 @@
+// moments_tc.cu — tensor-core form of the weighted moments that drive AMIS /
+// N-PMC adaptation (_weighted_moments!, src/adaptive_gaussian_execution.jl:268-273).
+//
+// One streaming pass over the retained samples. For a tile of samples the
+// operand is the 128 x K matrix A whose rows 0..d-1 hold sqrt(w) (x - c)
+// (c = previous proposal mean), row 64 holds sqrt(w), other rows zero; then
+//   D[128 x 80] += A A[0:80]^T
+// accumulates S2 = sum w z z^T (rows/cols 0..63), S1 = sum w z (row 64 or
+// col 64) and S0 = sum w (D[64][64]) in FP32 tensor memory over all tiles of
+// the CTA. A and B are the same shared-memory tile (B = its first 80 rows).
+// Two tile buffers alternate so staging overlaps the previous tile's MMAs.
+// Per-CTA partials are summed in FP64 and mean = c + S1/S0,
+// cov = S2/S0 - (S1/S0)(S1/S0)^T.
+#include "issm_device.cuh"
+#include "issm_internal.h"
+#include "tcgen05.cuh"
+
+namespace issm {
+
+constexpr int kMtThreads = 128;
+constexpr int kMtRows = 128;  // MMA M
+constexpr int kMtCols = 80;   // MMA N (64 dims + sqrt(w) + padding)
+
+template <int KIND>
+__global__ void __launch_bounds__(kMtThreads) moments_tc_kernel(const float *__restrict__ x, int d, int64_t n,
+                                                                 const float *__restrict__ lw,
+                                                                 const double *__restrict__ summary,
+                                                                 const double *__restrict__ center,
+                                                                 float *__restrict__ partial, int *error) {
+    constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
+    constexpr int TS = KIND == tc::kBF16 ? 128 : 64;  // samples per tile = MMA K extent per tile
+    constexpr int PER = 16 / EB;
+    constexpr int KG = TS / PER;                       // 16 core groups per row (256 bytes)
+    constexpr int BUF = kMtRows * TS * EB;             // 32 KB
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag;
+    __shared__ float cshift[64];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) tc::tmem_alloc(&tmem_base, 128);
+    if (tid == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        tc::fence_mbar_init();
+        abort_flag = 0;
+    }
+    for (int c = tid; c < 64; c += kMtThreads) cshift[c] = c < d ? (float)center[c] : 0.f;
+    for (int e = tid; e < 2 * BUF / 16; e += kMtThreads) reinterpret_cast<uint4 *>(smem)[e] = make_uint4(0, 0, 0, 0);
+    const float m = (float)summary[0];
+    const float inv = (float)(1.0 / summary[1]);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = tmem_base;
+    const int64_t ntiles = (n + TS - 1) / TS;
+    uint32_t uses[2] = {0u, 0u};
+    int it = 0, last_buf = -1;
+    const uint32_t idesc = tc::instr_desc(KIND, kMtRows, kMtCols);
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        const int buf = it & 1;
+        if (it >= 2) {
+            if (tid == 0 && !tc::mbar_wait(&bar[buf], (uses[buf] - 1) & 1)) {
+                atomicExch(error, 1);
+                abort_flag = 1;
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (abort_flag) break;
+        }
+        unsigned char *sa = smem + buf * BUF;
+        // ---- stage column `tid` (one sample) of the tile ----
+        if (tid < TS) {
+            const int64_t i = tile * TS + tid;
+            float sw = 0.f;
+            float z[64];
+#pragma unroll
+            for (int c = 0; c < 64; ++c) z[c] = 0.f;
+            if (i < n) {
+                const float w = expf(lw[i] - m) * inv;
+                sw = sqrtf(w);
+                const float *xi = x + i * d;
+#pragma unroll
+                for (int c = 0; c < 64; ++c)
+                    if (c < d) z[c] = sw * (xi[c] - cshift[c]);
+            }
+            const int kq = tid / PER, kr = tid % PER;
+#pragma unroll
+            for (int j = 0; j < 65; ++j) {
+                const float v = j < 64 ? z[j] : sw;
+                const uint32_t off = (uint32_t)((((j >> 3) * KG + kq) << 7) + ((j & 7) << 4) + kr * EB);
+                if (EB == 2) *reinterpret_cast<uint16_t *>(sa + off) = tc::bf16_bits(v);
+                else *reinterpret_cast<float *>(sa + off) = v;
+            }
+        }
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (tid == 0) {
+            const uint32_t a0 = tc::smem_u32(sa);
+            for (int s = 0; s < TS * EB / 32; ++s) {
+                const uint64_t da = tc::smem_desc(a0 + s * 256, 128, KG * 128);
+                if (KIND == tc::kTF32) tc::mma_tf32(tbase, da, da, idesc, it > 0 || s > 0);
+                else tc::mma(tbase, da, da, idesc, it > 0 || s > 0);
+            }
+            tc::commit(&bar[buf]);
+        }
+        uses[buf] += 1;
+        last_buf = buf;
+    }
+    // ---- wait for the last MMA group (commits track every earlier MMA) ----
+    if (last_buf >= 0 && !abort_flag) {
+        if (tid == 0 && !tc::mbar_wait(&bar[last_buf], (uses[last_buf] - 1) & 1)) {
+            atomicExch(error, 1);
+            abort_flag = 1;
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    float *out = partial + (size_t)blockIdx.x * 65 * kMtCols;
+    if (!abort_flag && warp < 3) {
+        const int row = 32 * warp + lane;
+#pragma unroll
+        for (int c0 = 0; c0 < kMtCols; c0 += 16) {
+            float v[16];
+            if (last_buf >= 0) {
+                tc::tmem_ld16(tbase + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+            } else {
+                for (int j = 0; j < 16; ++j) v[j] = 0.f;
+            }
+            if (row <= 64) {
+                for (int j = 0; j < 16; ++j) out[row * kMtCols + c0 + j] = v[j];
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, 128);
+}
+
+__global__ void moments_tc_finish_kernel(const float *__restrict__ partial, int blocks, int d,
+                                         const double *__restrict__ center, double *__restrict__ mean,
+                                         double *__restrict__ cov) {
+    __shared__ double s1[65];
+    for (int j = threadIdx.x; j <= 64; j += blockDim.x) {
+        double acc = 0.0;
+        for (int b = 0; b < blocks; ++b) acc += (double)partial[(size_t)b * 65 * kMtCols + 64 * kMtCols + j];
+        s1[j] = acc;  // s1[64] = S0
+    }
+    __syncthreads();
+    const double s0 = s1[64];
+    if (blockIdx.x == 0)
+        for (int j = threadIdx.x; j < d; j += blockDim.x) mean[j] = center[j] + s1[j] / s0;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d * d; e += gridDim.x * blockDim.x) {
+        const int r = e % d, c = e / d;
+        double acc = 0.0;
+        for (int b = 0; b < blocks; ++b) acc += (double)partial[(size_t)b * 65 * kMtCols + r * kMtCols + c];
+        cov[e] = acc / s0 - (s1[r] / s0) * (s1[c] / s0);
+    }
+}
+
+static int moments_tc_blocks(int64_t n, int ts) {
+    int64_t t = (n + ts - 1) / ts;
+    int64_t b = kSMs * 2;
+    return (int)(t < b ? (t < 1 ? 1 : t) : b);
+}
+
+size_t moments_tc_workspace_bytes(int64_t n) {
+    return sizeof(float) * (size_t)moments_tc_blocks(n, 64) * 65 * kMtCols + 64;
+}
+
+int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *summary, const double *shift,
+               double *mean, double *cov, int precision, void *ws, size_t ws_bytes, int *error, cudaStream_t stream) {
+    if (d > 64) return ISSM_E_UNSUPPORTED;
+    if (ws_bytes < moments_tc_workspace_bytes(n)) return ISSM_E_WORKSPACE;
+    const bool bf16 = precision == ISSM_PREC_BF16;
+    const int ts = bf16 ? 128 : 64;
+    const int blocks = moments_tc_blocks(n, ts);
+    const size_t smem = 2 * (size_t)kMtRows * ts * (bf16 ? 2 : 4);
+    float *partial = (float *)ws;
+    if (bf16) {
+        auto kern = moments_tc_kernel<tc::kBF16>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+        { kern<<<blocks, kMtThreads, smem, stream>>>((const float *)x, d, n, (const float *)lw, summary, shift,
+                                                     partial, error); note_launch(); }
+    } else {
+        auto kern = moments_tc_kernel<tc::kTF32>;
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+        { kern<<<blocks, kMtThreads, smem, stream>>>((const float *)x, d, n, (const float *)lw, summary, shift,
+                                                     partial, error); note_launch(); }
+    }
+    { moments_tc_finish_kernel<<<(d * d + 127) / 128, 128, 0, stream>>>(partial, blocks, d, shift, mean, cov); note_launch(); }
+    return (int)cudaGetLastError();
+}
+
+}  // namespace issm

@@ -91,6 +91,11 @@ SIGNATURES = [
     ("issm_fit_factor", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _p, _p, _p, _p, _i64, _p]),
     ("issm_target_logdensity", C.c_int, [C.POINTER(Target), _p, _i64, _p, _p]),
     ("issm_tc_selftest", C.c_int, [_p, _p, _p, _i32, _i32, _i32, _p, _p]),
+    ("issm_tc_workspace_bytes", _sz, [_i32, _i32]),
+    ("issm_mixture_logdensity_ws", C.c_int, [_bank, _den, _p, _i64, _p, _i32, _p, _p, _p, _i64, _i32, _p, _sz,
+                                             _p]),
+    ("issm_amis_append_ws", C.c_int, [_bank, _i32, _p, _p, _i64, _p, _p, _i32, _p, _sz, _p]),
+    ("issm_weighted_moments_ws", C.c_int, [_p, _i32, _i64, _p, _i32, _p, _p, _p, _p, _i32, _p, _sz, _p]),
 ]
 
 _lib = None
@@ -166,12 +171,23 @@ def call(name, *args):
 _workspaces = {}
 
 
-def workspace(nbytes, device=None, tag="default"):
-    """A cached device scratch buffer of at least nbytes (per device, per tag)."""
+def workspace(nbytes, device=None, tag="default", zero=False):
+    """A cached device scratch buffer of at least nbytes (per device, per tag);
+    zero=True allocates it zero-filled (sticky error words live at its end)."""
     device = device or torch.device("cuda", torch.cuda.current_device())
     key = (str(device), tag)
     buf = _workspaces.get(key)
     if buf is None or buf.numel() < nbytes:
-        buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+        alloc = torch.zeros if zero else torch.empty
+        buf = alloc(max(int(nbytes), 256), dtype=torch.uint8, device=device)
         _workspaces[key] = buf
     return buf
+
+
+def tc_error(device=None):
+    """The sticky tensor-core wait-timeout word of the device's tc workspace."""
+    device = device or torch.device("cuda", torch.cuda.current_device())
+    buf = _workspaces.get((str(device), "tc"))
+    if buf is None:
+        return 0
+    return int(buf[-64:-60].view(torch.int32).item())

@@ -59,14 +59,27 @@ def draw(bank, normals, n, slots=None, fixed_slot=0, radial_normals=None, rn_str
     return out
 
 
+def _tc_workspace(count, d, device):
+    nb = native.lib().issm_tc_workspace_bytes(int(count), int(d))
+    # the error word sits in the last 64 bytes of whatever buffer is passed: size it exactly
+    buf = native.workspace(max(nb, 1 << 20), device, "tc", zero=True)
+    return buf
+
+
 def mixture_logdensity(bank, den, x, slots=None, fixed_slot=0, failures=None, generating=False, index_base=0,
                        precision=native.PREC_NATIVE, out=None, bank_ref=None):
     n = x.shape[0]
     out = torch.empty(n, dtype=bank.dtype, device=x.device) if out is None else out
     gen = torch.empty(n, dtype=bank.dtype, device=x.device) if generating else None
-    native.call("issm_mixture_logdensity", bank_ref or bank.ref(), ctypes.byref(den), native.ptr(x), n,
-                native.ptr(slots), int(fixed_slot), native.ptr(out), native.ptr(gen), native.ptr(failures),
-                int(index_base), int(precision), _s())
+    if precision == native.PREC_NATIVE:
+        native.call("issm_mixture_logdensity", bank_ref or bank.ref(), ctypes.byref(den), native.ptr(x), n,
+                    native.ptr(slots), int(fixed_slot), native.ptr(out), native.ptr(gen), native.ptr(failures),
+                    int(index_base), int(precision), _s())
+    else:
+        ws = _tc_workspace(bank.count, bank.d, x.device)
+        native.call("issm_mixture_logdensity_ws", bank_ref or bank.ref(), ctypes.byref(den), native.ptr(x), n,
+                    native.ptr(slots), int(fixed_slot), native.ptr(out), native.ptr(gen), native.ptr(failures),
+                    int(index_base), int(precision), native.ptr(ws), ws.numel(), _s())
     return (out, gen) if generating else out
 
 
@@ -103,9 +116,15 @@ def subtract_logweights(logtargets, logden, failures=None, index_base=0, out=Non
     return out
 
 
-def amis_append(history_ref, slot, logcounts, x, lognum, failures=None, precision=native.PREC_NATIVE):
-    native.call("issm_amis_append", history_ref, int(slot), native.ptr(logcounts), native.ptr(x), x.shape[0],
-                native.ptr(lognum), native.ptr(failures), int(precision), _s())
+def amis_append(history_ref, slot, logcounts, x, lognum, failures=None, precision=native.PREC_NATIVE, count=None):
+    if precision == native.PREC_NATIVE:
+        native.call("issm_amis_append", history_ref, int(slot), native.ptr(logcounts), native.ptr(x), x.shape[0],
+                    native.ptr(lognum), native.ptr(failures), int(precision), _s())
+    else:
+        ws = _tc_workspace(count or (int(slot) + 1), x.shape[1], x.device)
+        native.call("issm_amis_append_ws", history_ref, int(slot), native.ptr(logcounts), native.ptr(x),
+                    x.shape[0], native.ptr(lognum), native.ptr(failures), int(precision), native.ptr(ws), ws.numel(),
+                    _s())
     return lognum
 
 
@@ -193,15 +212,16 @@ def local_resample(logweights, counts, uniforms, samples=None, ancestors=None, d
     return anc, destination
 
 
-def weighted_moments(x, logweights, summary, shift, mean=None, cov=None):
+def weighted_moments(x, logweights, summary, shift, mean=None, cov=None, precision=native.PREC_NATIVE):
     n, d = x.shape
     dev = x.device
     mean = torch.empty(d, dtype=torch.float64, device=dev) if mean is None else mean
     cov = torch.empty(d, d, dtype=torch.float64, device=dev) if cov is None else cov
     nb = native.lib().issm_moments_workspace_bytes(n, d)
-    ws = native.workspace(nb, dev, "moments")
-    native.call("issm_weighted_moments", native.ptr(x), d, n, native.ptr(logweights), _dt(x), native.ptr(summary),
-                native.ptr(shift), native.ptr(mean), native.ptr(cov), native.ptr(ws), ws.numel(), _s())
+    ws = native.workspace(nb, dev, "moments", zero=True)
+    native.call("issm_weighted_moments_ws", native.ptr(x), d, n, native.ptr(logweights), _dt(x),
+                native.ptr(summary), native.ptr(shift), native.ptr(mean), native.ptr(cov), int(precision),
+                native.ptr(ws), ws.numel(), _s())
     return mean, cov
 
 
@@ -218,6 +238,15 @@ def target_logdensity(target_struct, x, out=None):
     out = torch.empty(n, dtype=x.dtype, device=x.device) if out is None else out
     native.call("issm_target_logdensity", ctypes.byref(target_struct), native.ptr(x), n, native.ptr(out), _s())
     return out
+
+
+def check_tensor_core_errors(device):
+    """Raise if a tensor-core kernel reported a timed-out completion wait (the
+    sticky words at the end of the tc and moments workspaces)."""
+    for tag in ("tc", "moments"):
+        buf = native._workspaces.get((str(device), tag))
+        if buf is not None and int(buf[-64:-60].view(torch.int32).item()) != 0:
+            raise RuntimeError(f"a tensor-core kernel ({tag}) timed out waiting for MMA completion")
 
 
 def decode_failure(words):

@@ -329,7 +329,7 @@ def _run_moment(s):
                 fit_summary = ops.logweight_summary(lw_fit, out=s.summaries[t])
         with _Span(s, "moments", 2 * x_fit.shape[0] * (d + 1) * es):
             s.shift.copy_(h.locations[t])
-            ops.weighted_moments(x_fit, lw_fit, fit_summary, s.shift, s.mean, s.cov)
+            ops.weighted_moments(x_fit, lw_fit, fit_summary, s.shift, s.mean, s.cov, precision=s.precision)
         last = t + 1 == s.rounds
         out_loc = s.cand_loc if last else h.locations[t + 1]
         out_fac = s.cand_factor if last else h.scales[t + 1]
@@ -339,6 +339,8 @@ def _run_moment(s):
                            logconstant=h.logconstant, failures=fail, failure_index=n_tot + 1)
     words = s.round_failures.cpu().numpy()
     summaries = s.summaries.cpu().numpy()
+    if s.precision != native.PREC_NATIVE:
+        ops.check_tensor_core_errors(s.device)
     err = NPMCRoundError if is_npmc else AMISRoundError
     for t in range(s.rounds):
         if words[t][0] != 0:

@@ -172,6 +172,28 @@ int issm_mixture_logdensity(const issm_bank *bank, const issm_denominator *den,
                             int64_t index_base, int32_t precision,
                             issm_stream_t stream);
 
+/* Workspace variants that also run the tensor-core precision forms
+ * (ISSM_PREC_TF32, ISSM_PREC_BF16 = bf16 split in three products) for
+ * factor-Gaussian / factor-Student-t FP32 banks with d <= 64; NATIVE
+ * precision runs the SIMT path and ignores the workspace. The workspace
+ * holds the per-call inverse factors W_k = L_k^-1 (FP64-formed, stored FP32)
+ * and the shift vectors; its last 64 bytes hold a sticky error word that a
+ * timed-out tensor-core completion wait sets to 1 (zero the workspace once
+ * when it is created). workspace_bytes >= issm_tc_workspace_bytes(K, d). */
+size_t issm_tc_workspace_bytes(int32_t k, int32_t d);
+int issm_mixture_logdensity_ws(const issm_bank *bank, const issm_denominator *den,
+                               const void *x, int64_t n, const int32_t *slots,
+                               int32_t fixed_slot, void *out_logden,
+                               void *out_generating, uint64_t *failures,
+                               int64_t index_base, int32_t precision,
+                               void *workspace, size_t workspace_bytes,
+                               issm_stream_t stream);
+int issm_amis_append_ws(const issm_bank *history, int32_t slot,
+                        const void *logcounts, const void *x, int64_t n,
+                        void *lognumerators, uint64_t *failures,
+                        int32_t precision, void *workspace,
+                        size_t workspace_bytes, issm_stream_t stream);
+
 /* Fused static-MIS / DM-PMC round: draw + denominator + log weight.
  * logw_i = logtarget_i - logden_i when `logtargets` is non-NULL; with
  * logtargets == NULL the target is deferred (the reference's batch-target
@@ -290,6 +312,19 @@ int issm_weighted_moments(const void *x, int32_t d, int64_t n,
                           const double *summary, const double *shift,
                           double *mean, double *cov, void *workspace,
                           size_t workspace_bytes, issm_stream_t stream);
+/* As issm_weighted_moments with a precision: ISSM_PREC_TF32 / ISSM_PREC_BF16
+ * run one tensor-core pass over FP32 samples about `shift`, accumulating
+ * sum w z z^T, sum w z and sum w in FP32 tensor memory and finishing in FP64
+ * (d <= 64); NATIVE runs the two-pass SIMT kernels. workspace_bytes >=
+ * issm_moments_workspace_bytes(n, d); its last 64 bytes hold the sticky
+ * tensor-core timeout word (zero the workspace once when it is created). */
+int issm_weighted_moments_ws(const void *x, int32_t d, int64_t n,
+                             const void *logweights, int32_t dtype,
+                             const double *summary, const double *shift,
+                             double *mean, double *cov, int32_t precision,
+                             void *workspace, size_t workspace_bytes,
+                             issm_stream_t stream);
+
 /* Candidate fit: cov + ridge I with ridge = sqrt(eps(T)) tr(L_prev L_prev^T)
  * * c_nu / d (src/adaptive_gaussian_execution.jl:283-301, src/execution.jl:188-194),
  * FP64 Cholesky, Student-t scaling by sqrt((nu-2)/nu), lognormalizer and the

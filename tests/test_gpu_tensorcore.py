@@ -21,3 +21,123 @@ def test_tc_gemm_selftest_exact(issm, cuda, kind, n, k):
     torch.cuda.synchronize()
     assert int(status.item()) == 0
     assert torch.equal(c, a @ b.T)
+
+
+def _factor_bank(issm, rng, d, k, family, cuda, spread=1.5):
+    props = []
+    for _ in range(k):
+        A = rng.normal(size=(d, d))
+        L = np.linalg.cholesky(A @ A.T / d + 0.1 * np.eye(d)).astype(np.float32)
+        mu = (rng.normal(size=d) * spread).astype(np.float32)
+        if family == "gaussian":
+            props.append(issm.FactorGaussian(mu, L))
+        else:
+            props.append(issm.FactorStudentT(np.float32(5.0), mu, L))
+    return issm.pack_proposals(props, cuda)
+
+
+# relative to max(1, |value|): TF32 keeps ~11 bits per product, bf16 x3 ~16
+TOL = {"tf32": 4e-3, "bf16": 5e-5}
+
+
+@pytest.mark.parametrize("prec", ["tf32", "bf16"])
+@pytest.mark.parametrize("d,k,family", [(5, 3, "gaussian"), (16, 8, "gaussian"), (33, 5, "student"),
+                                        (64, 12, "gaussian"), (64, 40, "student")])
+@pytest.mark.parametrize("denom", ["prefix", "full", "generating"])
+def test_tc_mixture_vs_oracle(issm, orc, cuda, prec, d, k, family, denom):
+    from test_gpu_kernels import oracle_bank
+
+    rng = np.random.default_rng(d * 100 + k)
+    db = _factor_bank(issm, rng, d, k, family, cuda)
+    ob = oracle_bank(orc, db)
+    slot = k - 1 if denom == "prefix" else k // 2
+    n = 3001
+    L = db.scales[slot].double().cpu().numpy().T
+    x = (db.locations[slot].double().cpu().numpy() + rng.normal(size=(n, d)) @ L.T).astype(np.float32)
+    coef = torch.log(torch.softmax(torch.tensor(rng.normal(size=k), device=cuda), 0)).float().contiguous()
+    kind = {"prefix": issm.native.DENOM_PREFIX, "full": issm.native.DENOM_FULL,
+            "generating": issm.native.DENOM_GENERATING}[denom]
+    terms = k if denom == "prefix" else 0
+    den = issm.ops.denominator(kind, coef, terms=terms)
+    precision = issm.native.PREC_TF32 if prec == "tf32" else issm.native.PREC_BF16
+    fail = issm.ops.new_failures(cuda)
+    out, gen = issm.ops.mixture_logdensity(db, den, torch.tensor(x, device=cuda), fixed_slot=slot, failures=fail,
+                                           generating=True, precision=precision)
+    torch.cuda.synchronize()
+    issm.ops.check_tensor_core_errors(cuda)
+    eo, eg, _ = orc.mixture_logdensity(ob, x.astype(np.float64).reshape(-1), kind, coef.double().cpu().numpy(),
+                                       terms=terms, fixed_slot=slot)
+    got = out.double().cpu().numpy()
+    err = np.abs(got - eo) / np.maximum(1.0, np.abs(eo))
+    assert err.max() <= TOL[prec], err.max()
+    gerr = np.abs(gen.double().cpu().numpy() - eg) / np.maximum(1.0, np.abs(eg))
+    assert gerr.max() <= TOL[prec]
+    assert int(fail[0].item()) == 0
+
+
+@pytest.mark.parametrize("prec", ["tf32", "bf16"])
+@pytest.mark.parametrize("d", [8, 64])
+def test_tc_amis_append_vs_oracle(issm, orc, cuda, prec, d):
+    from test_gpu_kernels import oracle_bank
+
+    rng = np.random.default_rng(d)
+    k = 6
+    db = _factor_bank(issm, rng, d, k, "gaussian", cuda)
+    ob = oracle_bank(orc, db)
+    n = 70001
+    x = (rng.normal(size=(n, d)) * 2).astype(np.float32)
+    lognum = (rng.normal(size=n) - 50).astype(np.float32)
+    logcounts = torch.tensor(np.log(np.arange(1, k + 1, dtype=np.float32)), device=cuda)
+    slot = 4
+    t = torch.tensor(lognum, device=cuda)
+    precision = issm.native.PREC_TF32 if prec == "tf32" else issm.native.PREC_BF16
+    issm.ops.amis_append(db.ref(), slot, logcounts, torch.tensor(x, device=cuda), t, precision=precision,
+                         count=k)
+    torch.cuda.synchronize()
+    issm.ops.check_tensor_core_errors(cuda)
+    lq, _, _ = orc.mixture_logdensity(ob, x.astype(np.float64).reshape(-1), orc.DENOM_GENERATING, slots=None,
+                                      fixed_slot=slot)
+    exp = np.logaddexp(lognum.astype(np.float64), float(logcounts[slot]) + lq)
+    err = np.abs(t.double().cpu().numpy() - exp) / np.maximum(1.0, np.abs(exp))
+    assert err.max() <= TOL[prec]
+
+
+@pytest.mark.parametrize("prec", ["tf32", "bf16"])
+@pytest.mark.parametrize("d,n", [(3, 1000), (16, 100003), (64, 262145)])
+def test_tc_moments_vs_oracle(issm, orc, cuda, prec, d, n):
+    rng = np.random.default_rng(n)
+    A = rng.normal(size=(d, d)) / np.sqrt(d)
+    X = (rng.normal(size=(n, d)) @ A.T + 1.0).astype(np.float32)
+    lw = (rng.normal(size=n) * 0.5).astype(np.float32)
+    tx, tl = torch.tensor(X, device=cuda), torch.tensor(lw, device=cuda)
+    sm = issm.ops.logweight_summary(tl)
+    shift = torch.full((d,), 0.9, dtype=torch.float64, device=cuda)
+    precision = issm.native.PREC_TF32 if prec == "tf32" else issm.native.PREC_BF16
+    mean, cov = issm.ops.weighted_moments(tx, tl, sm, shift, precision=precision)
+    torch.cuda.synchronize()
+    issm.ops.check_tensor_core_errors(cuda)
+    em, ec, _ = orc.weighted_moments(X.astype(np.float64).reshape(-1), d, lw.astype(np.float64))
+    scale = np.sqrt(np.outer(np.diag(ec), np.diag(ec)))
+    tol = 2e-3 if prec == "tf32" else 1e-2
+    assert np.max(np.abs(mean.cpu().numpy() - em) / np.sqrt(np.diag(ec))) < tol
+    assert np.max(np.abs(cov.cpu().numpy() - ec) / scale) < tol
+
+
+@pytest.mark.parametrize("prec", ["tf32", "bf16"])
+def test_tc_amis_matches_native_form(issm, cuda, prec):
+    """Same draws, FP32 SIMT vs tensor-core forms: log Z and the posterior
+    mean agree to well inside the estimator's own error."""
+    rng = np.random.default_rng(5)
+    d = 16
+    Lt = np.tril(rng.normal(size=(d, d)) * 0.3, -1) + np.diag(1 + np.abs(rng.normal(size=d)))
+    target = issm.StudentTTarget(np.zeros(d), Lt, 5.0)
+    p = issm.FactorGaussian(np.zeros(d, dtype=np.float32), (2.5 * np.eye(d)).astype(np.float32))
+    out = {}
+    for name, precision in (("native", issm.native.PREC_NATIVE),
+                            (prec, issm.native.PREC_TF32 if prec == "tf32" else issm.native.PREC_BF16)):
+        s = issm.prepare_sampler(7, target, issm.AMIS(p, rounds=8, round_size=20000), device=cuda,
+                                 precision=precision)
+        r = issm.importance_sample_(s)
+        out[name] = (r.diagnostics["round_lognormalizers"][-1], issm.mean(r).cpu().numpy())
+    assert abs(out["native"][0] - out[prec][0]) < 2e-2
+    assert np.max(np.abs(out["native"][1] - out[prec][1])) < 5e-2
