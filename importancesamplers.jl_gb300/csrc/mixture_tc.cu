@@ -112,20 +112,39 @@ __global__ void __launch_bounds__(kTcThreads) mixture_tc_kernel(TcParams p) {
     const int nchunks = (nslots + p.chunk - 1) / p.chunk;
     int staged_chunk = -1;
     const uint32_t idesc = tc::instr_desc(KIND, kTcTile, DP);
-    float xs[DP];
+    // rows are loaded with 16-byte vectors when the layout allows it
+    const bool vec = (p.d % 4 == 0) && ((reinterpret_cast<uintptr_t>(p.x) & 15) == 0);
+    float xs[DP], xn[DP];
+    auto load_row = [&](int tile, float (&dst)[DP]) {
+        const int64_t r = (int64_t)tile * kTcTile + tid;
+#pragma unroll
+        for (int c = 0; c < DP; ++c) dst[c] = 0.f;
+        if (tile < p.ntile_total && r < p.n) {
+            const float *xi = p.x + r * p.d;
+            if (vec) {
+#pragma unroll
+                for (int c = 0; c < DP; c += 4)
+                    if (c < p.d) {
+                        const float4 q = __ldg(reinterpret_cast<const float4 *>(xi + c));
+                        dst[c] = q.x; dst[c + 1] = q.y; dst[c + 2] = q.z; dst[c + 3] = q.w;
+                    }
+            } else {
+#pragma unroll
+                for (int c = 0; c < DP; ++c)
+                    if (c < p.d) dst[c] = __ldg(xi + c);
+            }
+        }
+    };
+    load_row(blockIdx.x, xn);
 
     for (int tile = blockIdx.x; tile < p.ntile_total; tile += gridDim.x) {
         const int64_t i = (int64_t)tile * kTcTile + tid;
         const bool active = i < p.n;
-        // ---- stage A (shifted samples) ----
+        // ---- stage A (shifted samples) from the prefetched row ----
 #pragma unroll
-        for (int c = 0; c < DP; ++c) xs[c] = 0.f;
-        if (active) {
-            const float *xi = p.x + i * p.d;
-#pragma unroll
-            for (int c = 0; c < DP; ++c)
-                if (c < p.d) xs[c] = xi[c] - p.center[c];
-        }
+        for (int c = 0; c < DP; ++c) xs[c] = (c < p.d && active) ? xn[c] - p.center[c] : 0.f;
+        // the next tile's row is in flight while this tile's MMAs and epilogue run
+        load_row(tile + gridDim.x, xn);
 #pragma unroll
         for (int q = 0; q < KG; ++q) {
             put_chunk<KIND>(sa, tid, q, KG, xs + q * PER, false);
@@ -297,13 +316,20 @@ static int launch_tc(TcParams p, cudaStream_t stream) {
     p.chunk = chunk;
     size_t smem = (size_t)NPART * kTcTile * DP * EB + (size_t)NPART * chunk * DP * DP * EB +
                   sizeof(float) * chunk * DP;
-    // at most two CTAs per SM, so their TMEM allocations (<= 256 columns each) never wait
-    if (smem < 80 * 1024) smem = 80 * 1024;
+    // never more resident CTAs per SM than TMEM holds, so allocations never wait
+    const int ncols = chunk * DP <= 32 ? 32 : chunk * DP <= 64 ? 64 : chunk * DP <= 128 ? 128 : 256;
+    const int tmem_ctas = 512 / ncols;
+    const size_t floor_smem = 233472 / (tmem_ctas + 1) + 1024;
+    if (smem < floor_smem) smem = floor_smem;
     auto kern = mixture_tc_kernel<KIND, SPLIT, DP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
+    int occ = 1;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTcThreads, smem);
+    if (e != cudaSuccess) return (int)e;
+    occ = max(1, min(occ, tmem_ctas));
     p.ntile_total = (int)((p.n + kTcTile - 1) / kTcTile);
-    const int blocks = min(p.ntile_total, kSMs * 2);
+    const int blocks = min(p.ntile_total, kSMs * occ);
     if (blocks < 1) return 0;
     { kern<<<blocks, kTcThreads, smem, stream>>>(p); note_launch(); }
     return (int)cudaGetLastError();

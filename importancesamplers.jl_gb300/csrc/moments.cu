@@ -188,49 +188,55 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
     }
     for (int c = threadIdx.x; c < d; c += blockDim.x) A[c + c * d] += ridge;
     __syncthreads();
+    // right-looking Cholesky: every thread derives the pivot itself, so each
+    // column costs two barriers
     for (int j = 0; j < d; ++j) {
-        if (threadIdx.x == 0) {
-            const double djj = A[j + j * d];
-            if (!(djj > 0.0) || !isfinite(djj)) bad = 1;
-            A[j + j * d] = sqrt(djj);
-        }
+        const double djj = A[j + j * d];
+        const double ljj = sqrt(djj);
+        if (threadIdx.x == 0 && (!(djj > 0.0) || !isfinite(djj))) bad = 1;
+        const int m = d - j - 1;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) A[(j + 1 + i) + j * d] /= ljj;
         __syncthreads();
-        const double ljj = A[j + j * d];
-        for (int i = j + 1 + threadIdx.x; i < d; i += blockDim.x) A[i + j * d] /= ljj;
-        __syncthreads();
-        for (int e = threadIdx.x; e < (d - j - 1) * (d - j - 1); e += blockDim.x) {
-            const int i = j + 1 + e % (d - j - 1), c = j + 1 + e / (d - j - 1);
-            if (i >= c) A[i + c * d] -= A[i + j * d] * A[c + j * d];
+        if (threadIdx.x == 0) A[j + j * d] = ljj;
+        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+            const int i = e % m, c = e / m;
+            if (i >= c) A[(j + 1 + i) + (j + 1 + c) * d] -= A[(j + 1 + i) + j * d] * A[(j + 1 + c) + j * d];
         }
         __syncthreads();
     }
+    // Student-t scaling, rounding to T, validity and log|L| as block reductions
     const double f = dof > 0.0 ? sqrt(1.0 / mult) : 1.0;
+    double logdet = 0.0;
+    int invalid = 0;
     for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
         const int r = e % d, c = e / d;
-        const double v = r >= c ? A[e] * f : 0.0;
-        out_factor[e] = (T)v;
+        const T v = r >= c ? (T)(A[e] * f) : T(0);
+        out_factor[e] = v;
+        if (r >= c) {
+            invalid |= !isfinite((double)v);
+            if (r == c) {
+                invalid |= !((double)v > 0.0);
+                logdet += log(fabs((double)v));
+            }
+        }
     }
-    for (int c = threadIdx.x; c < d; c += blockDim.x) out_loc[c] = (T)mean[c];
-    __syncthreads();
+    for (int c = threadIdx.x; c < d; c += blockDim.x) {
+        const T v = (T)mean[c];
+        out_loc[c] = v;
+        invalid |= !isfinite((double)v);
+    }
+    red[threadIdx.x] = logdet;
+    invalid = __syncthreads_or(invalid);
+    for (int off = 128; off > 0; off >>= 1) {
+        if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
+        __syncthreads();
+    }
     if (threadIdx.x == 0) {
-        double logabsdet = 0.0;
-        bool valid = !bad;
-        for (int c = 0; c < d; ++c) {
-            const T lv = out_factor[c + c * d];
-            logabsdet += log(fabs((double)lv));
-            valid &= (bool)isfinite((double)out_loc[c]);
-        }
-        for (int e = 0; e < d * d; ++e) {
-            const int r = e % d, c = e / d;
-            if (r < c) continue;
-            const double v = (double)out_factor[e];
-            valid &= (bool)isfinite(v);
-            if (r == c) valid &= v > 0.0;
-        }
+        const double logabsdet = red[0];
         const double ln = dof > 0.0 ? logconst - logabsdet
                                     : -0.5 * (double)d * log(2.0 * 3.14159265358979323846) - logabsdet;
         *out_lognorm = (T)ln;
-        valid &= (bool)isfinite((double)(T)ln);
+        const bool valid = !bad && !invalid && isfinite((double)(T)ln);
         if (!valid) record_failure(failures, failure_index, 0, ISSM_REASON_MOMENT_FIT_INVALID);
     }
 }

@@ -57,6 +57,37 @@ __global__ void __launch_bounds__(kMtThreads) moments_tc_kernel(const float *__r
     uint32_t uses[2] = {0u, 0u};
     int it = 0, last_buf = -1;
     const uint32_t idesc = tc::instr_desc(KIND, kMtRows, kMtCols);
+    // thread -> (sample column, dimension half): TF32 tiles have 64 samples, so
+    // two threads share a sample, each staging 32 dimensions
+    constexpr int HALVES = kMtThreads / TS;   // 1 (bf16) or 2 (tf32)
+    constexpr int DH = 64 / HALVES;           // dimensions per thread
+    const int col = tid % TS, half = tid / TS, j0 = half * DH;
+    const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0);
+    float xr[DH];
+    float lr = -INFINITY;
+    auto load_col = [&](int64_t tile) {
+        const int64_t i = tile * TS + col;
+#pragma unroll
+        for (int c = 0; c < DH; ++c) xr[c] = 0.f;
+        lr = -INFINITY;
+        if (tile < ntiles && i < n) {
+            lr = __ldg(lw + i);
+            const float *xi = x + i * d + j0;
+            if (vec) {
+#pragma unroll
+                for (int c = 0; c < DH; c += 4)
+                    if (j0 + c < d) {
+                        const float4 q = __ldg(reinterpret_cast<const float4 *>(xi + c));
+                        xr[c] = q.x; xr[c + 1] = q.y; xr[c + 2] = q.z; xr[c + 3] = q.w;
+                    }
+            } else {
+#pragma unroll
+                for (int c = 0; c < DH; ++c)
+                    if (j0 + c < d) xr[c] = __ldg(xi + c);
+            }
+        }
+    };
+    load_col(blockIdx.x);
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int buf = it & 1;
         if (it >= 2) {
@@ -70,25 +101,19 @@ __global__ void __launch_bounds__(kMtThreads) moments_tc_kernel(const float *__r
             if (abort_flag) break;
         }
         unsigned char *sa = smem + buf * BUF;
-        // ---- stage column `tid` (one sample) of the tile ----
-        if (tid < TS) {
-            const int64_t i = tile * TS + tid;
-            float sw = 0.f;
-            float z[64];
+        // ---- stage this thread's (sample, dimension-half) of the tile ----
+        {
+            const float sw = lr == -INFINITY ? 0.f : sqrtf(expf(lr - m) * inv);
+            float z[DH];
 #pragma unroll
-            for (int c = 0; c < 64; ++c) z[c] = 0.f;
-            if (i < n) {
-                const float w = expf(lw[i] - m) * inv;
-                sw = sqrtf(w);
-                const float *xi = x + i * d;
+            for (int c = 0; c < DH; ++c) z[c] = (j0 + c < d) ? sw * (xr[c] - cshift[j0 + c]) : 0.f;
+            load_col(tile + gridDim.x);  // next tile's column is in flight during the stores and MMAs
+            const int kq = col / PER, kr = col % PER;
 #pragma unroll
-                for (int c = 0; c < 64; ++c)
-                    if (c < d) z[c] = sw * (xi[c] - cshift[c]);
-            }
-            const int kq = tid / PER, kr = tid % PER;
-#pragma unroll
-            for (int j = 0; j < 65; ++j) {
-                const float v = j < 64 ? z[j] : sw;
+            for (int jj = 0; jj <= DH; ++jj) {
+                if (jj == DH && half != HALVES - 1) break;
+                const int j = jj < DH ? j0 + jj : 64;
+                const float v = jj < DH ? z[jj] : sw;
                 const uint32_t off = (uint32_t)((((j >> 3) * KG + kq) << 7) + ((j & 7) << 4) + kr * EB);
                 if (EB == 2) *reinterpret_cast<uint16_t *>(sa + off) = tc::bf16_bits(v);
                 else *reinterpret_cast<float *>(sa + off) = v;
