@@ -90,7 +90,23 @@ class DeviceBank:
         self.struct = native.Bank(self.d, self.count, self.family, self.scale_kind, native.dtype_code(self.dtype),
                                   0, native.ptr(self.locations), native.ptr(self.scales),
                                   native.ptr(self.lognormalizers), native.ptr(self.dofs),
-                                  native.ptr(self.range_risk))
+                                  native.ptr(self.range_risk), native.ptr(getattr(self, "inverse_factors", None)))
+        return self
+
+    def attach_inverse_factors(self, first=0, count=None):
+        """Allocate (once) and fill the FP32 inverse factors W_k = L_k^-1 the
+        tensor-core forms read (issm_bank.inverse_factors)."""
+        if self.scale_kind != native.SCALE_FACTOR or self.dtype != torch.float32 or self.d > 64:
+            return self
+        dp = 16 if self.d <= 16 else 32 if self.d <= 32 else 64
+        if getattr(self, "inverse_factors", None) is None:
+            self.inverse_factors = torch.zeros(self.count, dp, dp, dtype=torch.float32, device=self.locations.device)
+            self.refresh()
+            self.__dict__.pop("_views", None)
+        count = self.count - first if count is None else count
+        if count > 0:
+            native.call("issm_invert_factors", self.ref(), int(first), int(count), native.ptr(self.inverse_factors),
+                        native.stream_ptr())
         return self
 
     def ref(self):
@@ -148,6 +164,7 @@ def pack(bank, device):
     db.logmasses = torch.tensor(logm.astype(proposals[0].dtype), device=device)
     db.cdf = torch.tensor(cdf.astype(proposals[0].dtype), device=device)
     db.host_ids, db.host_logmasses, db.host_cdf = ids, logm, cdf
+    db.attach_inverse_factors()
     return db
 
 
@@ -175,6 +192,7 @@ class DeviceHistory(DeviceBank):
         h = cls(d, rounds, fam, native.SCALE_FACTOR, tdt, loc, sc, lnorm, dofs, rr)
         h.logconstant = 0.0 if proposal.family != STUDENT_T else float(proposal.logconstant)
         h.dof = 0.0 if proposal.family != STUDENT_T else float(proposal.dof)
+        h.attach_inverse_factors(0, 1)
         return h
 
     def view(self, slots):
@@ -186,7 +204,8 @@ class DeviceHistory(DeviceBank):
             views[slots] = native.Bank(self.d, slots, self.family, self.scale_kind, native.dtype_code(self.dtype), 0,
                                        native.ptr(self.locations), native.ptr(self.scales),
                                        native.ptr(self.lognormalizers), native.ptr(self.dofs),
-                                       native.ptr(self.range_risk))
+                                       native.ptr(self.range_risk),
+                                       native.ptr(getattr(self, "inverse_factors", None)))
         return ctypes.byref(views[slots])
 
 

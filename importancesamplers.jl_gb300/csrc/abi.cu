@@ -136,6 +136,15 @@ size_t issm_tc_workspace_bytes(int32_t k, int32_t d) {
     return tc_workspace_bytes(k < 1 ? 1 : k, d < 1 ? 1 : d) + 64;
 }
 
+int issm_invert_factors(const issm_bank *bank, int32_t first, int32_t count, float *out, issm_stream_t stream) {
+    ISSM_TRY(check_bank(bank));
+    if (!out) return ISSM_E_NULL;
+    if (bank->scale_kind != ISSM_SCALE_FACTOR) return ISSM_E_KIND;
+    if (bank->dim > 64) return ISSM_E_UNSUPPORTED;
+    if (first < 0 || count < 0 || first + count > bank->count) return ISSM_E_SIZE;
+    return invert_factors(bank, first, count, out, (cudaStream_t)stream);
+}
+
 static int tc_args_ok(const issm_bank *bank, int precision) {
     if (precision != ISSM_PREC_TF32 && precision != ISSM_PREC_BF16) return ISSM_E_KIND;
     if (bank->dtype != ISSM_F32 || bank->scale_kind != ISSM_SCALE_FACTOR || bank->dim > 64) return ISSM_E_UNSUPPORTED;

@@ -69,6 +69,7 @@ int target_logdensity(const issm_target *t, const void *x, int64_t n, void *out,
 
 // tensor-core mixture density (mixture_tc.cu)
 size_t tc_workspace_bytes(int k, int d);
+int invert_factors(const issm_bank *bk, int first, int count, float *out, cudaStream_t stream);
 int tc_mixture(const issm_bank *bk, const issm_denominator *den, int mode, int first, int last, const void *x,
                int64_t n, const int32_t *slots, int fixed_slot, const void *coef, void *out_logden,
                void *out_generating, void *lognum, uint64_t *failures, int64_t index_base, int precision, void *ws,

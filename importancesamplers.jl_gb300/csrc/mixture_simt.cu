@@ -378,6 +378,53 @@ __device__ bool draw_sample(const MixParams<T> &p, int64_t i, int s, T (&x)[D], 
     return valid;
 }
 
+// Same draw with the component already staged in shared memory (fixed-slot
+// draws: every sample of the launch comes from one proposal).
+template <typename T, int D, bool FACTOR>
+__device__ bool draw_sample_staged(const MixParams<T> &p, int64_t i, const T *__restrict__ c, T (&x)[D],
+                                   uint16_t *reason) {
+    using Ly = Layout<D, FACTOR>;
+    const int d = p.d;
+    T m = T(1);
+    *reason = 0;
+    if (p.family == ISSM_STUDENT_T) {
+        uint16_t r;
+        m = radial_multiplier(c[2], p.rnormals + (size_t)i * p.rn_stride,
+                              p.runiforms ? p.runiforms + (size_t)i * p.ru_stride : nullptr,
+                              p.runiforms != nullptr && p.ru_stride > 0, &r);
+        if (r) {
+            record_failure(p.failures, p.index_base + i + 1, 0, r);
+            m = qnan<T>();
+        }
+    }
+    const T *nz = p.normals + (size_t)i * d;
+    T nm[D];
+#pragma unroll
+    for (int q = 0; q < D; ++q) nm[q] = q < d ? nz[q] * m : T(0);
+    bool valid = true;
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+        if (r < d) {
+            T v = c[Ly::kMu + r];
+            if constexpr (FACTOR) {
+#pragma unroll
+                for (int q = 0; q <= r; ++q) v += c[Ly::tri(r, q)] * nm[q];
+            } else {
+                v += c[Ly::kAux + r] * nm[r];
+            }
+            x[r] = v;
+            valid &= (bool)isfinite(v);
+        }
+    }
+    if (p.samples_out) {
+        T *out = p.samples_out + (size_t)i * d;
+#pragma unroll
+        for (int r = 0; r < D; ++r) if (r < d) out[r] = x[r];
+    }
+    if (!valid) *reason = ISSM_REASON_GENERATED_NONFINITE;
+    return valid;
+}
+
 enum Mode { kModeDenominator = 0, kModeRound = 1, kModeAppend = 2, kModeDraw = 3 };
 
 template <typename T, int D, bool FACTOR>
@@ -393,6 +440,16 @@ __global__ void __launch_bounds__(128) mixture_simt_kernel(MixParams<T> p) {
     for (int r = 0; r < D; ++r) x[r] = T(0);
     const int gen = active ? (p.slots ? p.slots[i] : p.fixed_slot) : 0;
     bool ok = active;
+    if (p.mode == kModeDraw && p.slots == nullptr) {
+        stage_components<T, D, FACTOR>(sm, p, p.fixed_slot, 1);
+        __syncthreads();
+        if (active) {
+            uint16_t reason;
+            if (!draw_sample_staged<T, D, FACTOR>(p, i, sm, x, &reason))
+                record_failure(p.failures, p.index_base + i + 1, 0, reason);
+        }
+        return;
+    }
     if (active) {
         if (p.mode == kModeRound || p.mode == kModeDraw) {
             uint16_t reason;
@@ -490,7 +547,7 @@ static int launch_simt(MixParams<T> p, cudaStream_t stream) {
     const size_t per = (size_t)Ly::kStride * sizeof(T);
     const size_t budget = 96 * 1024;
     int range = p.last_slot - p.first_slot + 1;
-    if (p.mode == kModeDraw) range = 0;
+    if (p.mode == kModeDraw) range = p.slots == nullptr ? 1 : 0;  // fixed-slot draws stage one component
     int chunk = range > 0 ? (int)(budget / per) : 1;
     if (chunk < 1) chunk = 1;
     if (chunk > range && range > 0) chunk = range;

@@ -5,9 +5,10 @@
 //
 // For every component k the reference solves L_k z = x - mu_k by forward
 // substitution (_packed_gaussian_logdensity!, src/native_execution.jl:346-384).
-// Here W_k = L_k^-1 is formed once per call in FP64 (prepare kernel) and the
-// samples are centred on one shift c (the generating / appended slot's mean):
-//   z_k = W_k (x - c) - b_k,   b_k = W_k (mu_k - c)   (b_k in FP32 from FP64),
+// Here W_k = L_k^-1 is formed in FP64 once per slot (invert_factors_kernel;
+// cached by the caller in issm_bank.inverse_factors) and the samples are
+// centred on one shift c (the generating / appended slot's mean):
+//   z_k = W_k (x - c) - b_k,   b_k = W_k (mu_k - c)   (b_k formed per CTA),
 // so each 128-sample tile is one GEMM  D[128 x K*DP] = X'[128 x DP] W^T.
 // Precision forms (FP32 accumulation in TMEM in both):
 //   TF32    one kind::tf32 MMA per K slice, operands rounded to tf32 (RNE);
@@ -32,7 +33,7 @@ struct TcParams {
     int64_t n;
     const float *x;
     const float *w;               // K x DP x DP, row j holds W_k[j, :]
-    const float *b;               // K x DP
+    const float *loc;             // d x K bank locations
     const float *lognorm, *coef, *dofs;
     const int32_t *slots, *group;
     int fixed_slot;
@@ -169,7 +170,14 @@ __global__ void __launch_bounds__(kTcThreads) mixture_tc_kernel(TcParams p) {
                     if (NPART == 2)
                         put_chunk<KIND>(sb + (size_t)(p.chunk + kk) * B_BYTES, row, q, KG, v, true);
                 }
-                for (int e = tid; e < cnt * DP; e += kTcThreads) sbv[e] = p.b[(size_t)k0 * DP + e];
+                // b_k = W_k (mu_k - c), accumulated in FP32 from the cached inverse
+                for (int e = tid; e < cnt * DP; e += kTcThreads) {
+                    const int kk = e / DP, j = e - kk * DP, k = k0 + kk;
+                    const float *wr = p.w + ((size_t)k * DP + j) * DP;
+                    float acc = 0.f;
+                    for (int c = 0; c < p.d; ++c) acc = fmaf(wr[c], p.loc[(size_t)k * p.d + c] - p.center[c], acc);
+                    sbv[e] = acc;
+                }
                 staged_chunk = ch;
             }
             tc::fence_proxy_async();
@@ -269,35 +277,47 @@ __global__ void __launch_bounds__(kTcThreads) mixture_tc_kernel(TcParams p) {
     if (warp == 0) tc::tmem_dealloc(tbase, ncols);
 }
 
-// W_k = L_k^-1 (FP64 forward substitution, one thread per column) and
-// b_k = W_k (mu_k - c), stored as FP32 DP x DP / DP, zero padded.
+// W_k = L_k^-1 in FP64: L_k is staged in shared memory, one thread solves
+// one column by forward substitution; written as FP32 DP x DP, zero padded.
 template <typename T>
-__global__ void prepare_tc_bank_kernel(const T *__restrict__ loc, const T *__restrict__ L, int d, int DP, int first,
-                                       const float *__restrict__ center, float *__restrict__ w,
-                                       float *__restrict__ b) {
+__global__ void invert_factors_kernel(const T *__restrict__ L, int d, int DP, int first, float *__restrict__ w) {
     const int k = first + blockIdx.x;
-    extern __shared__ double wcol[];  // d x d, W column-major
+    extern __shared__ double sm_inv[];
+    double *Ls = sm_inv;            // d x d column-major
+    double *Ws = sm_inv + d * d;    // d x d column-major
     const T *Lk = L + (size_t)k * d * d;
+    for (int e = threadIdx.x; e < d * d; e += blockDim.x) Ls[e] = (double)Lk[e];
+    __syncthreads();
     for (int c = threadIdx.x; c < d; c += blockDim.x) {
-        for (int r = 0; r < d; ++r) {
-            if (r < c) { wcol[r + c * d] = 0.0; continue; }
+        for (int r = 0; r < c; ++r) Ws[r + c * d] = 0.0;
+        for (int r = c; r < d; ++r) {
             double v = (r == c) ? 1.0 : 0.0;
-            for (int q = c; q < r; ++q) v -= (double)Lk[r + (size_t)q * d] * wcol[q + c * d];
-            wcol[r + c * d] = v / (double)Lk[r + (size_t)r * d];
+            for (int q = c; q < r; ++q) v -= Ls[r + q * d] * Ws[q + c * d];
+            Ws[r + c * d] = v / Ls[r + r * d];
         }
     }
     __syncthreads();
     float *wk = w + (size_t)k * DP * DP;
     for (int e = threadIdx.x; e < DP * DP; e += blockDim.x) {
         const int j = e / DP, c = e % DP;
-        wk[e] = (j < d && c < d) ? (float)wcol[j + c * d] : 0.f;
+        wk[e] = (j < d && c < d) ? (float)Ws[j + c * d] : 0.f;
     }
-    for (int j = threadIdx.x; j < DP; j += blockDim.x) {
-        double acc = 0.0;
-        if (j < d)
-            for (int c = 0; c < d; ++c) acc += wcol[j + c * d] * ((double)loc[(size_t)k * d + c] - (double)center[c]);
-        b[(size_t)k * DP + j] = (float)acc;
+}
+
+int invert_factors(const issm_bank *bk, int first, int count, float *out, cudaStream_t stream) {
+    const int d = bk->dim;
+    if (d > 64) return ISSM_E_UNSUPPORTED;
+    const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
+    const size_t smem = 2 * sizeof(double) * d * d;
+    if (count <= 0) return 0;
+    if (bk->dtype == ISSM_F32) {
+        { invert_factors_kernel<float><<<count, 64, smem, stream>>>((const float *)bk->scales, d, DP, first, out);
+          note_launch(); }
+    } else {
+        { invert_factors_kernel<double><<<count, 64, smem, stream>>>((const double *)bk->scales, d, DP, first, out);
+          note_launch(); }
     }
+    return (int)cudaGetLastError();
 }
 
 size_t tc_workspace_bytes(int k, int d) {
@@ -345,8 +365,7 @@ int tc_mixture(const issm_bank *bk, const issm_denominator *den, int mode, int f
     const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
     if (ws_bytes < tc_workspace_bytes(bk->count, d)) return ISSM_E_WORKSPACE;
     float *w = (float *)ws;
-    float *b = w + (size_t)bk->count * DP * DP;
-    float *center = b + (size_t)bk->count * DP;
+    float *center = w + (size_t)bk->count * DP * DP + (size_t)bk->count * DP;
     // shift: the generating (or appended) slot's mean
     const int cslot = (mode == 1) ? first : fixed_slot;
     cudaError_t e = cudaMemsetAsync(center, 0, sizeof(float) * DP, stream);
@@ -354,14 +373,17 @@ int tc_mixture(const issm_bank *bk, const issm_denominator *den, int mode, int f
     e = cudaMemcpyAsync(center, (const float *)bk->locations + (size_t)cslot * d, sizeof(float) * d,
                         cudaMemcpyDeviceToDevice, stream);
     if (e != cudaSuccess) return (int)e;
-    const size_t psmem = sizeof(double) * d * d;
-    { prepare_tc_bank_kernel<float><<<last - first + 1, 64, psmem, stream>>>(
-          (const float *)bk->locations, (const float *)bk->scales, d, DP, first, center, w, b); note_launch(); }
+    if (bk->inverse_factors) {
+        w = const_cast<float *>(bk->inverse_factors);
+    } else {
+        const int st = invert_factors(bk, first, last - first + 1, w, stream);
+        if (st) return st;
+    }
     TcParams p{};
     p.d = d; p.k = bk->count; p.family = bk->family; p.mode = mode;
     p.first_slot = first; p.last_slot = last;
     p.den_kind = den ? den->kind : ISSM_DENOM_FULL;
-    p.n = n; p.x = (const float *)x; p.w = w; p.b = b;
+    p.n = n; p.x = (const float *)x; p.w = w; p.loc = (const float *)bk->locations;
     p.lognorm = (const float *)bk->lognormalizers; p.coef = (const float *)coef; p.dofs = (const float *)bk->dofs;
     p.slots = slots; p.group = den ? den->group_of_slot : nullptr; p.fixed_slot = fixed_slot;
     p.center = center; p.out_logden = (float *)out_logden; p.out_generating = (float *)out_generating;

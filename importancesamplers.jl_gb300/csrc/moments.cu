@@ -198,9 +198,12 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
         for (int i = threadIdx.x; i < m; i += blockDim.x) A[(j + 1 + i) + j * d] /= ljj;
         __syncthreads();
         if (threadIdx.x == 0) A[j + j * d] = ljj;
-        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-            const int i = e % m, c = e / m;
-            if (i >= c) A[(j + 1 + i) + (j + 1 + c) * d] -= A[(j + 1 + i) + j * d] * A[(j + 1 + c) + j * d];
+        // 16 x 16 thread tile: consecutive threads walk a column (contiguous rows)
+        const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+        for (int c = ty; c < m; c += 16) {
+            const double lc = A[(j + 1 + c) + j * d];
+            for (int i = c + ((tx - c) & 15); i < m; i += 16)
+                A[(j + 1 + i) + (j + 1 + c) * d] -= A[(j + 1 + i) + j * d] * lc;
         }
         __syncthreads();
     }

@@ -166,24 +166,33 @@ __global__ void __launch_bounds__(kMtThreads) moments_tc_kernel(const float *__r
     if (warp == 0) tc::tmem_dealloc(tbase, 128);
 }
 
-__global__ void moments_tc_finish_kernel(const float *__restrict__ partial, int blocks, int d,
-                                         const double *__restrict__ center, double *__restrict__ mean,
-                                         double *__restrict__ cov) {
-    __shared__ double s1[65];
-    for (int j = threadIdx.x; j <= 64; j += blockDim.x) {
-        double acc = 0.0;
-        for (int b = 0; b < blocks; ++b) acc += (double)partial[(size_t)b * 65 * kMtCols + 64 * kMtCols + j];
-        s1[j] = acc;  // s1[64] = S0
-    }
+// Partials are [block][65][80] FP32; stage 1 sums them over blocks in FP64
+// (32 entries x 8 block-strided lanes per CTA, coalesced), stage 2 forms the
+// mean and covariance from the 65 x 80 sums.
+__global__ void moments_tc_reduce_kernel(const float *__restrict__ partial, int blocks, double *__restrict__ sums) {
+    __shared__ double acc_s[8][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    const int e = blockIdx.x * 32 + tx;
+    double acc = 0.0;
+    if (e < 65 * kMtCols)
+        for (int b = ty; b < blocks; b += 8) acc += (double)partial[(size_t)b * 65 * kMtCols + e];
+    acc_s[ty][tx] = acc;
     __syncthreads();
-    const double s0 = s1[64];
-    if (blockIdx.x == 0)
-        for (int j = threadIdx.x; j < d; j += blockDim.x) mean[j] = center[j] + s1[j] / s0;
+    if (ty == 0 && e < 65 * kMtCols) {
+        double t = 0.0;
+        for (int r = 0; r < 8; ++r) t += acc_s[r][tx];
+        sums[e] = t;
+    }
+}
+
+__global__ void moments_tc_finish_kernel(const double *__restrict__ sums, int d, const double *__restrict__ center,
+                                         double *__restrict__ mean, double *__restrict__ cov) {
+    const double s0 = sums[64 * kMtCols + 64];
+    for (int j = threadIdx.x; j < d; j += blockDim.x) mean[j] = center[j] + sums[64 * kMtCols + j] / s0;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d * d; e += gridDim.x * blockDim.x) {
         const int r = e % d, c = e / d;
-        double acc = 0.0;
-        for (int b = 0; b < blocks; ++b) acc += (double)partial[(size_t)b * 65 * kMtCols + r * kMtCols + c];
-        cov[e] = acc / s0 - (s1[r] / s0) * (s1[c] / s0);
+        const double mr = sums[64 * kMtCols + r] / s0, mc = sums[64 * kMtCols + c] / s0;
+        cov[e] = sums[r * kMtCols + c] / s0 - mr * mc;
     }
 }
 
@@ -194,7 +203,7 @@ static int moments_tc_blocks(int64_t n, int ts) {
 }
 
 size_t moments_tc_workspace_bytes(int64_t n) {
-    return sizeof(float) * (size_t)moments_tc_blocks(n, 64) * 65 * kMtCols + 64;
+    return sizeof(float) * (size_t)moments_tc_blocks(n, 64) * 65 * kMtCols + sizeof(double) * 65 * kMtCols + 128;
 }
 
 int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *summary, const double *shift,
@@ -219,7 +228,9 @@ int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *su
         { kern<<<blocks, kMtThreads, smem, stream>>>((const float *)x, d, n, (const float *)lw, summary, shift,
                                                      partial, error); note_launch(); }
     }
-    { moments_tc_finish_kernel<<<(d * d + 127) / 128, 128, 0, stream>>>(partial, blocks, d, shift, mean, cov); note_launch(); }
+    double *sums = reinterpret_cast<double *>(partial + (size_t)moments_tc_blocks(n, 64) * 65 * kMtCols);
+    { moments_tc_reduce_kernel<<<(65 * kMtCols + 31) / 32, 256, 0, stream>>>(partial, blocks, sums); note_launch(); }
+    { moments_tc_finish_kernel<<<(d * d + 255) / 256, 256, 0, stream>>>(sums, d, shift, mean, cov); note_launch(); }
     return (int)cudaGetLastError();
 }
 

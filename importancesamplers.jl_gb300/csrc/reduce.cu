@@ -19,31 +19,53 @@ struct Moments3 {
     double m, s, s2;
 };
 
-__device__ __forceinline__ Moments3 merge3(Moments3 a, Moments3 b) {
-    if (a.s == 0.0) return b;
-    if (b.s == 0.0) return a;
-    double M = fmax(a.m, b.m);
-    double l = exp(a.m - M), r = exp(b.m - M);
-    return Moments3{M, l * a.s + r * b.s, (l * l) * a.s2 + (r * r) * b.s2};
+// exp of a difference of two maxima; the maxima are log weights of dtype T,
+// so the factor is formed in T (FP64 exponentials are slow on this GPU and
+// add nothing for FP32 data).
+template <typename T> __device__ __forceinline__ double scale_factor(double a, double b) {
+    return (double)dexp((T)(a - b));
 }
 
-__device__ __forceinline__ Moments3 shfl3(Moments3 v, int off) {
-    return Moments3{__shfl_down_sync(0xffffffffu, v.m, off), __shfl_down_sync(0xffffffffu, v.s, off),
-                    __shfl_down_sync(0xffffffffu, v.s2, off)};
-}
-
-__device__ Moments3 block_merge3(Moments3 v) {
-    __shared__ Moments3 warp_part[32];
-    for (int off = 16; off > 0; off >>= 1) v = merge3(v, shfl3(v, off));
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) warp_part[warp] = v;
-    __syncthreads();
-    const int nw = (blockDim.x + 31) >> 5;
-    if (warp == 0) {
-        v = lane < nw ? warp_part[lane] : Moments3{-INFINITY, 0.0, 0.0};
-        for (int off = 16; off > 0; off >>= 1) v = merge3(v, shfl3(v, off));
-    }
+__device__ __forceinline__ double warp_max(double v) {
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
     return v;
+}
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Block-wide merge: take the block maximum first, then rescale every
+// thread's sums once and add them (one exponential per thread).
+template <typename T> __device__ Moments3 block_merge3(Moments3 v) {
+    __shared__ double red[3][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    double m = warp_max(v.s == 0.0 ? -INFINITY : v.m);
+    if (lane == 0) red[0][warp] = m;
+    __syncthreads();
+    double M = -INFINITY;
+    for (int w = 0; w < nw; ++w) M = fmax(M, red[0][w]);
+    double s = 0.0, s2 = 0.0;
+    if (v.s != 0.0) {
+        const double f = scale_factor<T>(v.m, M);
+        s = v.s * f;
+        s2 = v.s2 * (f * f);
+    }
+    s = warp_sum(s);
+    s2 = warp_sum(s2);
+    __syncthreads();
+    if (lane == 0) {
+        red[1][warp] = s;
+        red[2][warp] = s2;
+    }
+    __syncthreads();
+    double ts = 0.0, ts2 = 0.0;
+    for (int w = 0; w < nw; ++w) {
+        ts += red[1][w];
+        ts2 += red[2][w];
+    }
+    __syncthreads();
+    return Moments3{M, ts, ts2};
 }
 
 template <typename T>
@@ -67,8 +89,7 @@ __global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, 
         s += e;
         s2 += e * e;
     }
-    Moments3 v{(double)m, s, s2};
-    v = block_merge3(v);
+    Moments3 v = block_merge3<T>(Moments3{(double)m, s, s2});
     __shared__ bool last;
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = v;
@@ -79,11 +100,25 @@ __global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, 
     __syncthreads();
     if (!last) return;
     __threadfence();
-    Moments3 acc{-INFINITY, 0.0, 0.0};
+    // the last block merges the per-block partials the same way
     const volatile double *pv = reinterpret_cast<const volatile double *>(partials);
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-        acc = merge3(acc, Moments3{pv[3 * b], pv[3 * b + 1], pv[3 * b + 2]});
-    acc = block_merge3(acc);
+    double pm = -INFINITY, ps = 0.0, ps2 = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        const double bm = pv[3 * b], bs = pv[3 * b + 1], bs2 = pv[3 * b + 2];
+        if (bs == 0.0) continue;
+        if (ps == 0.0 || bm > pm) {
+            if (ps != 0.0) {
+                const double f = scale_factor<T>(pm, bm);
+                ps *= f;
+                ps2 *= f * f;
+            }
+            pm = bm;
+        }
+        const double f = scale_factor<T>(bm, pm);
+        ps += bs * f;
+        ps2 += bs2 * (f * f);
+    }
+    const Moments3 acc = block_merge3<T>(Moments3{pm, ps, ps2});
     if (threadIdx.x == 0) {
         out[0] = acc.s == 0.0 ? -INFINITY : acc.m;
         out[1] = acc.s;

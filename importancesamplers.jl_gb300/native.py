@@ -41,7 +41,7 @@ class Bank(C.Structure):
     _fields_ = [("dim", C.c_int32), ("count", C.c_int32), ("family", C.c_int32),
                 ("scale_kind", C.c_int32), ("dtype", C.c_int32), ("reserved", C.c_int32),
                 ("locations", C.c_void_p), ("scales", C.c_void_p), ("lognormalizers", C.c_void_p),
-                ("dofs", C.c_void_p), ("range_risk", C.c_void_p)]
+                ("dofs", C.c_void_p), ("range_risk", C.c_void_p), ("inverse_factors", C.c_void_p)]
 
 
 class Denominator(C.Structure):
@@ -92,6 +92,7 @@ SIGNATURES = [
     ("issm_target_logdensity", C.c_int, [C.POINTER(Target), _p, _i64, _p, _p]),
     ("issm_tc_selftest", C.c_int, [_p, _p, _p, _i32, _i32, _i32, _p, _p]),
     ("issm_tc_workspace_bytes", _sz, [_i32, _i32]),
+    ("issm_invert_factors", C.c_int, [_bank, _i32, _i32, _p, _p]),
     ("issm_mixture_logdensity_ws", C.c_int, [_bank, _den, _p, _i64, _p, _i32, _p, _p, _p, _i64, _i32, _p, _sz,
                                              _p]),
     ("issm_amis_append_ws", C.c_int, [_bank, _i32, _p, _p, _i64, _p, _p, _i32, _p, _sz, _p]),

@@ -235,7 +235,7 @@ def _run_static(s):
     rn, ru = _radial_buffers(s, n, dt)
     samples, lw, pid = ops.mis_round(db, s.den, slots, normals, None, rn, s.rn_stride, ru, s.ru_stride, fail,
                                      s.precision)
-    values = s.bound_target.evaluate(samples)
+    values = s.bound_target.evaluate(samples, precision=s.precision)
     ops.add_target_values(lw, values, fail)
     _raise_failures(fail.cpu().numpy())
     scheme = type(alg.mis_scheme).__name__
@@ -287,6 +287,7 @@ def _run_moment(s):
     h.locations[0].copy_(loc0)
     h.scales[0].copy_(fac0)
     h.lognormalizers[0].copy_(ln0)
+    h.attach_inverse_factors(0, 1)
     s.round_failures.zero_()
     s.round_ids.copy_(s.round_ids_init)
     for t in range(s.rounds):
@@ -302,7 +303,7 @@ def _run_moment(s):
             ops.draw(h, normals, n_new, fixed_slot=t, radial_normals=rn, rn_stride=s.rn_stride,
                      radial_uniforms=ru, ru_stride=s.ru_stride, failures=fail, out=x_new, bank_ref=view)
         with _Span(s, "target", n_new * (d + 1) * es):
-            s.bound_target.evaluate(x_new, out=s.logtargets[n_old:n_tot])
+            s.bound_target.evaluate(x_new, out=s.logtargets[n_old:n_tot], precision=s.precision)
             ops.check_target_values(s.logtargets[n_old:n_tot], s.round_ids[n_old:n_tot], fail)
         if is_npmc:
             den = ops.denominator(native.DENOM_GENERATING)
@@ -337,6 +338,8 @@ def _run_moment(s):
         with _Span(s, "fit", 3 * d * d * 8):
             ops.fit_factor(s.mean, s.cov, h.scales[t], out_loc, out_fac, out_ln, dof=h.dof,
                            logconstant=h.logconstant, failures=fail, failure_index=n_tot + 1)
+            if not last and s.precision != native.PREC_NATIVE:
+                h.attach_inverse_factors(t + 1, 1)
     words = s.round_failures.cpu().numpy()
     summaries = s.summaries.cpu().numpy()
     if s.precision != native.PREC_NATIVE:
@@ -429,7 +432,7 @@ def _run_dmpmc(s):
         x, lw, pid = ops.mis_round(db, den, s.slots[r], normals, None, rn, s.rn_stride, ru, s.ru_stride, fail,
                                    s.precision, samples=s.samples[lo:hi], logweights=s.logweights[lo:hi],
                                    proposal_ids_out=s.proposal_ids[lo:hi])
-        s.bound_target.evaluate(x, out=_scratch(s, n, dt))
+        s.bound_target.evaluate(x, out=_scratch(s, n, dt), precision=s.precision)
         ops.add_target_values(lw, s._scratch[:n], fail)
         ops.logweight_summary(lw, out=s.summaries[r])
         if local:

@@ -20,7 +20,7 @@ class LogTarget:
     def bind(self, device, dtype):
         return self
 
-    def evaluate(self, samples, out=None):
+    def evaluate(self, samples, out=None, precision=None):
         v = self.batch(samples)
         if not isinstance(v, torch.Tensor) or v.shape != (samples.shape[0],):
             raise ValueError("a batch target must return one log density per sample")
@@ -56,8 +56,39 @@ class _Bound:
     def __init__(self, target, struct, ta, tb):
         self.target, self.struct, self.keep = target, struct, (ta, tb)
 
-    def evaluate(self, samples, out=None):
+    def evaluate(self, samples, out=None, precision=None):
         return ops.target_logdensity(self.struct, samples, out)
+
+
+class _BoundBank:
+    """A normalised target that is itself a radial mixture: evaluated by the
+    same balance-heuristic kernels as the proposals (SIMT or tensor core)."""
+
+    def __init__(self, bank, coef):
+        self.bank, self.coef = bank, coef
+        kind = native.DENOM_GENERATING if coef is None else native.DENOM_FULL
+        self.den = ops.denominator(kind, coef)
+
+    def evaluate(self, samples, out=None, precision=None):
+        prec = native.PREC_NATIVE if precision is None else precision
+        if prec != native.PREC_NATIVE and (self.bank.scale_kind != native.SCALE_FACTOR or samples.dtype != torch.float32):
+            prec = native.PREC_NATIVE
+        return ops.mixture_logdensity(self.bank, self.den, samples, fixed_slot=0, precision=prec, out=out)
+
+
+def _bank_target(key_store, key, proposals, coef_value, device, dtype):
+    if key not in key_store:
+        from .bank import pack_proposals
+
+        npdt = np.float32 if dtype == torch.float32 else np.float64
+        props = [p(npdt) for p in proposals]
+        bank = pack_proposals(props, device)
+        bank.attach_inverse_factors()
+        coef = None
+        if coef_value is not None:
+            coef = torch.full((bank.count,), coef_value, dtype=dtype, device=device)
+        key_store[key] = _BoundBank(bank, coef)
+    return key_store[key]
 
 
 def _colmajor(a):
@@ -66,10 +97,18 @@ def _colmajor(a):
 
 
 class StandardNormalTarget(_NativeTarget):
+    """N(0, I), normalised: evaluated as a one-slot factor bank."""
     kind = native.TARGET_STD_NORMAL
 
     def __init__(self, d):
         super().__init__(d)
+
+    def bind(self, device, dtype):
+        from .proposals import FactorGaussian
+
+        d = self.d
+        return _bank_target(self._bound, ("bank", str(device), dtype),
+                            [lambda t: FactorGaussian(np.zeros(d, dtype=t), np.eye(d, dtype=t))], None, device, dtype)
 
 
 class QuadraticTarget(_NativeTarget):
@@ -82,16 +121,27 @@ class QuadraticTarget(_NativeTarget):
 
 
 class GaussianMixtureTarget(_NativeTarget):
-    """Equal-weight mixture of N(mean_j, I); means is (J, d)."""
+    """Equal-weight mixture of N(mean_j, I); means is (J, d). Evaluated as a
+    balance-heuristic bank with coefficients -log J."""
     kind = native.TARGET_GAUSS_MIX
 
     def __init__(self, means):
         m = np.atleast_2d(np.asarray(means, dtype=np.float64))
         super().__init__(m.shape[1], count=m.shape[0], a=m)
+        self.means = m
+
+    def bind(self, device, dtype):
+        from .proposals import FactorGaussian
+
+        d = self.d
+        props = [lambda t, mu=mu: FactorGaussian(mu.astype(t), np.eye(d, dtype=t)) for mu in self.means]
+        return _bank_target(self._bound, ("bank", str(device), dtype), props, -float(np.log(len(self.means))),
+                            device, dtype)
 
 
 class StudentTTarget(_NativeTarget):
-    """Normalised multivariate t with location, lower scale factor L and nu."""
+    """Normalised multivariate t with location, lower scale factor L and nu:
+    a one-slot factor Student-t bank."""
     kind = native.TARGET_STUDENT_T
 
     def __init__(self, location, factor, dof):
@@ -101,6 +151,13 @@ class StudentTTarget(_NativeTarget):
         logc = student_t_logconstant(float(dof), d) - float(np.sum(np.log(np.diag(L))))
         super().__init__(d, a=loc, b=_colmajor(L), p0=dof, p1=logc)
         self.location, self.factor, self.dof = loc, L, float(dof)
+
+    def bind(self, device, dtype):
+        from .proposals import FactorStudentT
+
+        loc, L, nu = self.location, self.factor, self.dof
+        return _bank_target(self._bound, ("bank", str(device), dtype),
+                            [lambda t: FactorStudentT(t(nu), loc.astype(t), L.astype(t))], None, device, dtype)
 
 
 class LinearRegressionTarget(_NativeTarget):

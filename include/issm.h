@@ -100,6 +100,11 @@ typedef struct issm_bank {
     const void *lognormalizers;  /* K                                     */
     const void *dofs;            /* K or NULL                             */
     const uint8_t *range_risk;   /* K or NULL                             */
+    /* Optional FP32 inverse factors W_k = L_k^-1 for the tensor-core forms,
+     * K x DP x DP row-major (row j holds W_k[j, :]), DP = 16 / 32 / 64 for
+     * d <= 16 / 32 / 64, zero padded (issm_invert_factors writes them).
+     * NULL: the tensor-core entry points form them per call. */
+    const float *inverse_factors;
 } issm_bank;
 
 typedef struct issm_denominator {
@@ -181,6 +186,11 @@ int issm_mixture_logdensity(const issm_bank *bank, const issm_denominator *den,
  * timed-out tensor-core completion wait sets to 1 (zero the workspace once
  * when it is created). workspace_bytes >= issm_tc_workspace_bytes(K, d). */
 size_t issm_tc_workspace_bytes(int32_t k, int32_t d);
+/* W_k = L_k^-1 for factor slots [first, first + count) of an FP32 or FP64
+ * factor bank, formed in FP64 and written as FP32 into out (K x DP x DP,
+ * layout of issm_bank.inverse_factors). */
+int issm_invert_factors(const issm_bank *bank, int32_t first, int32_t count,
+                        float *out, issm_stream_t stream);
 int issm_mixture_logdensity_ws(const issm_bank *bank, const issm_denominator *den,
                                const void *x, int64_t n, const int32_t *slots,
                                int32_t fixed_slot, void *out_logden,
