@@ -310,6 +310,10 @@ int invert_factors(const issm_bank *bk, int first, int count, float *out, cudaSt
     const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
     const size_t smem = 2 * sizeof(double) * d * d;
     if (count <= 0) return 0;
+    cudaError_t e = cudaFuncSetAttribute(bk->dtype == ISSM_F32 ? (const void *)invert_factors_kernel<float>
+                                                               : (const void *)invert_factors_kernel<double>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int)e;
     if (bk->dtype == ISSM_F32) {
         { invert_factors_kernel<float><<<count, 64, smem, stream>>>((const float *)bk->scales, d, DP, first, out);
           note_launch(); }
