@@ -370,9 +370,10 @@ int issm_weighted_moments(const void *x, int32_t d, int64_t n, const void *logwe
                             (cudaStream_t)stream);
 }
 
-int issm_fit_factor(const double *mean, const double *cov, int32_t d, const void *previous_factor, double dof,
-                    double logconstant, int32_t dtype, void *out_location, void *out_factor,
-                    void *out_lognormalizer, uint64_t *failures, int64_t failure_index, issm_stream_t stream) {
+int issm_fit_factor_ex(const double *mean, const double *cov, int32_t d, const void *previous_factor, double dof,
+                       double logconstant, int32_t dtype, void *out_location, void *out_factor,
+                       void *out_lognormalizer, float *out_inverse, uint64_t *failures, int64_t failure_index,
+                       issm_stream_t stream) {
     if (d < 1) return ISSM_E_SIZE;
     if (d > 64) return ISSM_E_UNSUPPORTED;
     if (!mean || !cov || !previous_factor || !out_location || !out_factor || !out_lognormalizer)
@@ -380,7 +381,14 @@ int issm_fit_factor(const double *mean, const double *cov, int32_t d, const void
     if (dof > 0.0 && !(dof > 2.0)) return ISSM_E_KIND;
     ISSM_TRY(check_dtype(dtype));
     return fit_factor(mean, cov, d, previous_factor, dof, logconstant, dtype, out_location, out_factor,
-                      out_lognormalizer, failures, failure_index, (cudaStream_t)stream);
+                      out_lognormalizer, failures, failure_index, out_inverse, (cudaStream_t)stream);
+}
+
+int issm_fit_factor(const double *mean, const double *cov, int32_t d, const void *previous_factor, double dof,
+                    double logconstant, int32_t dtype, void *out_location, void *out_factor,
+                    void *out_lognormalizer, uint64_t *failures, int64_t failure_index, issm_stream_t stream) {
+    return issm_fit_factor_ex(mean, cov, d, previous_factor, dof, logconstant, dtype, out_location, out_factor,
+                              out_lognormalizer, nullptr, failures, failure_index, stream);
 }
 
 int issm_target_logdensity(const issm_target *target, const void *x, int64_t n, void *out, issm_stream_t stream) {

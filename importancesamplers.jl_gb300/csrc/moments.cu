@@ -149,7 +149,8 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
                                                          const double *__restrict__ cov, int d,
                                                          const T *__restrict__ prev, double dof, double logconst,
                                                          double reg, T *out_loc, T *out_factor, T *out_lognorm,
-                                                         uint64_t *failures, int64_t failure_index) {
+                                                         uint64_t *failures, int64_t failure_index,
+                                                         float *out_inverse) {
     extern __shared__ __align__(16) double A[];  // d x d column-major
     __shared__ double red[256];
     __shared__ int bad;
@@ -188,22 +189,59 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
     }
     for (int c = threadIdx.x; c < d; c += blockDim.x) A[c + c * d] += ridge;
     __syncthreads();
-    // right-looking Cholesky: every thread derives the pivot itself, so each
-    // column costs two barriers
-    for (int j = 0; j < d; ++j) {
-        const double djj = A[j + j * d];
-        const double ljj = sqrt(djj);
-        if (threadIdx.x == 0 && (!(djj > 0.0) || !isfinite(djj))) bad = 1;
-        const int m = d - j - 1;
-        for (int i = threadIdx.x; i < m; i += blockDim.x) A[(j + 1 + i) + j * d] /= ljj;
+    // Blocked right-looking Cholesky (8-column panels): factor the diagonal
+    // block in one warp, solve the panel below it one row per thread, then
+    // the rank-8 trailing update; three barriers per panel. FP64 throughput is
+    // low on this GPU, so the sequential part is kept to the 8 x 8 blocks.
+    __shared__ double inv_diag[8];
+    for (int kb = 0; kb < d; kb += 8) {
+        const int nb = min(8, d - kb);
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            for (int j = kb; j < kb + nb; ++j) {
+                const double djj = A[j + j * d];
+                const double ljj = sqrt(djj);
+                const double rl = 1.0 / ljj;
+                if (lane == 0) {
+                    if (!(djj > 0.0) || !isfinite(djj)) bad = 1;
+                    inv_diag[j - kb] = rl;
+                }
+                const int rows = kb + nb - 1 - j;
+                if (lane < rows) A[(j + 1 + lane) + j * d] *= rl;
+                __syncwarp();
+                if (lane == 0) A[j + j * d] = ljj;
+                // update the rest of the diagonal block (rows, cols > j)
+                for (int e = lane; e < rows * rows; e += 32) {
+                    const int i = e % rows, c = e / rows;
+                    if (i >= c) A[(j + 1 + i) + (j + 1 + c) * d] -= A[(j + 1 + i) + j * d] * A[(j + 1 + c) + j * d];
+                }
+                __syncwarp();
+            }
+        }
         __syncthreads();
-        if (threadIdx.x == 0) A[j + j * d] = ljj;
-        // 16 x 16 thread tile: consecutive threads walk a column (contiguous rows)
+        // panel: rows below the block, L[i, kb:kb+nb] = A[i, kb:kb+nb] L_bb^-T
+        for (int i = kb + nb + threadIdx.x; i < d; i += blockDim.x) {
+            for (int c = 0; c < nb; ++c) {
+                double v = A[i + (kb + c) * d];
+                for (int q = 0; q < c; ++q) v -= A[i + (kb + q) * d] * A[(kb + c) + (kb + q) * d];
+                A[i + (kb + c) * d] = v * inv_diag[c];
+            }
+        }
+        __syncthreads();
+        // trailing rank-nb update of the lower triangle, 16 x 16 thread tile
+        const int m = d - kb - nb, base = kb + nb;
         const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
         for (int c = ty; c < m; c += 16) {
-            const double lc = A[(j + 1 + c) + j * d];
-            for (int i = c + ((tx - c) & 15); i < m; i += 16)
-                A[(j + 1 + i) + (j + 1 + c) * d] -= A[(j + 1 + i) + j * d] * lc;
+            double lc[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) lc[q] = q < nb ? A[(base + c) + (kb + q) * d] : 0.0;
+            for (int i = c + ((tx - c) & 15); i < m; i += 16) {
+                double acc = A[(base + i) + (base + c) * d];
+#pragma unroll
+                for (int q = 0; q < 8; ++q)
+                    if (q < nb) acc -= A[(base + i) + (kb + q) * d] * lc[q];
+                A[(base + i) + (base + c) * d] = acc;
+            }
         }
         __syncthreads();
     }
@@ -242,23 +280,39 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
         const bool valid = !bad && !invalid && isfinite((double)(T)ln);
         if (!valid) record_failure(failures, failure_index, 0, ISSM_REASON_MOMENT_FIT_INVALID);
     }
+    // inverse factor for the tensor-core forms: W = (f L)^-1 in FP32 from the
+    // stored factor, one column per thread, DP x DP row-major zero padded
+    if (out_inverse != nullptr) {
+        const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
+        for (int e = threadIdx.x; e < DP * DP; e += blockDim.x) out_inverse[e] = 0.f;
+        __syncthreads();
+        for (int c = threadIdx.x; c < d; c += blockDim.x) {
+            float w[64];
+            for (int r = c; r < d; ++r) {
+                float v = (r == c) ? 1.f : 0.f;
+                for (int q = c; q < r; ++q) v -= (float)(A[r + q * d] * f) * w[q];
+                w[r] = v / (float)(A[r + r * d] * f);
+                out_inverse[r * DP + c] = w[r];
+            }
+        }
+    }
 }
 
 int fit_factor(const double *mean, const double *cov, int d, const void *prev, double dof, double logconst,
                int dtype, void *out_loc, void *out_factor, void *out_lognorm, uint64_t *failures,
-               int64_t failure_index, cudaStream_t stream) {
+               int64_t failure_index, float *out_inverse, cudaStream_t stream) {
     if (d > 64) return ISSM_E_UNSUPPORTED;
     const size_t smem = sizeof(double) * (size_t)d * d;
     if (dtype == ISSM_F32) {
         const double reg = sqrt((double)FLT_EPSILON);
         { fit_factor_kernel<float><<<1, 256, smem, stream>>>(mean, cov, d, (const float *)prev, dof, logconst, reg,
                                                            (float *)out_loc, (float *)out_factor,
-                                                           (float *)out_lognorm, failures, failure_index); note_launch(); }
+                                                           (float *)out_lognorm, failures, failure_index, out_inverse); note_launch(); }
     } else {
         const double reg = sqrt(DBL_EPSILON);
         { fit_factor_kernel<double><<<1, 256, smem, stream>>>(mean, cov, d, (const double *)prev, dof, logconst,
                                                             reg, (double *)out_loc, (double *)out_factor,
-                                                            (double *)out_lognorm, failures, failure_index); note_launch(); }
+                                                            (double *)out_lognorm, failures, failure_index, out_inverse); note_launch(); }
     }
     return (int)cudaGetLastError();
 }

@@ -336,10 +336,11 @@ def _run_moment(s):
         out_fac = s.cand_factor if last else h.scales[t + 1]
         out_ln = s.cand_lognorm if last else h.lognormalizers[t + 1:t + 2]
         with _Span(s, "fit", 3 * d * d * 8):
+            inv = None
+            if not last and s.precision != native.PREC_NATIVE and getattr(h, "inverse_factors", None) is not None:
+                inv = h.inverse_factors[t + 1]
             ops.fit_factor(s.mean, s.cov, h.scales[t], out_loc, out_fac, out_ln, dof=h.dof,
-                           logconstant=h.logconstant, failures=fail, failure_index=n_tot + 1)
-            if not last and s.precision != native.PREC_NATIVE:
-                h.attach_inverse_factors(t + 1, 1)
+                           logconstant=h.logconstant, failures=fail, failure_index=n_tot + 1, out_inverse=inv)
     words = s.round_failures.cpu().numpy()
     summaries = s.summaries.cpu().numpy()
     if s.precision != native.PREC_NATIVE:

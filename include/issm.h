@@ -347,6 +347,15 @@ int issm_fit_factor(const double *mean, const double *cov, int32_t d,
                     void *out_factor, void *out_lognormalizer,
                     uint64_t *failures, int64_t failure_index,
                     issm_stream_t stream);
+/* As issm_fit_factor, also writing the FP32 inverse of the new factor
+ * (issm_bank.inverse_factors layout, one slot) when out_inverse != NULL, so a
+ * proposal history keeps its tensor-core operands current. */
+int issm_fit_factor_ex(const double *mean, const double *cov, int32_t d,
+                       const void *previous_factor, double dof,
+                       double logconstant, int32_t dtype, void *out_location,
+                       void *out_factor, void *out_lognormalizer,
+                       float *out_inverse, uint64_t *failures,
+                       int64_t failure_index, issm_stream_t stream);
 
 /* ---- built-in batch targets ------------------------------------------------
  * Native equivalents of the batch callbacks the benchmark workloads pass to

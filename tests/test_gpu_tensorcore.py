@@ -141,3 +141,31 @@ def test_tc_amis_matches_native_form(issm, cuda, prec):
         out[name] = (r.diagnostics["round_lognormalizers"][-1], issm.mean(r).cpu().numpy())
     assert abs(out["native"][0] - out[prec][0]) < 2e-2
     assert np.max(np.abs(out["native"][1] - out[prec][1])) < 5e-2
+
+
+@pytest.mark.parametrize("d", [3, 16, 40, 64])
+def test_fit_factor_writes_inverse(issm, orc, cuda, d):
+    """The FP64 blocked Cholesky matches the oracle and the FP32 inverse it
+    writes for the tensor-core forms inverts the stored factor."""
+    rng = np.random.default_rng(d + 1)
+    A = rng.normal(size=(d, d))
+    cov = A @ A.T / d + 0.3 * np.eye(d)
+    mean = rng.normal(size=d)
+    prev = np.linalg.cholesky(cov + np.eye(d)).astype(np.float32)
+    st, L, ln = orc.fit_factor(mean, cov, prev.astype(np.float64), regularization=float(np.sqrt(np.finfo(np.float32).eps)))
+    dp = 16 if d <= 16 else 32 if d <= 32 else 64
+    loc = torch.empty(d, dtype=torch.float32, device=cuda)
+    fac = torch.empty(d, d, dtype=torch.float32, device=cuda)
+    lnt = torch.empty(1, dtype=torch.float32, device=cuda)
+    inv = torch.full((dp, dp), float("nan"), dtype=torch.float32, device=cuda)
+    fail = issm.ops.new_failures(cuda)
+    issm.ops.fit_factor(torch.tensor(mean, device=cuda), torch.tensor(cov, device=cuda),
+                        torch.tensor(np.ascontiguousarray(prev.T), device=cuda), loc, fac, lnt, failures=fail,
+                        out_inverse=inv)
+    torch.cuda.synchronize()
+    assert st == 0 and int(fail[0].item()) == 0
+    Lg = fac.double().cpu().numpy().T
+    assert np.allclose(Lg, L, rtol=1e-6, atol=1e-6)
+    W = inv.double().cpu().numpy()
+    assert np.all(W[d:, :] == 0) and np.all(W[:, d:] == 0)
+    assert np.allclose(W[:d, :d] @ Lg, np.eye(d), atol=1e-4)
