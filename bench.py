@@ -182,8 +182,9 @@ def run_gb300(args):
 
     def step():
         # each step restarts from the same initial proposal (no carried adaptation)
-        sampler.committed = tuple(t.clone() for t in sampler.initial) if hasattr(sampler, "initial") else \
-            sampler.committed
+        if hasattr(sampler, "initial"):
+            for dst, src in zip(sampler.committed, sampler.initial):
+                dst.copy_(src)
         return issm.importance_sample_(sampler)
 
     sampler.initial = tuple(t.clone() for t in sampler.committed)
@@ -195,7 +196,7 @@ def run_gb300(args):
     with ClockSampler(dev.index) as clocks:
         barrier()
         torch.cuda.synchronize()
-        l0 = issm.native.lib().issm_kernel_launches()
+        l0 = issm.native.launches()
         start = torch.cuda.Event(enable_timing=True)
         end = torch.cuda.Event(enable_timing=True)
         start.record(stream)
@@ -204,7 +205,7 @@ def run_gb300(args):
         end.record(stream)
         torch.cuda.synchronize()
         barrier()
-        l1 = issm.native.lib().issm_kernel_launches()
+        l1 = issm.native.launches()
     ms = start.elapsed_time(end) / args.steps
     if world > 1:
         t = torch.tensor([ms], device=dev)

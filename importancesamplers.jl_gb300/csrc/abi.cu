@@ -84,14 +84,35 @@ int issm_fill_normals(uint64_t seed, uint64_t offset, int64_t n, void *out, int3
     if (n < 0) return ISSM_E_SIZE;
     if (n > 0 && !out) return ISSM_E_NULL;
     ISSM_TRY(check_dtype(dtype));
-    return fill_normals(seed, offset, n, out, dtype, (cudaStream_t)stream);
+    return fill_normals(seed, nullptr, offset, n, out, dtype, (cudaStream_t)stream);
 }
 
 int issm_fill_uniforms(uint64_t seed, uint64_t offset, int64_t n, void *out, int32_t dtype, issm_stream_t stream) {
     if (n < 0) return ISSM_E_SIZE;
     if (n > 0 && !out) return ISSM_E_NULL;
     ISSM_TRY(check_dtype(dtype));
-    return fill_uniforms(seed, offset, n, out, dtype, (cudaStream_t)stream);
+    return fill_uniforms(seed, nullptr, offset, n, out, dtype, (cudaStream_t)stream);
+}
+
+int issm_fill_normals_at(uint64_t seed, const uint64_t *offset_base, uint64_t offset, int64_t n, void *out,
+                         int32_t dtype, issm_stream_t stream) {
+    if (n < 0) return ISSM_E_SIZE;
+    if (n > 0 && (!out || !offset_base)) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return fill_normals(seed, offset_base, offset, n, out, dtype, (cudaStream_t)stream);
+}
+
+int issm_fill_uniforms_at(uint64_t seed, const uint64_t *offset_base, uint64_t offset, int64_t n, void *out,
+                          int32_t dtype, issm_stream_t stream) {
+    if (n < 0) return ISSM_E_SIZE;
+    if (n > 0 && (!out || !offset_base)) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return fill_uniforms(seed, offset_base, offset, n, out, dtype, (cudaStream_t)stream);
+}
+
+int issm_counter_advance(uint64_t *counter, uint64_t increment, issm_stream_t stream) {
+    if (!counter) return ISSM_E_NULL;
+    return counter_advance(counter, increment, (cudaStream_t)stream);
 }
 
 int issm_static_assign(const void *cdf, int32_t k, const void *uniforms, int64_t n, int32_t stratified,

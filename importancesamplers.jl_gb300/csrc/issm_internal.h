@@ -85,7 +85,10 @@ int tc_gemm_selftest(const float *a, const float *b, float *c, int n, int k, int
                      cudaStream_t stream);
 
 // random streams (rng.cu)
-int fill_normals(uint64_t seed, uint64_t offset, int64_t n, void *out, int dtype, cudaStream_t stream);
-int fill_uniforms(uint64_t seed, uint64_t offset, int64_t n, void *out, int dtype, cudaStream_t stream);
+int fill_normals(uint64_t seed, const uint64_t *base, uint64_t offset, int64_t n, void *out, int dtype,
+                 cudaStream_t stream);
+int fill_uniforms(uint64_t seed, const uint64_t *base, uint64_t offset, int64_t n, void *out, int dtype,
+                  cudaStream_t stream);
+int counter_advance(uint64_t *counter, uint64_t inc, cudaStream_t stream);
 
 }  // namespace issm

@@ -26,7 +26,8 @@ __device__ __forceinline__ uint4 philox4x32_10(uint64_t counter, uint64_t seed) 
 
 // Each thread evaluates one Philox block and writes every element of the
 // requested range that the block covers (4 per block in FP32, 2 in FP64).
-__global__ void normals_f64_kernel(uint64_t seed, uint64_t offset, int64_t n, double *out) {
+__global__ void normals_f64_kernel(uint64_t seed, const uint64_t *base, uint64_t offset, int64_t n, double *out) {
+    if (base) offset += *base;
     const uint64_t b0 = offset >> 1, b1 = (offset + (uint64_t)n - 1) >> 1;
     const int64_t nb = (int64_t)(b1 - b0 + 1);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -45,7 +46,8 @@ __global__ void normals_f64_kernel(uint64_t seed, uint64_t offset, int64_t n, do
     }
 }
 
-__global__ void normals_f32_kernel(uint64_t seed, uint64_t offset, int64_t n, float *out) {
+__global__ void normals_f32_kernel(uint64_t seed, const uint64_t *base, uint64_t offset, int64_t n, float *out) {
+    if (base) offset += *base;
     const uint64_t b0 = offset >> 2, b1 = (offset + (uint64_t)n - 1) >> 2;
     const int64_t nb = (int64_t)(b1 - b0 + 1);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -68,7 +70,8 @@ __global__ void normals_f32_kernel(uint64_t seed, uint64_t offset, int64_t n, fl
     }
 }
 
-__global__ void uniforms_f64_kernel(uint64_t seed, uint64_t offset, int64_t n, double *out) {
+__global__ void uniforms_f64_kernel(uint64_t seed, const uint64_t *base, uint64_t offset, int64_t n, double *out) {
+    if (base) offset += *base;
     const uint64_t b0 = offset >> 1, b1 = (offset + (uint64_t)n - 1) >> 1;
     const int64_t nb = (int64_t)(b1 - b0 + 1);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -82,7 +85,8 @@ __global__ void uniforms_f64_kernel(uint64_t seed, uint64_t offset, int64_t n, d
     }
 }
 
-__global__ void uniforms_f32_kernel(uint64_t seed, uint64_t offset, int64_t n, float *out) {
+__global__ void uniforms_f32_kernel(uint64_t seed, const uint64_t *base, uint64_t offset, int64_t n, float *out) {
+    if (base) offset += *base;
     const uint64_t b0 = offset >> 2, b1 = (offset + (uint64_t)n - 1) >> 2;
     const int64_t nb = (int64_t)(b1 - b0 + 1);
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -99,19 +103,28 @@ __global__ void uniforms_f32_kernel(uint64_t seed, uint64_t offset, int64_t n, f
     }
 }
 
-int fill_normals(uint64_t seed, uint64_t offset, int64_t n, void *out, int dtype, cudaStream_t stream) {
+int fill_normals(uint64_t seed, const uint64_t *base, uint64_t offset, int64_t n, void *out, int dtype,
+                 cudaStream_t stream) {
     if (n <= 0) return 0;
     const int blocks = grid_for(n / (dtype == ISSM_F32 ? 4 : 2) + 2, 256, 8);
-    if (dtype == ISSM_F32) { normals_f32_kernel<<<blocks, 256, 0, stream>>>(seed, offset, n, (float *)out); note_launch(); }
-    else { normals_f64_kernel<<<blocks, 256, 0, stream>>>(seed, offset, n, (double *)out); note_launch(); }
+    if (dtype == ISSM_F32) { normals_f32_kernel<<<blocks, 256, 0, stream>>>(seed, base, offset, n, (float *)out); note_launch(); }
+    else { normals_f64_kernel<<<blocks, 256, 0, stream>>>(seed, base, offset, n, (double *)out); note_launch(); }
     return (int)cudaGetLastError();
 }
 
-int fill_uniforms(uint64_t seed, uint64_t offset, int64_t n, void *out, int dtype, cudaStream_t stream) {
+int fill_uniforms(uint64_t seed, const uint64_t *base, uint64_t offset, int64_t n, void *out, int dtype,
+                  cudaStream_t stream) {
     if (n <= 0) return 0;
     const int blocks = grid_for(n / (dtype == ISSM_F32 ? 4 : 2) + 2, 256, 8);
-    if (dtype == ISSM_F32) { uniforms_f32_kernel<<<blocks, 256, 0, stream>>>(seed, offset, n, (float *)out); note_launch(); }
-    else { uniforms_f64_kernel<<<blocks, 256, 0, stream>>>(seed, offset, n, (double *)out); note_launch(); }
+    if (dtype == ISSM_F32) { uniforms_f32_kernel<<<blocks, 256, 0, stream>>>(seed, base, offset, n, (float *)out); note_launch(); }
+    else { uniforms_f64_kernel<<<blocks, 256, 0, stream>>>(seed, base, offset, n, (double *)out); note_launch(); }
+    return (int)cudaGetLastError();
+}
+
+__global__ void counter_advance_kernel(uint64_t *counter, uint64_t inc) { *counter += inc; }
+
+int counter_advance(uint64_t *counter, uint64_t inc, cudaStream_t stream) {
+    { counter_advance_kernel<<<1, 1, 0, stream>>>(counter, inc); note_launch(); }
     return (int)cudaGetLastError();
 }
 

@@ -66,6 +66,9 @@ SIGNATURES = [
     ("issm_failure_reset", C.c_int, [_p, _p]),
     ("issm_fill_normals", C.c_int, [_u64, _u64, _i64, _p, _i32, _p]),
     ("issm_fill_uniforms", C.c_int, [_u64, _u64, _i64, _p, _i32, _p]),
+    ("issm_fill_normals_at", C.c_int, [_u64, _p, _u64, _i64, _p, _i32, _p]),
+    ("issm_fill_uniforms_at", C.c_int, [_u64, _p, _u64, _i64, _p, _i32, _p]),
+    ("issm_counter_advance", C.c_int, [_p, _u64, _p]),
     ("issm_static_assign", C.c_int, [_p, _i32, _p, _i64, _i32, _p, _i32, _p]),
     ("issm_draw", C.c_int, [_bank, _p, _i32, _p, _p, _i32, _p, _i32, _i64, _p, _p, _i64, _p]),
     ("issm_mixture_logdensity", C.c_int, [_bank, _den, _p, _i64, _p, _i32, _p, _p, _p, _i64, _i32, _p]),
@@ -170,7 +173,22 @@ def call(name, *args):
     return st
 
 
+_replayed = [0]
+
+
+def note_replay(launches):
+    """Count the kernels of a replayed CUDA graph (their host launch calls ran
+    once, at capture)."""
+    _replayed[0] += int(launches)
+
+
+def launches():
+    """Kernels launched by this process: direct launches plus graph replays."""
+    return int(lib().issm_kernel_launches()) + _replayed[0]
+
+
 _workspaces = {}
+_retired = []  # outgrown workspaces stay allocated: a recorded CUDA graph may still address them
 
 
 def workspace(nbytes, device=None, tag="default", zero=False):
@@ -180,6 +198,8 @@ def workspace(nbytes, device=None, tag="default", zero=False):
     key = (str(device), tag)
     buf = _workspaces.get(key)
     if buf is None or buf.numel() < nbytes:
+        if buf is not None:
+            _retired.append(buf)
         alloc = torch.zeros if zero else torch.empty
         buf = alloc(max(int(nbytes), 256), dtype=torch.uint8, device=device)
         _workspaces[key] = buf

@@ -42,6 +42,26 @@ def fill_uniforms(n, dtype, device, seed, offset=0, out=None):
     return out
 
 
+def fill_normals_at(n, dtype, device, seed, counter, offset=0, out=None):
+    """Normals at Philox offset counter[0] + offset, with the counter read on
+    the device when the kernel runs (graph replays see the advanced value)."""
+    out = torch.empty(int(n), dtype=dtype, device=device) if out is None else out
+    native.call("issm_fill_normals_at", int(seed) & (2 ** 64 - 1), native.ptr(counter), int(offset), int(n),
+                native.ptr(out), native.dtype_code(dtype), _s())
+    return out
+
+
+def fill_uniforms_at(n, dtype, device, seed, counter, offset=0, out=None):
+    out = torch.empty(int(n), dtype=dtype, device=device) if out is None else out
+    native.call("issm_fill_uniforms_at", int(seed) & (2 ** 64 - 1), native.ptr(counter), int(offset), int(n),
+                native.ptr(out), native.dtype_code(dtype), _s())
+    return out
+
+
+def counter_advance(counter, increment):
+    native.call("issm_counter_advance", native.ptr(counter), int(increment), _s())
+
+
 def static_assign(cdf, uniforms, stratified=True, out=None):
     n = uniforms.numel()
     out = torch.empty(n, dtype=torch.int32, device=uniforms.device) if out is None else out

@@ -126,7 +126,7 @@ class _Span:
 
 
 class PreparedSampler:
-    def __init__(self, seed, target, algorithm, device, precision):
+    def __init__(self, seed, target, algorithm, device, precision, graphs=True):
         self.profile = None  # list of (name, start, end, algorithmic bytes) when profiling
         self.seed = int(seed) & (2 ** 64 - 1)
         self.offset = 0
@@ -136,25 +136,40 @@ class PreparedSampler:
         self.precision = precision
         self.busy = False
         self.calls = 0
+        self.counter = None  # device uint64 Philox base (moment methods)
+        self.graphs = graphs
+        self.graph = None
 
-    # counter-based stream: disjoint (seed, offset) ranges per draw
+    # counter-based stream: disjoint (seed, offset) ranges per draw. With a
+    # device counter the offsets are relative to counter[0], which the run
+    # advances on the device at its end (so a replayed graph draws new numbers).
     def normals(self, n, dtype):
-        out = ops.fill_normals(n, dtype, self.device, self.seed, self.offset)
+        if self.counter is not None:
+            out = ops.fill_normals_at(n, dtype, self.device, self.seed, self.counter, self.offset)
+        else:
+            out = ops.fill_normals(n, dtype, self.device, self.seed, self.offset)
         self.offset += int(n) + 8
         return out
 
     def uniforms(self, n, dtype):
-        out = ops.fill_uniforms(n, dtype, self.device, self.seed, self.offset)
+        if self.counter is not None:
+            out = ops.fill_uniforms_at(n, dtype, self.device, self.seed, self.counter, self.offset)
+        else:
+            out = ops.fill_uniforms(n, dtype, self.device, self.seed, self.offset)
         self.offset += int(n) + 8
         return out
 
 
-def prepare_sampler(seed, target, algorithm, device="cuda", precision=native.PREC_NATIVE):
+def prepare_sampler(seed, target, algorithm, device="cuda", precision=native.PREC_NATIVE, graphs=True):
     """prepare_sampler(rng, logtarget, alg) with the device applied: packs the
-    proposal(s) and allocates every buffer on the device."""
+    proposal(s) and allocates every buffer on the device.
+
+    graphs=True lets an AMIS sampler with a native target record its whole
+    run as one CUDA graph on the second call and replay it afterwards (the
+    first call runs eagerly and sizes every workspace)."""
     native.require()
     device = torch.device(device)
-    s = PreparedSampler(seed, target, algorithm, device, precision)
+    s = PreparedSampler(seed, target, algorithm, device, precision, graphs)
     if isinstance(algorithm, ImportanceSampling):
         _prepare_static(s)
     elif isinstance(algorithm, (AMIS, NPMC)):
@@ -183,8 +198,8 @@ def importance_sample_(sampler):
         sampler.calls += 1
 
 
-def importance_sample(seed, target, algorithm, device="cuda", precision=native.PREC_NATIVE):
-    return importance_sample_(prepare_sampler(seed, target, algorithm, device, precision))
+def importance_sample(seed, target, algorithm, device="cuda", precision=native.PREC_NATIVE, graphs=True):
+    return importance_sample_(prepare_sampler(seed, target, algorithm, device, precision, graphs))
 
 
 # ---- static MIS ------------------------------------------------------------------
@@ -271,6 +286,7 @@ def _prepare_moment(s):
     s.cand_factor = torch.zeros(d, d, dtype=dt, device=dev)
     s.cand_lognorm = torch.zeros(1, dtype=dt, device=dev)
     s.committed = (s.history.locations[0].clone(), s.history.scales[0].clone(), s.history.lognormalizers[0].clone())
+    s.counter = torch.zeros(1, dtype=torch.int64, device=dev)
     dofs = None if p.family != STUDENT_T else [float(p.dof)]
     s.rn_stride, s.ru_stride = _radial_strides(dofs)
     s.bound_target = s.target.bind(s.device, dt)
@@ -279,10 +295,41 @@ def _prepare_moment(s):
     s.round_ids = s.round_ids_init.clone()
 
 
+def _graph_eligible(s):
+    """Whole-run graph capture needs a run with no host decisions: AMIS (NPMC
+    clips through a selection), a native target, no per-span profiling and
+    the sampler's own random stream."""
+    from .targets import _Bound, _BoundBank
+
+    return (s.graphs and isinstance(s.algorithm, AMIS) and s.profile is None
+            and isinstance(s.bound_target, (_Bound, _BoundBank))
+            and "normals" not in s.__dict__ and "uniforms" not in s.__dict__)
+
+
 def _run_moment(s):
     is_npmc = isinstance(s.algorithm, NPMC)
+    if _graph_eligible(s) and s.calls >= 1:
+        if s.graph is None:
+            g = torch.cuda.CUDAGraph()
+            torch.cuda.synchronize(s.device)
+            l0 = native.lib().issm_kernel_launches()
+            with torch.cuda.graph(g):
+                _moment_body(s, is_npmc)
+            s.graph_launches = int(native.lib().issm_kernel_launches() - l0)
+            native.note_replay(-s.graph_launches)  # captured, not run
+            s.graph = g
+        s.graph.replay()
+        native.note_replay(s.graph_launches)
+    else:
+        _moment_body(s, is_npmc)
+    return _finish_moment(s, is_npmc)
+
+
+def _moment_body(s, is_npmc):
+    """Every launch of one AMIS/NPMC run, stream-ordered, no host reads."""
     h = s.history
     d, dt = h.d, h.dtype
+    s.offset = 0
     loc0, fac0, ln0 = s.committed
     h.locations[0].copy_(loc0)
     h.scales[0].copy_(fac0)
@@ -341,6 +388,10 @@ def _run_moment(s):
                 inv = h.inverse_factors[t + 1]
             ops.fit_factor(s.mean, s.cov, h.scales[t], out_loc, out_fac, out_ln, dof=h.dof,
                            logconstant=h.logconstant, failures=fail, failure_index=n_tot + 1, out_inverse=inv)
+    ops.counter_advance(s.counter, s.offset)
+
+
+def _finish_moment(s, is_npmc):
     words = s.round_failures.cpu().numpy()
     summaries = s.summaries.cpu().numpy()
     if s.precision != native.PREC_NATIVE:
@@ -357,7 +408,8 @@ def _run_moment(s):
         n_t = int(s.schedule[t]) if is_npmc else int(s.offsets[t + 1])
         ess[t] = 0.0 if sm == 0 else sm * sm / s2
         logz[t] = -np.inf if sm == 0 else m + np.log(sm) - np.log(n_t)
-    s.committed = (s.cand_loc.clone(), s.cand_factor.clone(), s.cand_lognorm[0].clone())
+    for dst, src in zip(s.committed, (s.cand_loc, s.cand_factor, s.cand_lognorm[0])):
+        dst.copy_(src)
     diagnostics = {"method": "npmc" if is_npmc else "amis", "rounds": s.rounds, "round_sizes": list(s.schedule),
                    "round_ess": ess, "round_lognormalizers": logz, "target_evaluations": total,
                    "proposal_evaluations": total if is_npmc else s.rounds * total, "failures": 0}

@@ -135,6 +135,18 @@ int issm_fill_normals(uint64_t seed, uint64_t offset, int64_t n, void *out,
                       int32_t dtype, issm_stream_t stream);
 int issm_fill_uniforms(uint64_t seed, uint64_t offset, int64_t n, void *out,
                        int32_t dtype, issm_stream_t stream);
+/* Same streams at offset (*offset_base + offset) with the base read on the
+ * device, so a captured CUDA graph draws fresh numbers on every replay once
+ * issm_counter_advance moves the base. */
+int issm_fill_normals_at(uint64_t seed, const uint64_t *offset_base,
+                         uint64_t offset, int64_t n, void *out, int32_t dtype,
+                         issm_stream_t stream);
+int issm_fill_uniforms_at(uint64_t seed, const uint64_t *offset_base,
+                          uint64_t offset, int64_t n, void *out, int32_t dtype,
+                          issm_stream_t stream);
+/* *counter += increment, stream-ordered (one-thread kernel). */
+int issm_counter_advance(uint64_t *counter, uint64_t increment,
+                         issm_stream_t stream);
 
 /* ---- assignment and draw ---------------------------------------------- */
 /* Static-MIS assignment: u' = (i + u_i)/N (stratified) or u_i (random), then

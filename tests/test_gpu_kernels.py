@@ -466,6 +466,21 @@ def test_philox_normals_match_oracle(issm, orc, cuda):
     assert abs(float(f.mean())) < 5e-3 and abs(float(f.std()) - 1.0) < 5e-3
 
 
+def test_device_counter_offsets(issm, orc, cuda):
+    """fill_*_at reads its Philox base from device memory; counter_advance
+    moves it on the stream."""
+    ctr = torch.tensor([70], dtype=torch.int64, device=cuda)
+    out = issm.ops.fill_normals_at(4097, torch.float64, cuda, 123, ctr, offset=7).cpu().numpy()
+    assert np.allclose(out, orc.philox_normals(123, 77, 4097), rtol=1e-13, atol=1e-13)
+    issm.ops.counter_advance(ctr, 1000)
+    assert int(ctr.item()) == 1070
+    u = issm.ops.fill_uniforms_at(333, torch.float64, cuda, 5, ctr, offset=3).cpu().numpy()
+    assert np.array_equal(u, orc.philox_uniforms(5, 1073, 333))
+    f = issm.ops.fill_normals_at(1001, torch.float32, cuda, 9, ctr, offset=0)
+    g = issm.ops.fill_normals(1001, torch.float32, cuda, seed=9, offset=1070)
+    assert torch.equal(f, g)
+
+
 @pytest.mark.parametrize("stratified", [True, False])
 def test_static_assign_vs_oracle(issm, orc, cuda, stratified):
     rng = np.random.default_rng(2)
