@@ -70,6 +70,7 @@ const char *issm_status_string(int status) {
     case ISSM_E_UNSUPPORTED: return "request not supported by this build";
     case ISSM_E_WORKSPACE: return "workspace too small";
     case ISSM_E_NOT_POSDEF: return "covariance is not positive definite";
+    case ISSM_E_SCRATCH_LIMIT: return "input larger than the fixed scratch of a no-allocation entry point allows";
     }
     if (status > 0) return cudaGetErrorString((cudaError_t)status);
     return "unknown status";

@@ -83,6 +83,8 @@ SIGNATURES = [
     ("issm_logweight_summary", C.c_int, [_p, _i64, _i32, _p, _p, _sz, _p]),
     ("issm_normalize", C.c_int, [_p, _i64, _i32, _p, _p, _p]),
     ("issm_resampling_cdf", C.c_int, [_p, _i64, _i32, _p, _p, _sz, _p]),
+    ("issm_resampling_cdf_static_max", _i64, []),
+    ("issm_resampling_cdf_static", C.c_int, [_p, _i64, _i32, _p, _p]),
     ("issm_resample_select", C.c_int, [_p, _p, _i64, _p, _i64, _i32, _p, _p]),
     ("issm_resample_workspace_bytes", _sz, [_i64]),
     ("issm_resample_multinomial", C.c_int, [_p, _i64, _i32, _p, _i64, _p, _p, _sz, _p]),

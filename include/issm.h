@@ -48,6 +48,7 @@ typedef struct CUstream_st *issm_stream_t;
 #define ISSM_E_UNSUPPORTED    (-6)   /* valid request this build does not run */
 #define ISSM_E_WORKSPACE      (-7)   /* workspace too small                   */
 #define ISSM_E_NOT_POSDEF     (-8)   /* Cholesky met a non-positive pivot     */
+#define ISSM_E_SCRATCH_LIMIT  (-9)   /* input larger than a fixed scratch allows */
 
 /* ---- enums ------------------------------------------------------------- */
 #define ISSM_F32 0
@@ -289,6 +290,20 @@ int issm_normalize(const void *logweights, int64_t n, int32_t dtype,
 int issm_resampling_cdf(const void *logweights, int64_t n, int32_t dtype,
                         void *cdf, void *workspace, size_t workspace_bytes,
                         issm_stream_t stream);
+/* No-allocation variant of issm_resampling_cdf, with no counterpart in the
+ * reference. For callers that cannot allocate device memory around the call
+ * (a binding holding only the log-weight and CDF pointers, a host with a
+ * fixed device-memory budget): the workspace is one fixed 264 KiB __device__
+ * array inside the library, so the call allocates nothing. At most
+ * issm_resampling_cdf_static_max() = 2^27 log weights; larger n returns
+ * ISSM_E_SCRATCH_LIMIT. The first call on each device looks up the array's
+ * address (cudaGetSymbolAddress), which may load the module: make it before
+ * any stream capture. The array is shared by all calls on a device, so calls
+ * that overlap in time there (other streams or threads) race and corrupt each
+ * other's results: serialise them. Same results as issm_resampling_cdf. */
+int64_t issm_resampling_cdf_static_max(void);
+int issm_resampling_cdf_static(const void *logweights, int64_t n, int32_t dtype,
+                               void *cdf, issm_stream_t stream);
 /* Ancestors (1-based, as the reference) for given uniforms: first j with
  * u < cdf[j] (strict), then the -Inf plateau repair. Replaces
  * _select_resampling_ancestors_kernel! (src/resampling.jl:92-118). */
