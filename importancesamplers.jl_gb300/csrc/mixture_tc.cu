@@ -5,44 +5,43 @@
 //
 // For every component k the reference solves L_k z = x - mu_k by forward
 // substitution (_packed_gaussian_logdensity!, src/native_execution.jl:346-384).
-// Here W_k = L_k^-1 is formed in FP64 once per slot (invert_factors_kernel;
-// cached by the caller in issm_bank.inverse_factors) and the samples are
-// centred on one shift c (the generating / appended slot's mean):
-//   z_k = W_k (x - c) - b_k,   b_k = W_k (mu_k - c)   (b_k formed per CTA),
+// Here W_k = L_k^-1 (FP32, cached per slot in issm_bank.inverse_factors) and
+// the samples are centred on one shift c (the generating / appended slot's
+// mean):
+//   z_k = W_k (x - c) - b_k,   b_k = W_k (mu_k - c),
 // so each 128-sample tile is one GEMM  D[128 x K*DP] = X'[128 x DP] W^T.
 // Precision forms (FP32 accumulation in TMEM in both):
 //   TF32    one kind::tf32 MMA per K slice, operands rounded to tf32 (RNE);
 //   BF16x3  operands split v = hi + lo in bf16, D = Xh Wh + Xl Wh + Xh Wl,
 //           about 16 significant bits per product.
-// One CTA = 4 warps; warp w owns TMEM lanes 32w..32w+31, i.e. samples
-// 32w..32w+31 of the tile, for every component, so the per-sample log-sum-exp
-// state stays in registers across component chunks.
+//
+// Two kernels per launch:
+//   tc_prepare_kernel  one CTA per slot: W_k in MMA operand form (bf16 hi/lo
+//                      or tf32, row-contiguous canonical layout) and b_k;
+//   mixture_tc_kernel  persistent, 8 warps, one 128-sample tile at a time:
+//     * sample tiles stream in with cp.async (16-byte, L1 bypass) into a ring
+//       of padded shared-memory stages, prefetched raw_stages tiles ahead;
+//     * all threads centre, round and split the tile into the A operand
+//       (double-buffered, so converting tile t+1 overlaps MMAs of tile t);
+//     * component operands arrive by bulk copies on an mbarrier, double-
+//       buffered by chunk when a tile needs several chunks of components;
+//     * one thread issues the MMAs of item j (tile, component chunk) into one
+//       of two TMEM accumulators while all warps run the epilogue of item
+//       j-1 from the other: warp w reads TMEM lanes 32 (w mod 4).. and takes
+//       the components of parity w / 4; the two halves merge their
+//       log-sum-exp states through shared memory when the tile completes.
+// Every wait is bounded; a timeout sets the sticky error word and the CTA
+// unwinds after draining its outstanding copies and MMAs.
 #include "issm_device.cuh"
 #include "issm_internal.h"
 #include "tcgen05.cuh"
+#include "trinv.cuh"
 
 namespace issm {
 
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;
 constexpr int kTcTile = 128;
-
-struct TcParams {
-    int d, k, family, mode;       // mode: 0 denominator, 1 append
-    int first_slot, last_slot, chunk, ntile_total;
-    int den_kind;
-    int64_t n;
-    const float *x;
-    const float *w;               // K x DP x DP, row j holds W_k[j, :]
-    const float *loc;             // d x K bank locations
-    const float *lognorm, *coef, *dofs;
-    const int32_t *slots, *group;
-    int fixed_slot;
-    const float *center;          // DP
-    float *out_logden, *out_generating, *lognum;
-    uint64_t *failures;
-    int64_t index_base;
-    int *error;
-};
+constexpr size_t kTcMaxSmem = 232448 - 1024;  // dynamic shared memory per CTA, static part reserved
 
 __device__ __forceinline__ uint32_t tf32_bits(float f) {
     uint32_t u = __float_as_uint(f);
@@ -51,256 +50,448 @@ __device__ __forceinline__ uint32_t tf32_bits(float f) {
     return u & ~0x1FFFu;
 }
 
-// write one 16-byte core-matrix row chunk of operand values (elements e..e+per)
-template <int KIND>
-__device__ __forceinline__ void put_chunk(unsigned char *tile, int row, int kgrp, int KG, const float *v,
-                                          bool lo_part) {
-    const uint32_t off = (uint32_t)((((row >> 3) * KG + kgrp) << 7) + ((row & 7) << 4));
-    if (KIND == tc::kTF32) {
-        uint4 q;
-        q.x = tf32_bits(v[0]);
-        q.y = tf32_bits(v[1]);
-        q.z = tf32_bits(v[2]);
-        q.w = tf32_bits(v[3]);
-        *reinterpret_cast<uint4 *>(tile + off) = q;
-    } else {
-        uint32_t h[4];
+// 16 bytes of operand values: 4 tf32, or 8 bf16 (the hi part, or the lo part
+// bf16(v - hi)).
+template <int KIND> __device__ __forceinline__ uint4 pack16(const float *v, bool lo_part) {
+    if (KIND == tc::kTF32) return make_uint4(tf32_bits(v[0]), tf32_bits(v[1]), tf32_bits(v[2]), tf32_bits(v[3]));
+    uint32_t h[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            float a = v[2 * i], c = v[2 * i + 1];
-            uint16_t ha = tc::bf16_bits(a), hc = tc::bf16_bits(c);
-            if (lo_part) {
-                ha = tc::bf16_bits(a - __uint_as_float((uint32_t)ha << 16));
-                hc = tc::bf16_bits(c - __uint_as_float((uint32_t)hc << 16));
-            }
-            h[i] = (uint32_t)ha | ((uint32_t)hc << 16);
+    for (int i = 0; i < 4; ++i) {
+        const float a = v[2 * i], c = v[2 * i + 1];
+        uint16_t ha = tc::bf16_bits(a), hc = tc::bf16_bits(c);
+        if (lo_part) {
+            ha = tc::bf16_bits(a - __uint_as_float((uint32_t)ha << 16));
+            hc = tc::bf16_bits(c - __uint_as_float((uint32_t)hc << 16));
         }
-        *reinterpret_cast<uint4 *>(tile + off) = make_uint4(h[0], h[1], h[2], h[3]);
+        h[i] = (uint32_t)ha | ((uint32_t)hc << 16);
+    }
+    return make_uint4(h[0], h[1], h[2], h[3]);
+}
+
+// Operand form of slot k, NPART parts of DP x DP elements each: part p, K
+// group q, row j at byte  p * DP*DP*EB + q * DP*16 + j * 16.
+template <int KIND, int SPLIT, int DP>
+__global__ void __launch_bounds__(256) tc_prepare_kernel(const float *__restrict__ w, const float *__restrict__ loc,
+                                                         int d, int first, int cslot, unsigned char *__restrict__ ops,
+                                                         float *__restrict__ bvec, float *__restrict__ center) {
+    constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
+    constexpr int PER = 16 / EB;
+    constexpr int KG = DP / PER;
+    constexpr int NPART = SPLIT == 3 ? 2 : 1;
+    constexpr int LD = DP + 1;
+    __shared__ float ws[DP * LD];
+    __shared__ float dc[DP];
+    const int k = first + blockIdx.x;
+    const float *wk = w + (size_t)k * DP * DP;
+    for (int e = threadIdx.x; e < DP * DP; e += blockDim.x) ws[(e / DP) * LD + e % DP] = wk[e];
+    for (int c = threadIdx.x; c < DP; c += blockDim.x) {
+        const float cc = c < d ? loc[(size_t)cslot * d + c] : 0.f;
+        dc[c] = c < d ? loc[(size_t)k * d + c] - cc : 0.f;
+        if (blockIdx.x == 0) center[c] = cc;
+    }
+    __syncthreads();
+    unsigned char *okp = ops + (size_t)k * NPART * DP * DP * EB;
+    for (int e = threadIdx.x; e < NPART * KG * DP; e += blockDim.x) {
+        const int part = e / (KG * DP), rem = e - part * KG * DP, q = rem / DP, j = rem - q * DP;
+        float v[PER];
+#pragma unroll
+        for (int m = 0; m < PER; ++m) v[m] = ws[j * LD + q * PER + m];
+        *reinterpret_cast<uint4 *>(okp + (size_t)part * DP * DP * EB + (size_t)q * DP * 16 + (size_t)j * 16) =
+            pack16<KIND>(v, part == 1);
+    }
+    // b_k = W_k (mu_k - c) in FP32
+    for (int j = threadIdx.x; j < DP; j += blockDim.x) {
+        float acc = 0.f;
+        for (int c = 0; c < d; ++c) acc = fmaf(ws[j * LD + c], dc[c], acc);
+        bvec[(size_t)k * DP + j] = acc;
     }
 }
 
+struct TcParams {
+    int d, mode, family, den_kind, fixed_slot;
+    int first_slot, last_slot, chunk, nchunks, ntiles, raw_stages;
+    int64_t n;
+    const float *x;
+    const unsigned char *ops;
+    const float *bvec, *center;
+    const float *lognorm, *coef, *dofs;
+    const int32_t *group;
+    float *out_logden, *out_generating, *lognum;
+    uint64_t *failures;
+    int64_t index_base;
+    int *error;
+};
+
 template <int KIND, int SPLIT, int DP>
-__global__ void __launch_bounds__(kTcThreads) mixture_tc_kernel(TcParams p) {
+__global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
-    constexpr int PER = 16 / EB;          // elements per core-matrix row
-    constexpr int KG = DP / PER;          // K groups of the DP-long rows
-    constexpr int A_BYTES = kTcTile * DP * EB;
-    constexpr int B_BYTES = DP * DP * EB;  // one component
+    constexpr int PER = 16 / EB;              // elements per 16-byte K group
+    constexpr int KG = DP / PER;              // K groups of one row
+    constexpr int QH = KG / 2;                // K groups converted per thread
     constexpr int NPART = SPLIT == 3 ? 2 : 1;
+    constexpr int RS = DP + 4;                // padded raw row (floats): conflict-free row reads
+    constexpr int RAW_BYTES = kTcTile * RS * 4;
+    constexpr int A_PART = kTcTile * DP * EB;
+    constexpr int B_COMP = DP * DP * EB;
+    constexpr int KSTEPS = DP * EB / 32;      // MMA K slices of 32 bytes
+    constexpr uint32_t LBO_A = kTcTile * 16;
+    const int chunk = p.chunk, nchunks = p.nchunks, S = p.raw_stages;
+    const int nbufB = nchunks > 1 ? 2 : 1;
+    const uint32_t LBO_B = (uint32_t)(chunk * DP * 16);
+
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *sa = smem;                                  // NPART x A
-    unsigned char *sb = smem + NPART * A_BYTES;                // NPART x chunk x B
-    float *sbv = reinterpret_cast<float *>(sb + (size_t)NPART * p.chunk * B_BYTES);  // chunk x DP
-    __shared__ __align__(8) uint64_t bar;
+    unsigned char *s_raw = smem;
+    unsigned char *s_a = s_raw + (size_t)S * RAW_BYTES;
+    unsigned char *s_b = s_a + (size_t)2 * NPART * A_PART;
+    float *s_bv = reinterpret_cast<float *>(s_b + (size_t)nbufB * NPART * chunk * B_COMP);
+    float *s_x = s_bv + 3 * chunk * DP;
+    float *s_c = s_x + 4 * kTcTile;
+    __shared__ __align__(8) uint64_t bar_mma[2];
+    __shared__ __align__(8) uint64_t bar_b[2];
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
+
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const uint32_t ncols_raw = (uint32_t)(p.chunk * DP);
-    const uint32_t ncols = ncols_raw <= 32 ? 32 : ncols_raw <= 64 ? 64 : ncols_raw <= 128 ? 128 : ncols_raw <= 256 ? 256 : 512;
+    const int NW = chunk * DP;  // TMEM columns of one accumulator
+    const uint32_t ncols = 2 * NW <= 32 ? 32 : 2 * NW <= 64 ? 64 : 2 * NW <= 128 ? 128 : 2 * NW <= 256 ? 256 : 512;
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     if (tid == 0) {
-        tc::mbar_init(&bar, 1);
+        tc::mbar_init(&bar_mma[0], 1);
+        tc::mbar_init(&bar_mma[1], 1);
+        tc::mbar_init(&bar_b[0], 1);
+        tc::mbar_init(&bar_b[1], 1);
         tc::fence_mbar_init();
         abort_flag = 0;
     }
+    for (int c = tid; c < DP; c += kTcThreads) s_c[c] = p.center[c];
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = tmem_base;
-    const uint32_t lane_base = tbase + ((uint32_t)(32 * warp) << 16);
-    uint32_t phase = 0;
-    const int nslots = p.last_slot - p.first_slot + 1;
-    const int nchunks = (nslots + p.chunk - 1) / p.chunk;
-    int staged_chunk = -1;
-    const uint32_t idesc = tc::instr_desc(KIND, kTcTile, DP);
-    // rows are loaded with 16-byte vectors when the layout allows it
+
+    const int my_tiles = (p.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int J = my_tiles * nchunks;
     const bool vec = (p.d % 4 == 0) && ((reinterpret_cast<uintptr_t>(p.x) & 15) == 0);
-    float xs[DP], xn[DP];
-    auto load_row = [&](int tile, float (&dst)[DP]) {
-        const int64_t r = (int64_t)tile * kTcTile + tid;
-#pragma unroll
-        for (int c = 0; c < DP; ++c) dst[c] = 0.f;
-        if (tile < p.ntile_total && r < p.n) {
-            const float *xi = p.x + r * p.d;
+    const int ggen = (p.den_kind == ISSM_DENOM_PARTIAL) ? p.group[p.fixed_slot] : 0;
+
+    auto tile_of = [&](int it) -> int64_t { return (int64_t)blockIdx.x + (int64_t)it * gridDim.x; };
+    auto chunk_range = [&](int ch, int &k0, int &cnt) {
+        k0 = p.first_slot + ch * chunk;
+        cnt = min(chunk, p.last_slot - k0 + 1);
+    };
+
+    // ---- raw sample tiles: cp.async into stage it % S, one commit group per tile
+    auto issue_raw = [&](int it) {
+        if (it < my_tiles) {
+            const int64_t row0 = tile_of(it) * kTcTile;
+            const int rows = (int)min((int64_t)kTcTile, p.n - row0);
+            float *dst = reinterpret_cast<float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
+            const float *src = p.x + row0 * p.d;
             if (vec) {
-#pragma unroll
-                for (int c = 0; c < DP; c += 4)
-                    if (c < p.d) {
-                        const float4 q = __ldg(reinterpret_cast<const float4 *>(xi + c));
-                        dst[c] = q.x; dst[c + 1] = q.y; dst[c + 2] = q.z; dst[c + 3] = q.w;
-                    }
+                const int q4 = p.d >> 2, total = rows * q4;
+                for (int e = tid; e < total; e += kTcThreads) {
+                    const int r = e / q4, c4 = e - r * q4;
+                    tc::cp_async16(dst + r * RS + c4 * 4, src + (size_t)r * p.d + c4 * 4);
+                }
             } else {
-#pragma unroll
-                for (int c = 0; c < DP; ++c)
-                    if (c < p.d) dst[c] = __ldg(xi + c);
+                const int total = rows * p.d;
+                for (int e = tid; e < total; e += kTcThreads) {
+                    const int r = e / p.d, c = e - r * p.d;
+                    tc::cp_async4(dst + r * RS + c, src + (size_t)r * p.d + c);
+                }
             }
+        }
+        tc::cp_async_commit();
+    };
+    auto wait_raw = [&]() {
+        if (S == 1) tc::cp_async_wait<0>();
+        else if (S == 2) tc::cp_async_wait<1>();
+        else tc::cp_async_wait<2>();
+    };
+
+    // ---- component operands of item j: bulk copies on bar_b (warp 0 only)
+    int b_issued = 0;  // items whose operands were requested (warp 0)
+    auto issue_b = [&](int j) {
+        int k0, cnt;
+        chunk_range(j % nchunks, k0, cnt);
+        const int buf = nbufB == 1 ? 0 : (j & 1);
+        const uint32_t bytes = (uint32_t)(NPART * KG * cnt * DP * 16 + cnt * DP * 4);
+        if (lane == 0) tc::mbar_arrive_expect_tx(&bar_b[buf], bytes);
+        __syncwarp();
+        unsigned char *dstb = s_b + (size_t)buf * NPART * chunk * B_COMP;
+        for (int e = lane; e < NPART * KG * cnt; e += 32) {
+            const int part = e / (KG * cnt), rem = e - part * KG * cnt, q = rem / cnt, kk = rem - q * cnt;
+            const unsigned char *src = p.ops + ((size_t)(k0 + kk) * NPART + part) * B_COMP + (size_t)q * DP * 16;
+            unsigned char *dst = dstb + (size_t)part * chunk * B_COMP + (size_t)q * LBO_B + (size_t)kk * DP * 16;
+            tc::bulk_copy_g2s(dst, src, DP * 16, &bar_b[buf]);
+        }
+        if (lane == 0)
+            tc::bulk_copy_g2s(s_bv + (nchunks == 1 ? 0 : j % 3) * chunk * DP, p.bvec + (size_t)k0 * DP,
+                              (uint32_t)(cnt * DP * 4), &bar_b[buf]);
+        ++b_issued;
+    };
+
+    // ---- centre, round and split tile it into A buffer it & 1
+    float ln_pref0 = 0.f, ln_pref1 = 0.f;
+    auto convert = [&](int it) {
+        const float *raw = reinterpret_cast<const float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
+        unsigned char *a = s_a + (size_t)(it & 1) * NPART * A_PART;
+        const int row = tid & (kTcTile - 1), half = tid >> 7;
+        const int64_t i = tile_of(it) * kTcTile + row;
+        const bool active = i < p.n;
+#pragma unroll
+        for (int qq = 0; qq < QH; ++qq) {
+            const int q = half * QH + qq;
+            float v[PER];
+#pragma unroll
+            for (int m = 0; m < PER; m += 4) {
+                const int c = q * PER + m;
+                float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (active) f = *reinterpret_cast<const float4 *>(raw + row * RS + c);
+                v[m] = (active && c < p.d) ? f.x - s_c[c] : 0.f;
+                v[m + 1] = (active && c + 1 < p.d) ? f.y - s_c[c + 1] : 0.f;
+                v[m + 2] = (active && c + 2 < p.d) ? f.z - s_c[c + 2] : 0.f;
+                v[m + 3] = (active && c + 3 < p.d) ? f.w - s_c[c + 3] : 0.f;
+            }
+            *reinterpret_cast<uint4 *>(a + (size_t)q * LBO_A + row * 16) = pack16<KIND>(v, false);
+            if (NPART == 2)
+                *reinterpret_cast<uint4 *>(a + A_PART + (size_t)q * LBO_A + row * 16) = pack16<KIND>(v, true);
+        }
+        if (p.mode == 1 && half == 0) {
+            const float l = active ? p.lognum[i] : 0.f;
+            if (it & 1) ln_pref1 = l;
+            else ln_pref0 = l;
         }
     };
-    load_row(blockIdx.x, xn);
 
-    for (int tile = blockIdx.x; tile < p.ntile_total; tile += gridDim.x) {
-        const int64_t i = (int64_t)tile * kTcTile + tid;
-        const bool active = i < p.n;
-        // ---- stage A (shifted samples) from the prefetched row ----
+    // ---- MMAs of item j (one thread)
+    int mma_issued = 0, mma_waited = 0;  // thread 0 bookkeeping for the drain
+    auto issue_mma = [&](int j, int abuf) {
+        int k0, cnt;
+        chunk_range(j % nchunks, k0, cnt);
+        const int bbuf = nbufB == 1 ? 0 : (j & 1);
+        const uint32_t d_tmem = tbase + (uint32_t)((j & 1) * NW);
+        const uint32_t idesc = tc::instr_desc(KIND, kTcTile, cnt * DP);
+        const uint32_t a0 = tc::smem_u32(s_a + (size_t)abuf * NPART * A_PART);
+        const uint32_t b0 = tc::smem_u32(s_b + (size_t)bbuf * NPART * chunk * B_COMP);
 #pragma unroll
-        for (int c = 0; c < DP; ++c) xs[c] = (c < p.d && active) ? xn[c] - p.center[c] : 0.f;
-        // the next tile's row is in flight while this tile's MMAs and epilogue run
-        load_row(tile + gridDim.x, xn);
-#pragma unroll
-        for (int q = 0; q < KG; ++q) {
-            put_chunk<KIND>(sa, tid, q, KG, xs + q * PER, false);
-            if (NPART == 2) put_chunk<KIND>(sa + A_BYTES, tid, q, KG, xs + q * PER, true);
-        }
-        const int gen = active ? (p.slots ? p.slots[i] : p.fixed_slot) : 0;
-        const int ggen = (p.den_kind == ISSM_DENOM_PARTIAL && active) ? p.group[gen] : 0;
-        LseState<float> lse;
-        float gen_lq = 0.f, last_lq = 0.f;
-        for (int ch = 0; ch < nchunks; ++ch) {
-            const int k0 = p.first_slot + ch * p.chunk;
-            const int cnt = min(p.chunk, p.last_slot - k0 + 1);
-            if (staged_chunk != ch) {
-                // ---- stage B (inverse factors) and the shift vectors ----
-                for (int e = tid; e < cnt * DP * KG; e += kTcThreads) {
-                    const int kk = e / (DP * KG), rem = e - kk * DP * KG, row = rem / KG, q = rem - row * KG;
-                    const float *src = p.w + ((size_t)(k0 + kk) * DP + row) * DP + q * PER;
-                    float v[PER];
-#pragma unroll
-                    for (int j = 0; j < PER; ++j) v[j] = src[j];
-                    put_chunk<KIND>(sb + (size_t)kk * B_BYTES, row, q, KG, v, false);
-                    if (NPART == 2)
-                        put_chunk<KIND>(sb + (size_t)(p.chunk + kk) * B_BYTES, row, q, KG, v, true);
+        for (int s = 0; s < KSTEPS; ++s) {
+            const uint64_t da = tc::smem_desc(a0 + s * 2 * LBO_A, LBO_A, 128);
+            const uint64_t db = tc::smem_desc(b0 + s * 2 * LBO_B, LBO_B, 128);
+            if (KIND == tc::kTF32) {
+                tc::mma_tf32(d_tmem, da, db, idesc, s > 0);
+            } else {
+                tc::mma(d_tmem, da, db, idesc, s > 0);
+                if (SPLIT == 3) {
+                    const uint64_t dal = tc::smem_desc(a0 + A_PART + s * 2 * LBO_A, LBO_A, 128);
+                    const uint64_t dbl = tc::smem_desc(b0 + chunk * B_COMP + s * 2 * LBO_B, LBO_B, 128);
+                    tc::mma(d_tmem, dal, db, idesc, true);
+                    tc::mma(d_tmem, da, dbl, idesc, true);
                 }
-                // b_k = W_k (mu_k - c), accumulated in FP32 from the cached inverse
-                for (int e = tid; e < cnt * DP; e += kTcThreads) {
-                    const int kk = e / DP, j = e - kk * DP, k = k0 + kk;
-                    const float *wr = p.w + ((size_t)k * DP + j) * DP;
-                    float acc = 0.f;
-                    for (int c = 0; c < p.d; ++c) acc = fmaf(wr[c], p.loc[(size_t)k * p.d + c] - p.center[c], acc);
-                    sbv[e] = acc;
-                }
-                staged_chunk = ch;
             }
+        }
+        tc::commit(&bar_mma[j & 1]);
+        ++mma_issued;
+    };
+
+    // ---- epilogue of item j: radial densities and the log-sum-exp
+    const int qd = warp & 3, h = warp >> 2;
+    const int erow = 32 * qd + lane;
+    LseState<float> lse;
+    float gen_lq = 0.f, last_lq = 0.f;
+    bool has_gen = false;
+    auto epilogue = [&](int j, bool good) {
+        const int it = j / nchunks, ch = j - it * nchunks;
+        int k0, cnt;
+        chunk_range(ch, k0, cnt);
+        if (good) {
+            const uint32_t lane_base = tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)((j & 1) * NW);
+            const float *bv = s_bv + (nchunks == 1 ? 0 : j % 3) * chunk * DP;
+            for (int kk = h; kk < cnt; kk += 2) {
+                const int k = k0 + kk;
+                float r2 = 0.f;
+#pragma unroll
+                for (int c0 = 0; c0 < DP; c0 += 16) {
+                    float v[16];
+                    tc::tmem_ld16(lane_base + (uint32_t)(kk * DP + c0), v);
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        const float z = v[q] - bv[kk * DP + c0 + q];
+                        r2 = fmaf(z, z, r2);
+                    }
+                }
+                float lq;
+                if (p.family == ISSM_GAUSSIAN) {
+                    lq = p.lognorm[k] - 0.5f * r2;
+                } else {
+                    const float nu = p.dofs[k];
+                    lq = p.lognorm[k] - (nu + (float)p.d) * 0.5f * log1pf(r2 / nu);
+                }
+                bool member = true;
+                if (p.den_kind == ISSM_DENOM_GENERATING) member = (k == p.fixed_slot);
+                else if (p.den_kind == ISSM_DENOM_PARTIAL) member = (p.group[k] == ggen);
+                if (k == p.fixed_slot) {
+                    gen_lq = lq;
+                    has_gen = true;
+                }
+                last_lq = lq;
+                if (member) lse.add((p.coef ? p.coef[k] : 0.f) + lq);
+            }
+        }
+        if (ch != nchunks - 1) return;
+        // tile complete: the upper half hands its state to the lower half
+        if (h == 1) {
+            s_x[erow] = lse.m;
+            s_x[kTcTile + erow] = lse.s;
+            s_x[2 * kTcTile + erow] = gen_lq;
+            s_x[3 * kTcTile + erow] = (float)((lse.nan ? 2 : 0) | (has_gen ? 1 : 0));
+        }
+        __syncthreads();
+        if (h == 0 && good) {
+            const float om = s_x[erow], os = s_x[kTcTile + erow];
+            const int of = (int)s_x[3 * kTcTile + erow];
+            if (of & 2) lse.nan = true;
+            if (of & 1) {
+                gen_lq = s_x[2 * kTcTile + erow];
+                has_gen = true;
+            }
+            if (om != -INFINITY) {
+                if (lse.m == -INFINITY) {
+                    lse.m = om;
+                    lse.s = os;
+                } else if (om > lse.m) {
+                    lse.s = lse.s * expf(lse.m - om) + os;
+                    lse.m = om;
+                } else if (om == lse.m) {
+                    lse.s += os;
+                } else {
+                    lse.s += os * expf(om - lse.m);
+                }
+            }
+            const int64_t i = tile_of(it) * kTcTile + erow;
+            if (i < p.n) {
+                if (p.mode == 1) {
+                    const float prev = (it & 1) ? ln_pref1 : ln_pref0;
+                    uint16_t reason = isnan(last_lq) ? ISSM_REASON_PROPOSAL_INVALID : 0;
+                    if (!reason) {
+                        const float v = logaddexp(prev, p.coef[p.first_slot] + last_lq);
+                        if (isnan(v) || v == -INFINITY) reason = ISSM_REASON_PROPOSAL_INVALID;
+                        else p.lognum[i] = v;
+                    }
+                    if (reason) record_failure(p.failures, p.index_base + i + 1, 0, reason);
+                } else {
+                    float den = lse.value();
+                    const bool bad = isnan(gen_lq) || gen_lq == -INFINITY || isnan(den) || den == -INFINITY;
+                    if (bad) {
+                        record_failure(p.failures, p.index_base + i + 1, 0, ISSM_REASON_PROPOSAL_INVALID);
+                        den = -INFINITY;
+                    }
+                    p.out_logden[i] = den;
+                    if (p.out_generating) p.out_generating[i] = bad ? -INFINITY : gen_lq;
+                }
+            }
+        }
+        lse = LseState<float>();
+        gen_lq = 0.f;
+        last_lq = 0.f;
+        has_gen = false;
+    };
+
+    auto fail = [&]() {
+        atomicExch(p.error, 1);
+        abort_flag = 1;
+    };
+
+    // ---- prologue
+    for (int s = 0; s < S; ++s) issue_raw(s);
+    if (warp == 0 && J > 0) {
+        issue_b(0);
+        if (nchunks > 1 && J > 1) issue_b(1);
+    }
+    int b_waited = 0;  // items whose operands this thread has seen land
+    bool good = true;
+
+    for (int j = 0; j < J; ++j) {
+        const int it = j / nchunks, ch = j - it * nchunks;
+        if (ch == 0) {
+            wait_raw();
+            __syncthreads();
+            convert(it);
             tc::fence_proxy_async();
-            tc::fence_before_sync();
             __syncthreads();
-            tc::fence_after_sync();
-            if (abort_flag) break;
-            if (tid == 0) {
-                const uint32_t a0 = tc::smem_u32(sa), b0 = tc::smem_u32(sb);
-                for (int kk = 0; kk < cnt; ++kk) {
-                    const uint32_t dcol = tbase + (uint32_t)(kk * DP);
-                    for (int s = 0; s < DP * EB / 32; ++s) {
-                        const uint64_t da = tc::smem_desc(a0 + s * 256, 128, KG * 128);
-                        const uint64_t db = tc::smem_desc(b0 + kk * B_BYTES + s * 256, 128, KG * 128);
-                        if (KIND == tc::kTF32) {
-                            tc::mma_tf32(dcol, da, db, idesc, s > 0);
-                        } else {
-                            tc::mma(dcol, da, db, idesc, s > 0);
-                            if (SPLIT == 3) {
-                                const uint64_t dal = tc::smem_desc(a0 + A_BYTES + s * 256, 128, KG * 128);
-                                const uint64_t dbl =
-                                    tc::smem_desc(b0 + (p.chunk + kk) * B_BYTES + s * 256, 128, KG * 128);
-                                tc::mma(dcol, dal, db, idesc, true);
-                                tc::mma(dcol, da, dbl, idesc, true);
-                            }
-                        }
-                    }
-                }
-                tc::commit(&bar);
-                // one thread observes completion; the barrier below publishes it
-                if (!tc::mbar_wait(&bar, phase)) {
-                    atomicExch(p.error, 1);
-                    abort_flag = 1;
-                }
-            }
-            phase ^= 1u;
-            tc::fence_before_sync();
-            __syncthreads();
-            tc::fence_after_sync();
-            const bool ok = abort_flag == 0;  // block-uniform
-            if (ok) {
-                // ---- epilogue: radial density and log-sum-exp per component ----
-                for (int kk = 0; kk < cnt; ++kk) {
-                    const int k = k0 + kk;
-                    float r2 = 0.f;
-#pragma unroll
-                    for (int c0 = 0; c0 < DP; c0 += 16) {
-                        float v[16];
-                        tc::tmem_ld16(lane_base + (uint32_t)(kk * DP + c0), v);
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            const float z = v[j] - sbv[kk * DP + c0 + j];
-                            r2 = fmaf(z, z, r2);
-                        }
-                    }
-                    float lq;
-                    if (p.family == ISSM_GAUSSIAN) {
-                        lq = p.lognorm[k] - 0.5f * r2;
-                    } else {
-                        const float nu = p.dofs[k];
-                        lq = p.lognorm[k] - (nu + (float)p.d) * 0.5f * log1pf(r2 / nu);
-                    }
-                    bool member = true;
-                    if (p.den_kind == ISSM_DENOM_GENERATING) member = (k == gen);
-                    else if (p.den_kind == ISSM_DENOM_PARTIAL) member = (p.group[k] == ggen);
-                    if (k == gen) gen_lq = lq;
-                    last_lq = lq;
-                    if (member) lse.add((p.coef ? p.coef[k] : 0.f) + lq);
-                }
-            }
-            tc::fence_before_sync();
-            __syncthreads();
+            issue_raw(it + S);  // into the stage just consumed
         }
+        if (nchunks > 1 || j == 0) {
+            const int buf = nbufB == 1 ? 0 : (j & 1);
+            const uint32_t par = nbufB == 1 ? 0u : (uint32_t)((j >> 1) & 1);
+            if (!tc::mbar_wait(&bar_b[buf], par)) {
+                good = false;
+                fail();
+            }
+            b_waited = j + 1;
+        }
+        if (tid == 0 && good) {
+            tc::fence_after_sync();
+            issue_mma(j, it & 1);
+        }
+        if (j > 0) {
+            if (!tc::mbar_wait(&bar_mma[(j - 1) & 1], (uint32_t)(((j - 1) >> 1) & 1))) {
+                good = false;
+                fail();
+            }
+            mma_waited = j;
+            good = __all_sync(0xffffffffu, good);
+            tc::fence_after_sync();
+            if (warp == 0 && nchunks > 1 && j + 1 < J && good) issue_b(j + 1);
+            epilogue(j - 1, good);
+        }
+        tc::fence_before_sync();
+        __syncthreads();
         if (abort_flag) break;
-        if (!active) continue;
-        if (p.mode == 1) {
-            uint16_t reason = isnan(last_lq) ? ISSM_REASON_PROPOSAL_INVALID : 0;
-            if (!reason) {
-                const float v = logaddexp(p.lognum[i], p.coef[p.first_slot] + last_lq);
-                if (isnan(v) || v == -INFINITY) reason = ISSM_REASON_PROPOSAL_INVALID;
-                else p.lognum[i] = v;
-            }
-            if (reason) record_failure(p.failures, p.index_base + i + 1, 0, reason);
-        } else {
-            float den = lse.value();
-            bool bad = isnan(gen_lq) || gen_lq == -INFINITY || isnan(den) || den == -INFINITY;
-            if (bad) {
-                record_failure(p.failures, p.index_base + i + 1, 0, ISSM_REASON_PROPOSAL_INVALID);
-                den = -INFINITY;
-            }
-            p.out_logden[i] = den;
-            if (p.out_generating) p.out_generating[i] = bad ? -INFINITY : gen_lq;
+    }
+    if (!abort_flag && J > 0) {
+        if (!tc::mbar_wait(&bar_mma[(J - 1) & 1], (uint32_t)(((J - 1) >> 1) & 1))) {
+            good = false;
+            fail();
         }
+        mma_waited = J;
+        good = __all_sync(0xffffffffu, good);
+        tc::fence_after_sync();
+        epilogue(J - 1, good);
+    }
+    // drain: no copy or MMA may still target this CTA's memory at exit
+    tc::cp_async_wait_all();
+    if (tid == 0) {
+        for (int q = b_waited; q < b_issued; ++q)
+            tc::mbar_wait(&bar_b[nbufB == 1 ? 0 : (q & 1)], nbufB == 1 ? 0u : (uint32_t)((q >> 1) & 1));
+        for (int q = mma_waited; q < mma_issued; ++q) tc::mbar_wait(&bar_mma[q & 1], (uint32_t)((q >> 1) & 1));
     }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tbase, ncols);
 }
 
-// W_k = L_k^-1 in FP64: L_k is staged in shared memory, one thread solves
-// one column by forward substitution; written as FP32 DP x DP, zero padded.
+// W_k = L_k^-1 (FP32) for slots first..first+count-1, written DP x DP
+// row-major (row j = W_k[j, :]) with zero padding; one CTA of 256 per slot.
 template <typename T>
-__global__ void invert_factors_kernel(const T *__restrict__ L, int d, int DP, int first, float *__restrict__ w) {
+__global__ void __launch_bounds__(256) invert_factors_kernel(const T *__restrict__ L, int d, int DP, int first,
+                                                             float *__restrict__ w) {
+    constexpr int LD = 65;
+    __shared__ float Ls[64 * LD];
+    __shared__ float Ws[64 * LD];
     const int k = first + blockIdx.x;
-    extern __shared__ double sm_inv[];
-    double *Ls = sm_inv;            // d x d column-major
-    double *Ws = sm_inv + d * d;    // d x d column-major
     const T *Lk = L + (size_t)k * d * d;
-    for (int e = threadIdx.x; e < d * d; e += blockDim.x) Ls[e] = (double)Lk[e];
-    __syncthreads();
-    for (int c = threadIdx.x; c < d; c += blockDim.x) {
-        for (int r = 0; r < c; ++r) Ws[r + c * d] = 0.0;
-        for (int r = c; r < d; ++r) {
-            double v = (r == c) ? 1.0 : 0.0;
-            for (int q = c; q < r; ++q) v -= Ls[r + q * d] * Ws[q + c * d];
-            Ws[r + c * d] = v / Ls[r + r * d];
-        }
+    // column-major source: element (r, c) at r + c d
+    for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+        const int r = e % d, c = e / d;
+        Ls[r * LD + c] = (float)Lk[e];
     }
     __syncthreads();
+    invert_lower_f32(Ls, Ws, d, LD);
     float *wk = w + (size_t)k * DP * DP;
     for (int e = threadIdx.x; e < DP * DP; e += blockDim.x) {
         const int j = e / DP, c = e % DP;
-        wk[e] = (j < d && c < d) ? (float)Ws[j + c * d] : 0.f;
+        wk[e] = (j < d && c < d) ? Ws[j * LD + c] : 0.f;
     }
 }
 
@@ -308,52 +499,68 @@ int invert_factors(const issm_bank *bk, int first, int count, float *out, cudaSt
     const int d = bk->dim;
     if (d > 64) return ISSM_E_UNSUPPORTED;
     const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
-    const size_t smem = 2 * sizeof(double) * d * d;
     if (count <= 0) return 0;
-    cudaError_t e = cudaFuncSetAttribute(bk->dtype == ISSM_F32 ? (const void *)invert_factors_kernel<float>
-                                                               : (const void *)invert_factors_kernel<double>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return (int)e;
     if (bk->dtype == ISSM_F32) {
-        { invert_factors_kernel<float><<<count, 64, smem, stream>>>((const float *)bk->scales, d, DP, first, out);
+        { invert_factors_kernel<float><<<count, 256, 0, stream>>>((const float *)bk->scales, d, DP, first, out);
           note_launch(); }
     } else {
-        { invert_factors_kernel<double><<<count, 64, smem, stream>>>((const double *)bk->scales, d, DP, first, out);
+        { invert_factors_kernel<double><<<count, 256, 0, stream>>>((const double *)bk->scales, d, DP, first, out);
           note_launch(); }
     }
     return (int)cudaGetLastError();
 }
 
+// Workspace: operand forms K x DP*DP*4 bytes | b vectors K x DP | centre
+// (256 bytes) | inverse factors K x DP*DP (only when the bank has none).
+static int dp_of(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : 64; }
+
 size_t tc_workspace_bytes(int k, int d) {
-    const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
-    return sizeof(float) * ((size_t)k * DP * DP + (size_t)k * DP + DP) + 64;
+    const int DP = dp_of(d);
+    return (size_t)2 * k * DP * DP * 4 + (size_t)k * DP * 4 + 256 + 64;
 }
 
 template <int KIND, int SPLIT, int DP>
-static int launch_tc(TcParams p, cudaStream_t stream) {
+static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, unsigned char *ops, float *bvec,
+                     float *center, cudaStream_t stream) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
     constexpr int NPART = SPLIT == 3 ? 2 : 1;
+    constexpr size_t RAW_BYTES = (size_t)kTcTile * (DP + 4) * 4;
+    constexpr size_t A_PART = (size_t)kTcTile * DP * EB;
+    constexpr size_t B_COMP = (size_t)DP * DP * EB;
     const int nslots = p.last_slot - p.first_slot + 1;
-    const int maxcols = 256;  // two CTAs per SM share the 512 TMEM columns
-    int chunk = maxcols / DP;
-    if (chunk > nslots) chunk = nslots;
+    int chunk = min(nslots, 256 / DP);
+    size_t smem = 0;
+    int nch = 1, stages = 1;
+    for (;;) {
+        nch = (nslots + chunk - 1) / chunk;
+        stages = nch == 1 ? 3 : 1;
+        const int nbufB = nch > 1 ? 2 : 1;
+        for (; stages >= 1; --stages) {
+            smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)nbufB * NPART * chunk * B_COMP +
+                   (size_t)3 * chunk * DP * 4 + (size_t)4 * kTcTile * 4 + (size_t)DP * 4;
+            if (smem <= kTcMaxSmem) break;
+        }
+        if (stages >= 1 || chunk == 1) break;
+        --chunk;
+    }
+    if (stages < 1) return ISSM_E_UNSUPPORTED;
     p.chunk = chunk;
-    size_t smem = (size_t)NPART * kTcTile * DP * EB + (size_t)NPART * chunk * DP * DP * EB +
-                  sizeof(float) * chunk * DP;
-    // never more resident CTAs per SM than TMEM holds, so allocations never wait
-    const int ncols = chunk * DP <= 32 ? 32 : chunk * DP <= 64 ? 64 : chunk * DP <= 128 ? 128 : 256;
-    const int tmem_ctas = 512 / ncols;
-    const size_t floor_smem = 233472 / (tmem_ctas + 1) + 1024;
-    if (smem < floor_smem) smem = floor_smem;
+    p.nchunks = nch;
+    p.raw_stages = stages;
+    { tc_prepare_kernel<KIND, SPLIT, DP><<<nslots, 256, 0, stream>>>(w, loc, p.d, p.first_slot, cslot, ops, bvec,
+                                                                       center);
+      note_launch(); }
     auto kern = mixture_tc_kernel<KIND, SPLIT, DP>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int)e;
     int occ = 1;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTcThreads, smem);
     if (e != cudaSuccess) return (int)e;
-    occ = max(1, min(occ, tmem_ctas));
-    p.ntile_total = (int)((p.n + kTcTile - 1) / kTcTile);
-    const int blocks = min(p.ntile_total, kSMs * occ);
+    const int nw2 = 2 * chunk * DP;
+    const int ncols = nw2 <= 32 ? 32 : nw2 <= 64 ? 64 : nw2 <= 128 ? 128 : nw2 <= 256 ? 256 : 512;
+    occ = max(1, min(occ, 512 / ncols));  // TMEM allocations never wait
+    p.ntiles = (int)((p.n + kTcTile - 1) / kTcTile);
+    const int blocks = min(p.ntiles, kSMs * occ);
     if (blocks < 1) return 0;
     { kern<<<blocks, kTcThreads, smem, stream>>>(p); note_launch(); }
     return (int)cudaGetLastError();
@@ -366,36 +573,42 @@ int tc_mixture(const issm_bank *bk, const issm_denominator *den, int mode, int f
                int precision, void *ws, size_t ws_bytes, int *error, cudaStream_t stream) {
     const int d = bk->dim;
     if (bk->dtype != ISSM_F32 || bk->scale_kind != ISSM_SCALE_FACTOR || d > 64) return ISSM_E_UNSUPPORTED;
-    const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
-    if (ws_bytes < tc_workspace_bytes(bk->count, d)) return ISSM_E_WORKSPACE;
-    float *w = (float *)ws;
-    float *center = w + (size_t)bk->count * DP * DP + (size_t)bk->count * DP;
-    // shift: the generating (or appended) slot's mean
-    const int cslot = (mode == 1) ? first : fixed_slot;
-    cudaError_t e = cudaMemsetAsync(center, 0, sizeof(float) * DP, stream);
-    if (e != cudaSuccess) return (int)e;
-    e = cudaMemcpyAsync(center, (const float *)bk->locations + (size_t)cslot * d, sizeof(float) * d,
-                        cudaMemcpyDeviceToDevice, stream);
-    if (e != cudaSuccess) return (int)e;
-    if (bk->inverse_factors) {
-        w = const_cast<float *>(bk->inverse_factors);
-    } else {
-        const int st = invert_factors(bk, first, last - first + 1, w, stream);
+    if (slots != nullptr) return ISSM_E_UNSUPPORTED;  // one centre per launch
+    const int DP = dp_of(d);
+    const int K = bk->count;
+    if (ws_bytes < tc_workspace_bytes(K, d)) return ISSM_E_WORKSPACE;
+    unsigned char *ops = (unsigned char *)ws;
+    float *bvec = (float *)(ops + (size_t)K * DP * DP * 4);
+    float *center = bvec + (size_t)K * DP;
+    float *winv = (float *)((unsigned char *)center + 256);
+    const int den_kind = den ? den->kind : ISSM_DENOM_FULL;
+    // only the generating slot contributes to a generating-only denominator
+    if (mode == 0 && den_kind == ISSM_DENOM_GENERATING) first = last = fixed_slot;
+    const float *w = bk->inverse_factors;
+    if (!w) {
+        const int st = invert_factors(bk, first, last - first + 1, winv, stream);
         if (st) return st;
+        w = winv;
     }
+    const int cslot = (mode == 1) ? first : fixed_slot;
     TcParams p{};
-    p.d = d; p.k = bk->count; p.family = bk->family; p.mode = mode;
+    p.d = d; p.mode = mode; p.family = bk->family; p.den_kind = den_kind; p.fixed_slot = fixed_slot;
     p.first_slot = first; p.last_slot = last;
-    p.den_kind = den ? den->kind : ISSM_DENOM_FULL;
-    p.n = n; p.x = (const float *)x; p.w = w; p.loc = (const float *)bk->locations;
+    p.n = n; p.x = (const float *)x; p.ops = ops; p.bvec = bvec; p.center = center;
     p.lognorm = (const float *)bk->lognormalizers; p.coef = (const float *)coef; p.dofs = (const float *)bk->dofs;
-    p.slots = slots; p.group = den ? den->group_of_slot : nullptr; p.fixed_slot = fixed_slot;
-    p.center = center; p.out_logden = (float *)out_logden; p.out_generating = (float *)out_generating;
+    p.group = den ? den->group_of_slot : nullptr;
+    p.out_logden = (float *)out_logden; p.out_generating = (float *)out_generating;
     p.lognum = (float *)lognum; p.failures = failures; p.index_base = index_base; p.error = error;
+    const float *loc = (const float *)bk->locations;
     const bool tf32 = precision == ISSM_PREC_TF32;
-    if (DP == 16) return tf32 ? launch_tc<tc::kTF32, 1, 16>(p, stream) : launch_tc<tc::kBF16, 3, 16>(p, stream);
-    if (DP == 32) return tf32 ? launch_tc<tc::kTF32, 1, 32>(p, stream) : launch_tc<tc::kBF16, 3, 32>(p, stream);
-    return tf32 ? launch_tc<tc::kTF32, 1, 64>(p, stream) : launch_tc<tc::kBF16, 3, 64>(p, stream);
+    if (DP == 16)
+        return tf32 ? launch_tc<tc::kTF32, 1, 16>(p, w, loc, cslot, ops, bvec, center, stream)
+                    : launch_tc<tc::kBF16, 3, 16>(p, w, loc, cslot, ops, bvec, center, stream);
+    if (DP == 32)
+        return tf32 ? launch_tc<tc::kTF32, 1, 32>(p, w, loc, cslot, ops, bvec, center, stream)
+                    : launch_tc<tc::kBF16, 3, 32>(p, w, loc, cslot, ops, bvec, center, stream);
+    return tf32 ? launch_tc<tc::kTF32, 1, 64>(p, w, loc, cslot, ops, bvec, center, stream)
+                : launch_tc<tc::kBF16, 3, 64>(p, w, loc, cslot, ops, bvec, center, stream);
 }
 
 }  // namespace issm

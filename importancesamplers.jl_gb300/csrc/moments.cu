@@ -11,6 +11,7 @@
 // in shared memory (d <= 64).
 #include "issm_device.cuh"
 #include "issm_internal.h"
+#include "trinv.cuh"
 
 namespace issm {
 
@@ -280,20 +281,22 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
         const bool valid = !bad && !invalid && isfinite((double)(T)ln);
         if (!valid) record_failure(failures, failure_index, 0, ISSM_REASON_MOMENT_FIT_INVALID);
     }
-    // inverse factor for the tensor-core forms: W = (f L)^-1 in FP32 from the
-    // stored factor, one column per thread, DP x DP row-major zero padded
+    // inverse factor for the tensor-core forms: W = (stored factor)^-1 in
+    // FP32, DP x DP row-major zero padded
     if (out_inverse != nullptr) {
-        const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
-        for (int e = threadIdx.x; e < DP * DP; e += blockDim.x) out_inverse[e] = 0.f;
+        constexpr int LD = 65;
+        float *Lf = reinterpret_cast<float *>(A + d * d);
+        float *Wf = Lf + 64 * LD;
+        for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+            const int r = e % d, c = e / d;
+            Lf[r * LD + c] = r >= c ? (float)(T)(A[e] * f) : 0.f;
+        }
         __syncthreads();
-        for (int c = threadIdx.x; c < d; c += blockDim.x) {
-            float w[64];
-            for (int r = c; r < d; ++r) {
-                float v = (r == c) ? 1.f : 0.f;
-                for (int q = c; q < r; ++q) v -= (float)(A[r + q * d] * f) * w[q];
-                w[r] = v / (float)(A[r + r * d] * f);
-                out_inverse[r * DP + c] = w[r];
-            }
+        invert_lower_f32(Lf, Wf, d, LD);
+        const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
+        for (int e = threadIdx.x; e < DP * DP; e += blockDim.x) {
+            const int j = e / DP, c = e % DP;
+            out_inverse[e] = (j < d && c < d) ? Wf[j * LD + c] : 0.f;
         }
     }
 }
@@ -302,7 +305,14 @@ int fit_factor(const double *mean, const double *cov, int d, const void *prev, d
                int dtype, void *out_loc, void *out_factor, void *out_lognorm, uint64_t *failures,
                int64_t failure_index, float *out_inverse, cudaStream_t stream) {
     if (d > 64) return ISSM_E_UNSUPPORTED;
-    const size_t smem = sizeof(double) * (size_t)d * d;
+    size_t smem = sizeof(double) * (size_t)d * d;
+    if (out_inverse != nullptr) {
+        smem += sizeof(float) * 2 * 64 * 65;
+        cudaError_t e = cudaFuncSetAttribute(dtype == ISSM_F32 ? (const void *)fit_factor_kernel<float>
+                                                               : (const void *)fit_factor_kernel<double>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+    }
     if (dtype == ISSM_F32) {
         const double reg = sqrt((double)FLT_EPSILON);
         { fit_factor_kernel<float><<<1, 256, smem, stream>>>(mean, cov, d, (const float *)prev, dof, logconst, reg,

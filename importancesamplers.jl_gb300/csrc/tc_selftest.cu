@@ -8,9 +8,11 @@
 
 namespace issm {
 
+// layout 0: core matrices K-group-major within 8-row groups (tc::kmajor_offset);
+// layout 1: row-contiguous per K group (tc::rowgroup_offset).
 __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__restrict__ A, const float *__restrict__ B,
                                                                float *__restrict__ C, int n, int k, int kind,
-                                                               int *status) {
+                                                               int layout, int *status) {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t bar;
     __shared__ uint32_t tmem_base;
@@ -26,13 +28,13 @@ __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__re
     }
     for (int e = threadIdx.x; e < 128 * k; e += blockDim.x) {
         const int r = e / k, c = e % k;
-        const uint32_t off = tc::kmajor_offset(r, c, kg, eb);
+        const uint32_t off = layout ? tc::rowgroup_offset(r, c, 128, eb) : tc::kmajor_offset(r, c, kg, eb);
         if (eb == 2) *reinterpret_cast<uint16_t *>(sa + off) = tc::bf16_bits(A[e]);
         else *reinterpret_cast<float *>(sa + off) = A[e];
     }
     for (int e = threadIdx.x; e < n * k; e += blockDim.x) {
         const int r = e / k, c = e % k;
-        const uint32_t off = tc::kmajor_offset(r, c, kg, eb);
+        const uint32_t off = layout ? tc::rowgroup_offset(r, c, n, eb) : tc::kmajor_offset(r, c, kg, eb);
         if (eb == 2) *reinterpret_cast<uint16_t *>(sb + off) = tc::bf16_bits(B[e]);
         else *reinterpret_cast<float *>(sb + off) = B[e];
     }
@@ -45,8 +47,10 @@ __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__re
         const uint32_t idesc = tc::instr_desc(kind, 128, n);
         const int steps = k * eb / 32;
         for (int s = 0; s < steps; ++s) {
-            const uint64_t da = tc::smem_desc(tc::smem_u32(sa) + s * 256, 128, kg * 128);
-            const uint64_t db = tc::smem_desc(tc::smem_u32(sb) + s * 256, 128, kg * 128);
+            const uint64_t da = layout ? tc::smem_desc(tc::smem_u32(sa) + s * 2 * 128 * 16, 128 * 16, 128)
+                                       : tc::smem_desc(tc::smem_u32(sa) + s * 256, 128, kg * 128);
+            const uint64_t db = layout ? tc::smem_desc(tc::smem_u32(sb) + s * 2 * n * 16, n * 16, 128)
+                                       : tc::smem_desc(tc::smem_u32(sb) + s * 256, 128, kg * 128);
             if (kind == tc::kBF16) tc::mma(tbase, da, db, idesc, s > 0);
             else tc::mma_tf32(tbase, da, db, idesc, s > 0);
         }
@@ -72,6 +76,8 @@ __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__re
 
 int tc_gemm_selftest(const float *a, const float *b, float *c, int n, int k, int kind, int *status,
                      cudaStream_t stream) {
+    const int layout = (kind >> 8) & 1;
+    kind &= 0xff;
     const int eb = kind == tc::kBF16 ? 2 : 4;
     const size_t smem = (size_t)(128 + n) * k * eb;
     auto kern = tc_gemm_selftest_kernel;
@@ -79,7 +85,7 @@ int tc_gemm_selftest(const float *a, const float *b, float *c, int n, int k, int
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return (int)e;
     }
-    { kern<<<1, 128, smem, stream>>>(a, b, c, n, k, kind, status); note_launch(); }
+    { kern<<<1, 128, smem, stream>>>(a, b, c, n, k, kind, layout, status); note_launch(); }
     return (int)cudaGetLastError();
 }
 

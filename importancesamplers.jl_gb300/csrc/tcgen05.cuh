@@ -30,6 +30,17 @@ __device__ __forceinline__ uint32_t kmajor_offset(int row, int k, int k_groups, 
     return (uint32_t)((((row >> 3) * k_groups + k / per) << 7) + ((row & 7) << 4) + (k % per) * elem_bytes);
 }
 
+// Row-contiguous variant of the same canonical layout: for each 16-byte K
+// group q the tile's `rows` rows are stored consecutively (row r at 16 r), so
+// core matrix (row group g, K group q) sits at q * rows * 16 + g * 128: the
+// leading byte offset is rows * 16 and the stride byte offset 128. Writing one
+// K group for 32 consecutive rows touches 512 contiguous bytes (no bank
+// conflicts), and one K slice of 32 bytes advances the start by 2 * rows * 16.
+__device__ __forceinline__ uint32_t rowgroup_offset(int row, int k, int rows, int elem_bytes) {
+    const int per = 16 / elem_bytes;
+    return (uint32_t)((k / per) * rows * 16 + row * 16 + (k % per) * elem_bytes);
+}
+
 // 64-bit shared-memory matrix descriptor (version 1, no swizzle).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes, uint32_t sbo_bytes) {
     uint64_t d = 0;
@@ -131,6 +142,35 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---- asynchronous copies ------------------------------------------------------
+// 16-byte global -> shared copy that bypasses L1 (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(void *dst_smem, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst_smem)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst_smem, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst_smem)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Expect `bytes` of bulk-copy completions on the mbarrier, and arrive once.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+// Bulk global -> shared copy (addresses 16-byte aligned, size a multiple of
+// 16) whose completion is counted on the mbarrier in bytes.
+__device__ __forceinline__ void bulk_copy_g2s(void *dst_smem, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst_smem)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
 }
 
 __device__ __forceinline__ uint16_t bf16_bits(float f) {

@@ -7,10 +7,11 @@ import torch
 pytestmark = pytest.mark.gpu
 
 
+@pytest.mark.parametrize("layout", [0, 1])
 @pytest.mark.parametrize("kind", ["bf16", "tf32"])
-@pytest.mark.parametrize("n,k", [(16, 16), (64, 32), (80, 64), (128, 48), (256, 64)])
-def test_tc_gemm_selftest_exact(issm, cuda, kind, n, k):
-    prec = issm.native.PREC_BF16 if kind == "bf16" else issm.native.PREC_TF32
+@pytest.mark.parametrize("n,k", [(16, 16), (64, 32), (80, 64), (128, 48), (192, 64), (256, 64)])
+def test_tc_gemm_selftest_exact(issm, cuda, kind, n, k, layout):
+    prec = (issm.native.PREC_BF16 if kind == "bf16" else issm.native.PREC_TF32) | (layout << 8)
     g = torch.Generator(device=cuda).manual_seed(n * 131 + k)
     a = torch.randint(-4, 5, (128, k), generator=g, device=cuda).float()
     b = torch.randint(-4, 5, (n, k), generator=g, device=cuda).float()
