@@ -7,12 +7,36 @@
 #include "issm_internal.h"
 
 #include <atomic>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 using namespace issm;
 
 namespace issm {
 static std::atomic<unsigned long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int allow_dynamic_smem(const void *kernel) {
+    static std::mutex mu;
+    static std::vector<std::pair<int, const void *>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return (int)e;
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto &k : done)
+        if (k.first == dev && k.second == kernel) return 0;
+    int optin = 0;
+    e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return (int)e;
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, kernel);
+    if (e != cudaSuccess) return (int)e;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
+    if (e != cudaSuccess) return (int)e;
+    done.emplace_back(dev, kernel);
+    return 0;
+}
 }  // namespace issm
 
 namespace {

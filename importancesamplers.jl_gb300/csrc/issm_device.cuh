@@ -118,6 +118,11 @@ template <typename T> __device__ __forceinline__ uint16_t target_reason(T v) {
 // Host-side count of kernels this library has launched (issm_kernel_launches).
 void note_launch();
 
+// Raise a kernel's dynamic shared-memory limit to the per-block maximum, once
+// per kernel and device. The limit is never lowered afterwards: a recorded
+// CUDA graph replays launches of several sizes and each must stay allowed.
+int allow_dynamic_smem(const void *kernel);
+
 inline int grid_for(int64_t n, int threads, int per_sm = 8) {
     int64_t blocks = (n + threads - 1) / threads;
     int64_t cap = (int64_t)kSMs * per_sm * 64;

@@ -555,8 +555,8 @@ static int launch_simt(MixParams<T> p, cudaStream_t stream) {
     size_t smem = range > 0 ? (size_t)chunk * per : 16;
     auto kern = mixture_simt_kernel<T, D, FACTOR>;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return (int)e;
+        const int e = allow_dynamic_smem((const void *)kern);
+        if (e) return e;
     }
     const int threads = 128;
     int64_t blocks = (p.n + threads - 1) / threads;

@@ -551,10 +551,10 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
                                                                        center);
       note_launch(); }
     auto kern = mixture_tc_kernel<KIND, SPLIT, DP>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return (int)e;
+    const int st = allow_dynamic_smem((const void *)kern);
+    if (st) return st;
     int occ = 1;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTcThreads, smem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kTcThreads, smem);
     if (e != cudaSuccess) return (int)e;
     const int nw2 = 2 * chunk * DP;
     const int ncols = nw2 <= 32 ? 32 : nw2 <= 64 ? 64 : nw2 <= 128 ? 128 : nw2 <= 256 ? 256 : 512;

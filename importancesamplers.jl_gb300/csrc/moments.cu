@@ -119,7 +119,10 @@ static int moments_t(const T *x, int d, int64_t n, const T *lw, const double *su
     const size_t smem = sizeof(T) * ((size_t)kMomTile * d + kMomTile);
     if (d * d > 16 * kMomThreads) return ISSM_E_UNSUPPORTED;
     auto kern = moments_partial_kernel<T>;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > 48 * 1024) {
+        const int e = allow_dynamic_smem((const void *)kern);
+        if (e) return e;
+    }
     { kern<<<blocks, kMomThreads, smem, stream>>>(x, d, n, lw, summary, shift, 0, partial); note_launch(); }
     { moments_finish_kernel<<<1, 256, 0, stream>>>(partial, blocks, d, 0, shift, mean, nullptr); note_launch(); }
     { kern<<<blocks, kMomThreads, smem, stream>>>(x, d, n, lw, summary, mean, 1, partial); note_launch(); }
@@ -308,10 +311,9 @@ int fit_factor(const double *mean, const double *cov, int d, const void *prev, d
     size_t smem = sizeof(double) * (size_t)d * d;
     if (out_inverse != nullptr) {
         smem += sizeof(float) * 2 * 64 * 65;
-        cudaError_t e = cudaFuncSetAttribute(dtype == ISSM_F32 ? (const void *)fit_factor_kernel<float>
-                                                               : (const void *)fit_factor_kernel<double>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return (int)e;
+        const int e = allow_dynamic_smem(dtype == ISSM_F32 ? (const void *)fit_factor_kernel<float>
+                                                           : (const void *)fit_factor_kernel<double>);
+        if (e) return e;
     }
     if (dtype == ISSM_F32) {
         const double reg = sqrt((double)FLT_EPSILON);

@@ -217,14 +217,14 @@ int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *su
     float *partial = (float *)ws;
     if (bf16) {
         auto kern = moments_tc_kernel<tc::kBF16>;
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return (int)e;
+        const int e = allow_dynamic_smem((const void *)kern);
+        if (e) return e;
         { kern<<<blocks, kMtThreads, smem, stream>>>((const float *)x, d, n, (const float *)lw, summary, shift,
                                                      partial, error); note_launch(); }
     } else {
         auto kern = moments_tc_kernel<tc::kTF32>;
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return (int)e;
+        const int e = allow_dynamic_smem((const void *)kern);
+        if (e) return e;
         { kern<<<blocks, kMtThreads, smem, stream>>>((const float *)x, d, n, (const float *)lw, summary, shift,
                                                      partial, error); note_launch(); }
     }

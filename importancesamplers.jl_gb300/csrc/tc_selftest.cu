@@ -82,8 +82,8 @@ int tc_gemm_selftest(const float *a, const float *b, float *c, int n, int k, int
     const size_t smem = (size_t)(128 + n) * k * eb;
     auto kern = tc_gemm_selftest_kernel;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return (int)e;
+        const int e = allow_dynamic_smem((const void *)kern);
+        if (e) return e;
     }
     { kern<<<1, 128, smem, stream>>>(a, b, c, n, k, kind, layout, status); note_launch(); }
     return (int)cudaGetLastError();
