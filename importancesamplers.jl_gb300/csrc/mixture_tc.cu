@@ -50,37 +50,40 @@ __device__ __forceinline__ uint32_t tf32_bits(float f) {
     return u & ~0x1FFFu;
 }
 
-// 16 bytes of operand values: 4 tf32, or 8 bf16 (the hi part, or the lo part
-// bf16(v - hi)).
-template <int KIND> __device__ __forceinline__ uint4 pack16(const float *v, bool lo_part) {
-    if (KIND == tc::kTF32) return make_uint4(tf32_bits(v[0]), tf32_bits(v[1]), tf32_bits(v[2]), tf32_bits(v[3]));
-    uint32_t h[4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const float a = v[2 * i], c = v[2 * i + 1];
-        uint16_t ha = tc::bf16_bits(a), hc = tc::bf16_bits(c);
-        if (lo_part) {
-            ha = tc::bf16_bits(a - __uint_as_float((uint32_t)ha << 16));
-            hc = tc::bf16_bits(c - __uint_as_float((uint32_t)hc << 16));
-        }
-        h[i] = (uint32_t)ha | ((uint32_t)hc << 16);
-    }
-    return make_uint4(h[0], h[1], h[2], h[3]);
+// 16 bytes of operand values from v[PER]: 4 tf32 (nearest even), or 8 bf16
+// (the hi part; pack_lo gives the lo part bf16(v - hi)).
+template <int KIND> __device__ __forceinline__ uint4 pack_hi(const float *v) {
+    if (KIND == tc::kTF32) return make_uint4(tc::tf32_rn(v[0]), tc::tf32_rn(v[1]), tc::tf32_rn(v[2]), tc::tf32_rn(v[3]));
+    return make_uint4(tc::pack_bf16x2(v[0], v[1]), tc::pack_bf16x2(v[2], v[3]), tc::pack_bf16x2(v[4], v[5]),
+                      tc::pack_bf16x2(v[6], v[7]));
+}
+__device__ __forceinline__ uint32_t lo_pair(float a, float b, uint32_t hi) {
+    return tc::pack_bf16x2(a - __uint_as_float(hi << 16), b - __uint_as_float(hi & 0xffff0000u));
+}
+__device__ __forceinline__ uint4 pack_lo(const float *v, uint4 hi) {
+    return make_uint4(lo_pair(v[0], v[1], hi.x), lo_pair(v[2], v[3], hi.y), lo_pair(v[4], v[5], hi.z),
+                      lo_pair(v[6], v[7], hi.w));
 }
 
-// Operand form of slot k, NPART parts of DP x DP elements each: part p, K
-// group q, row j at byte  p * DP*DP*EB + q * DP*16 + j * 16.
+// Operand form of slot k: the DP x (DP + X) matrix [W_k | -b_k | 0], X = 16
+// bf16 or 8 tf32 elements (two extra 16-byte K groups), so the MMA yields
+// z = W_k (x - c) - b_k directly against samples extended by a constant 1.
+// NPART parts of KGX = KG + 2 groups: part p, K group q, row j at byte
+//   p * DP*KGX*16 + q * DP*16 + j * 16.
 template <int KIND, int SPLIT, int DP>
 __global__ void __launch_bounds__(256) tc_prepare_kernel(const float *__restrict__ w, const float *__restrict__ loc,
                                                          int d, int first, int cslot, unsigned char *__restrict__ ops,
-                                                         float *__restrict__ bvec, float *__restrict__ center) {
+                                                         float *__restrict__ center) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
     constexpr int PER = 16 / EB;
     constexpr int KG = DP / PER;
+    constexpr int KGX = KG + 2;
     constexpr int NPART = SPLIT == 3 ? 2 : 1;
     constexpr int LD = DP + 1;
+    constexpr int B_COMP = DP * KGX * 16;
     __shared__ float ws[DP * LD];
     __shared__ float dc[DP];
+    __shared__ float nb[DP];
     const int k = first + blockIdx.x;
     const float *wk = w + (size_t)k * DP * DP;
     for (int e = threadIdx.x; e < DP * DP; e += blockDim.x) ws[(e / DP) * LD + e % DP] = wk[e];
@@ -90,20 +93,23 @@ __global__ void __launch_bounds__(256) tc_prepare_kernel(const float *__restrict
         if (blockIdx.x == 0) center[c] = cc;
     }
     __syncthreads();
-    unsigned char *okp = ops + (size_t)k * NPART * DP * DP * EB;
-    for (int e = threadIdx.x; e < NPART * KG * DP; e += blockDim.x) {
-        const int part = e / (KG * DP), rem = e - part * KG * DP, q = rem / DP, j = rem - q * DP;
-        float v[PER];
-#pragma unroll
-        for (int m = 0; m < PER; ++m) v[m] = ws[j * LD + q * PER + m];
-        *reinterpret_cast<uint4 *>(okp + (size_t)part * DP * DP * EB + (size_t)q * DP * 16 + (size_t)j * 16) =
-            pack16<KIND>(v, part == 1);
-    }
-    // b_k = W_k (mu_k - c) in FP32
+    // -b_k = -W_k (mu_k - c) in FP32
     for (int j = threadIdx.x; j < DP; j += blockDim.x) {
         float acc = 0.f;
         for (int c = 0; c < d; ++c) acc = fmaf(ws[j * LD + c], dc[c], acc);
-        bvec[(size_t)k * DP + j] = acc;
+        nb[j] = -acc;
+    }
+    __syncthreads();
+    unsigned char *okp = ops + (size_t)k * NPART * B_COMP;
+    for (int e = threadIdx.x; e < KGX * DP; e += blockDim.x) {
+        const int q = e / DP, j = e - q * DP;
+        float v[PER];
+#pragma unroll
+        for (int m = 0; m < PER; ++m)
+            v[m] = q < KG ? ws[j * LD + q * PER + m] : (q == KG && m == 0 ? nb[j] : 0.f);
+        const uint4 hi = pack_hi<KIND>(v);
+        *reinterpret_cast<uint4 *>(okp + (size_t)q * DP * 16 + (size_t)j * 16) = hi;
+        if (NPART == 2) *reinterpret_cast<uint4 *>(okp + B_COMP + (size_t)q * DP * 16 + (size_t)j * 16) = pack_lo(v, hi);
     }
 }
 
@@ -113,7 +119,7 @@ struct TcParams {
     int64_t n;
     const float *x;
     const unsigned char *ops;
-    const float *bvec, *center;
+    const float *center;
     const float *lognorm, *coef, *dofs;
     const int32_t *group;
     float *out_logden, *out_generating, *lognum;
@@ -126,25 +132,28 @@ template <int KIND, int SPLIT, int DP>
 __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
     constexpr int PER = 16 / EB;              // elements per 16-byte K group
-    constexpr int KG = DP / PER;              // K groups of one row
+    constexpr int KG = DP / PER;              // K groups of the sample coordinates
+    constexpr int KGX = KG + 2;               // plus the constant-1 column and padding
     constexpr int QH = KG / 2;                // K groups converted per thread
     constexpr int NPART = SPLIT == 3 ? 2 : 1;
     constexpr int RS = DP + 4;                // padded raw row (floats): conflict-free row reads
     constexpr int RAW_BYTES = kTcTile * RS * 4;
-    constexpr int A_PART = kTcTile * DP * EB;
-    constexpr int B_COMP = DP * DP * EB;
-    constexpr int KSTEPS = DP * EB / 32;      // MMA K slices of 32 bytes
+    constexpr int A_PART = kTcTile * KGX * 16;
+    constexpr int B_COMP = DP * KGX * 16;
+    constexpr int KSTEPS = KGX / 2;           // MMA K slices of 32 bytes
     constexpr uint32_t LBO_A = kTcTile * 16;
+    constexpr int HALF = DP / 2;              // columns per warp half when one component is split
     const int chunk = p.chunk, nchunks = p.nchunks, S = p.raw_stages;
     const int nbufB = nchunks > 1 ? 2 : 1;
     const uint32_t LBO_B = (uint32_t)(chunk * DP * 16);
+    // one component per tile: both warp halves share it, by column halves
+    const bool split_cols = (nchunks == 1 && chunk == 1);
 
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *s_raw = smem;
     unsigned char *s_a = s_raw + (size_t)S * RAW_BYTES;
     unsigned char *s_b = s_a + (size_t)2 * NPART * A_PART;
-    float *s_bv = reinterpret_cast<float *>(s_b + (size_t)nbufB * NPART * chunk * B_COMP);
-    float *s_x = s_bv + 3 * chunk * DP;
+    float *s_x = reinterpret_cast<float *>(s_b + (size_t)nbufB * NPART * chunk * B_COMP);
     float *s_c = s_x + 4 * kTcTile;
     __shared__ __align__(8) uint64_t bar_mma[2];
     __shared__ __align__(8) uint64_t bar_b[2];
@@ -164,6 +173,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
         abort_flag = 0;
     }
     for (int c = tid; c < DP; c += kTcThreads) s_c[c] = p.center[c];
+    // constant K groups of both A buffers: a 1 in column DP (hi part), zeros elsewhere
+    for (int e = tid; e < 2 * NPART * 2 * kTcTile; e += kTcThreads) {
+        const int row = e % kTcTile, g = (e / kTcTile) & 1, part = (e / (2 * kTcTile)) % NPART,
+                  buf = e / (2 * kTcTile * NPART);
+        const uint32_t one = KIND == tc::kTF32 ? 0x3F800000u : 0x3F80u;
+        const uint32_t first = (g == 0 && part == 0) ? one : 0u;
+        *reinterpret_cast<uint4 *>(s_a + (size_t)(buf * NPART + part) * A_PART + (size_t)(KG + g) * LBO_A +
+                                   row * 16) = make_uint4(first, 0u, 0u, 0u);
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -187,7 +205,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
             const int rows = (int)min((int64_t)kTcTile, p.n - row0);
             float *dst = reinterpret_cast<float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
             const float *src = p.x + row0 * p.d;
-            if (vec) {
+            if (vec && p.d == DP) {
+                constexpr int Q4 = DP / 4;
+                const int total = rows * Q4;
+                for (int e = tid; e < total; e += kTcThreads) {
+                    const int r = e / Q4, c4 = e % Q4;
+                    tc::cp_async16(dst + r * RS + c4 * 4, src + (size_t)e * 4);
+                }
+            } else if (vec) {
                 const int q4 = p.d >> 2, total = rows * q4;
                 for (int e = tid; e < total; e += kTcThreads) {
                     const int r = e / q4, c4 = e - r * q4;
@@ -215,19 +240,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
         int k0, cnt;
         chunk_range(j % nchunks, k0, cnt);
         const int buf = nbufB == 1 ? 0 : (j & 1);
-        const uint32_t bytes = (uint32_t)(NPART * KG * cnt * DP * 16 + cnt * DP * 4);
+        const uint32_t bytes = (uint32_t)(NPART * KGX * cnt * DP * 16);
         if (lane == 0) tc::mbar_arrive_expect_tx(&bar_b[buf], bytes);
         __syncwarp();
         unsigned char *dstb = s_b + (size_t)buf * NPART * chunk * B_COMP;
-        for (int e = lane; e < NPART * KG * cnt; e += 32) {
-            const int part = e / (KG * cnt), rem = e - part * KG * cnt, q = rem / cnt, kk = rem - q * cnt;
+        for (int e = lane; e < NPART * KGX * cnt; e += 32) {
+            const int part = e / (KGX * cnt), rem = e - part * KGX * cnt, q = rem / cnt, kk = rem - q * cnt;
             const unsigned char *src = p.ops + ((size_t)(k0 + kk) * NPART + part) * B_COMP + (size_t)q * DP * 16;
             unsigned char *dst = dstb + (size_t)part * chunk * B_COMP + (size_t)q * LBO_B + (size_t)kk * DP * 16;
             tc::bulk_copy_g2s(dst, src, DP * 16, &bar_b[buf]);
         }
-        if (lane == 0)
-            tc::bulk_copy_g2s(s_bv + (nchunks == 1 ? 0 : j % 3) * chunk * DP, p.bvec + (size_t)k0 * DP,
-                              (uint32_t)(cnt * DP * 4), &bar_b[buf]);
         ++b_issued;
     };
 
@@ -248,14 +270,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
                 const int c = q * PER + m;
                 float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (active) f = *reinterpret_cast<const float4 *>(raw + row * RS + c);
-                v[m] = (active && c < p.d) ? f.x - s_c[c] : 0.f;
-                v[m + 1] = (active && c + 1 < p.d) ? f.y - s_c[c + 1] : 0.f;
-                v[m + 2] = (active && c + 2 < p.d) ? f.z - s_c[c + 2] : 0.f;
-                v[m + 3] = (active && c + 3 < p.d) ? f.w - s_c[c + 3] : 0.f;
+                const float4 cc = *reinterpret_cast<const float4 *>(s_c + c);
+                v[m] = (active && c < p.d) ? f.x - cc.x : 0.f;
+                v[m + 1] = (active && c + 1 < p.d) ? f.y - cc.y : 0.f;
+                v[m + 2] = (active && c + 2 < p.d) ? f.z - cc.z : 0.f;
+                v[m + 3] = (active && c + 3 < p.d) ? f.w - cc.w : 0.f;
             }
-            *reinterpret_cast<uint4 *>(a + (size_t)q * LBO_A + row * 16) = pack16<KIND>(v, false);
-            if (NPART == 2)
-                *reinterpret_cast<uint4 *>(a + A_PART + (size_t)q * LBO_A + row * 16) = pack16<KIND>(v, true);
+            const uint4 hi = pack_hi<KIND>(v);
+            *reinterpret_cast<uint4 *>(a + (size_t)q * LBO_A + row * 16) = hi;
+            if (NPART == 2) *reinterpret_cast<uint4 *>(a + A_PART + (size_t)q * LBO_A + row * 16) = pack_lo(v, hi);
         }
         if (p.mode == 1 && half == 0) {
             const float l = active ? p.lognum[i] : 0.f;
@@ -298,74 +321,97 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     const int qd = warp & 3, h = warp >> 2;
     const int erow = 32 * qd + lane;
     LseState<float> lse;
-    float gen_lq = 0.f, last_lq = 0.f;
+    float gen_lq = 0.f, last_lq = 0.f, r2_half = 0.f;
     bool has_gen = false;
+    auto radial = [&](int k, float r2) -> float {
+        if (p.family == ISSM_GAUSSIAN) return p.lognorm[k] - 0.5f * r2;
+        const float nu = p.dofs[k];
+        return p.lognorm[k] - (nu + (float)p.d) * 0.5f * log1pf(r2 / nu);
+    };
+    auto take = [&](int k, float lq) {
+        bool member = true;
+        if (p.den_kind == ISSM_DENOM_GENERATING) member = (k == p.fixed_slot);
+        else if (p.den_kind == ISSM_DENOM_PARTIAL) member = (p.group[k] == ggen);
+        if (k == p.fixed_slot) {
+            gen_lq = lq;
+            has_gen = true;
+        }
+        last_lq = lq;
+        if (member) lse.add((p.coef ? p.coef[k] : 0.f) + lq);
+    };
     auto epilogue = [&](int j, bool good) {
         const int it = j / nchunks, ch = j - it * nchunks;
         int k0, cnt;
         chunk_range(ch, k0, cnt);
         if (good) {
             const uint32_t lane_base = tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)((j & 1) * NW);
-            const float *bv = s_bv + (nchunks == 1 ? 0 : j % 3) * chunk * DP;
-            for (int kk = h; kk < cnt; kk += 2) {
-                const int k = k0 + kk;
+            if (split_cols) {
                 float r2 = 0.f;
+                if (HALF >= 16) {
 #pragma unroll
-                for (int c0 = 0; c0 < DP; c0 += 16) {
-                    float v[16];
-                    tc::tmem_ld16(lane_base + (uint32_t)(kk * DP + c0), v);
+                    for (int c0 = 0; c0 < HALF; c0 += 16) {
+                        float v[16];
+                        tc::tmem_ld16(lane_base + (uint32_t)(h * HALF + c0), v);
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) {
-                        const float z = v[q] - bv[kk * DP + c0 + q];
-                        r2 = fmaf(z, z, r2);
+                        for (int q = 0; q < 16; ++q) r2 = fmaf(v[q], v[q], r2);
                     }
-                }
-                float lq;
-                if (p.family == ISSM_GAUSSIAN) {
-                    lq = p.lognorm[k] - 0.5f * r2;
                 } else {
-                    const float nu = p.dofs[k];
-                    lq = p.lognorm[k] - (nu + (float)p.d) * 0.5f * log1pf(r2 / nu);
+                    float v[8];
+                    tc::tmem_ld8(lane_base + (uint32_t)(h * HALF), v);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) r2 = fmaf(v[q], v[q], r2);
                 }
-                bool member = true;
-                if (p.den_kind == ISSM_DENOM_GENERATING) member = (k == p.fixed_slot);
-                else if (p.den_kind == ISSM_DENOM_PARTIAL) member = (p.group[k] == ggen);
-                if (k == p.fixed_slot) {
-                    gen_lq = lq;
-                    has_gen = true;
+                r2_half = r2;
+            } else {
+                for (int kk = h; kk < cnt; kk += 2) {
+                    float r2 = 0.f;
+#pragma unroll
+                    for (int c0 = 0; c0 < DP; c0 += 16) {
+                        float v[16];
+                        tc::tmem_ld16(lane_base + (uint32_t)(kk * DP + c0), v);
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) r2 = fmaf(v[q], v[q], r2);
+                    }
+                    take(k0 + kk, radial(k0 + kk, r2));
                 }
-                last_lq = lq;
-                if (member) lse.add((p.coef ? p.coef[k] : 0.f) + lq);
             }
         }
         if (ch != nchunks - 1) return;
         // tile complete: the upper half hands its state to the lower half
         if (h == 1) {
-            s_x[erow] = lse.m;
-            s_x[kTcTile + erow] = lse.s;
-            s_x[2 * kTcTile + erow] = gen_lq;
-            s_x[3 * kTcTile + erow] = (float)((lse.nan ? 2 : 0) | (has_gen ? 1 : 0));
+            if (split_cols) {
+                s_x[erow] = r2_half;
+            } else {
+                s_x[erow] = lse.m;
+                s_x[kTcTile + erow] = lse.s;
+                s_x[2 * kTcTile + erow] = gen_lq;
+                s_x[3 * kTcTile + erow] = (float)((lse.nan ? 2 : 0) | (has_gen ? 1 : 0));
+            }
         }
         __syncthreads();
         if (h == 0 && good) {
-            const float om = s_x[erow], os = s_x[kTcTile + erow];
-            const int of = (int)s_x[3 * kTcTile + erow];
-            if (of & 2) lse.nan = true;
-            if (of & 1) {
-                gen_lq = s_x[2 * kTcTile + erow];
-                has_gen = true;
-            }
-            if (om != -INFINITY) {
-                if (lse.m == -INFINITY) {
-                    lse.m = om;
-                    lse.s = os;
-                } else if (om > lse.m) {
-                    lse.s = lse.s * expf(lse.m - om) + os;
-                    lse.m = om;
-                } else if (om == lse.m) {
-                    lse.s += os;
-                } else {
-                    lse.s += os * expf(om - lse.m);
+            if (split_cols) {
+                take(k0, radial(k0, r2_half + s_x[erow]));
+            } else {
+                const float om = s_x[erow], os = s_x[kTcTile + erow];
+                const int of = (int)s_x[3 * kTcTile + erow];
+                if (of & 2) lse.nan = true;
+                if (of & 1) {
+                    gen_lq = s_x[2 * kTcTile + erow];
+                    has_gen = true;
+                }
+                if (om != -INFINITY) {
+                    if (lse.m == -INFINITY) {
+                        lse.m = om;
+                        lse.s = os;
+                    } else if (om > lse.m) {
+                        lse.s = lse.s * expf(lse.m - om) + os;
+                        lse.m = om;
+                    } else if (om == lse.m) {
+                        lse.s += os;
+                    } else {
+                        lse.s += os * expf(om - lse.m);
+                    }
                 }
             }
             const int64_t i = tile_of(it) * kTcTile + erow;
@@ -394,6 +440,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
         lse = LseState<float>();
         gen_lq = 0.f;
         last_lq = 0.f;
+        r2_half = 0.f;
         has_gen = false;
     };
 
@@ -510,23 +557,26 @@ int invert_factors(const issm_bank *bk, int first, int count, float *out, cudaSt
     return (int)cudaGetLastError();
 }
 
-// Workspace: operand forms K x DP*DP*4 bytes | b vectors K x DP | centre
-// (256 bytes) | inverse factors K x DP*DP (only when the bank has none).
+// Workspace: operand forms K x DP * (4 DP + 64) bytes | centre (256 bytes) |
+// inverse factors K x DP * DP floats (only when the bank has none).
 static int dp_of(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : 64; }
+static size_t ops_slot_bytes(int DP) { return (size_t)DP * (4 * DP + 64); }
 
 size_t tc_workspace_bytes(int k, int d) {
     const int DP = dp_of(d);
-    return (size_t)2 * k * DP * DP * 4 + (size_t)k * DP * 4 + 256 + 64;
+    return (size_t)k * ops_slot_bytes(DP) + 256 + (size_t)k * DP * DP * 4 + 64;
 }
 
 template <int KIND, int SPLIT, int DP>
-static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, unsigned char *ops, float *bvec,
-                     float *center, cudaStream_t stream) {
+static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, unsigned char *ops, float *center,
+                     cudaStream_t stream) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
+    constexpr int KGX = DP * EB / 16 + 2;
     constexpr int NPART = SPLIT == 3 ? 2 : 1;
     constexpr size_t RAW_BYTES = (size_t)kTcTile * (DP + 4) * 4;
-    constexpr size_t A_PART = (size_t)kTcTile * DP * EB;
-    constexpr size_t B_COMP = (size_t)DP * DP * EB;
+    constexpr size_t A_PART = (size_t)kTcTile * KGX * 16;
+    constexpr size_t B_COMP = (size_t)DP * KGX * 16;
+    static_assert(NPART * B_COMP <= (size_t)DP * (4 * DP + 64), "operand form exceeds its workspace slot");
     const int nslots = p.last_slot - p.first_slot + 1;
     int chunk = min(nslots, 256 / DP);
     size_t smem = 0;
@@ -537,7 +587,7 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
         const int nbufB = nch > 1 ? 2 : 1;
         for (; stages >= 1; --stages) {
             smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)nbufB * NPART * chunk * B_COMP +
-                   (size_t)3 * chunk * DP * 4 + (size_t)4 * kTcTile * 4 + (size_t)DP * 4;
+                   (size_t)4 * kTcTile * 4 + (size_t)DP * 4;
             if (smem <= kTcMaxSmem) break;
         }
         if (stages >= 1 || chunk == 1) break;
@@ -547,8 +597,7 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     p.chunk = chunk;
     p.nchunks = nch;
     p.raw_stages = stages;
-    { tc_prepare_kernel<KIND, SPLIT, DP><<<nslots, 256, 0, stream>>>(w, loc, p.d, p.first_slot, cslot, ops, bvec,
-                                                                       center);
+    { tc_prepare_kernel<KIND, SPLIT, DP><<<nslots, 256, 0, stream>>>(w, loc, p.d, p.first_slot, cslot, ops, center);
       note_launch(); }
     auto kern = mixture_tc_kernel<KIND, SPLIT, DP>;
     const int st = allow_dynamic_smem((const void *)kern);
@@ -578,8 +627,7 @@ int tc_mixture(const issm_bank *bk, const issm_denominator *den, int mode, int f
     const int K = bk->count;
     if (ws_bytes < tc_workspace_bytes(K, d)) return ISSM_E_WORKSPACE;
     unsigned char *ops = (unsigned char *)ws;
-    float *bvec = (float *)(ops + (size_t)K * DP * DP * 4);
-    float *center = bvec + (size_t)K * DP;
+    float *center = (float *)(ops + (size_t)K * ops_slot_bytes(DP));
     float *winv = (float *)((unsigned char *)center + 256);
     const int den_kind = den ? den->kind : ISSM_DENOM_FULL;
     // only the generating slot contributes to a generating-only denominator
@@ -594,7 +642,7 @@ int tc_mixture(const issm_bank *bk, const issm_denominator *den, int mode, int f
     TcParams p{};
     p.d = d; p.mode = mode; p.family = bk->family; p.den_kind = den_kind; p.fixed_slot = fixed_slot;
     p.first_slot = first; p.last_slot = last;
-    p.n = n; p.x = (const float *)x; p.ops = ops; p.bvec = bvec; p.center = center;
+    p.n = n; p.x = (const float *)x; p.ops = ops; p.center = center;
     p.lognorm = (const float *)bk->lognormalizers; p.coef = (const float *)coef; p.dofs = (const float *)bk->dofs;
     p.group = den ? den->group_of_slot : nullptr;
     p.out_logden = (float *)out_logden; p.out_generating = (float *)out_generating;
@@ -602,13 +650,13 @@ int tc_mixture(const issm_bank *bk, const issm_denominator *den, int mode, int f
     const float *loc = (const float *)bk->locations;
     const bool tf32 = precision == ISSM_PREC_TF32;
     if (DP == 16)
-        return tf32 ? launch_tc<tc::kTF32, 1, 16>(p, w, loc, cslot, ops, bvec, center, stream)
-                    : launch_tc<tc::kBF16, 3, 16>(p, w, loc, cslot, ops, bvec, center, stream);
+        return tf32 ? launch_tc<tc::kTF32, 1, 16>(p, w, loc, cslot, ops, center, stream)
+                    : launch_tc<tc::kBF16, 3, 16>(p, w, loc, cslot, ops, center, stream);
     if (DP == 32)
-        return tf32 ? launch_tc<tc::kTF32, 1, 32>(p, w, loc, cslot, ops, bvec, center, stream)
-                    : launch_tc<tc::kBF16, 3, 32>(p, w, loc, cslot, ops, bvec, center, stream);
-    return tf32 ? launch_tc<tc::kTF32, 1, 64>(p, w, loc, cslot, ops, bvec, center, stream)
-                : launch_tc<tc::kBF16, 3, 64>(p, w, loc, cslot, ops, bvec, center, stream);
+        return tf32 ? launch_tc<tc::kTF32, 1, 32>(p, w, loc, cslot, ops, center, stream)
+                    : launch_tc<tc::kBF16, 3, 32>(p, w, loc, cslot, ops, center, stream);
+    return tf32 ? launch_tc<tc::kTF32, 1, 64>(p, w, loc, cslot, ops, center, stream)
+                : launch_tc<tc::kBF16, 3, 64>(p, w, loc, cslot, ops, center, stream);
 }
 
 }  // namespace issm

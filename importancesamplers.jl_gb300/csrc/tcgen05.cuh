@@ -173,6 +173,31 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst_smem, const void *src, u
         : "memory");
 }
 
+// Two FP32 values rounded to nearest-even bf16 and packed: a in the low half,
+// b in the high half (cvt.rn.bf16x2 puts its first source in the high half).
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    uint32_t r;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+    return r;
+}
+// FP32 rounded to nearest-even tf32 (low 13 mantissa bits cleared).
+__device__ __forceinline__ uint32_t tf32_rn(float f) {
+    uint32_t r;
+    asm("cvt.rn.tf32.f32 %0, %1;" : "=r"(r) : "f"(f));
+    return r;
+}
+
+// 8-column variant of tmem_ld16.
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 __device__ __forceinline__ uint16_t bf16_bits(float f) {
     // round to nearest even (finite inputs); NaN stays NaN
     uint32_t u = __float_as_uint(f);
