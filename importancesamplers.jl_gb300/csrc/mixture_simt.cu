@@ -541,8 +541,89 @@ __global__ void __launch_bounds__(128) mixture_simt_kernel(MixParams<T> p) {
     if (p.out_generating) p.out_generating[i] = gen_lq;
 }
 
+// Fixed-slot draws from one factor component, x = mu + L (m z) with the
+// reference's summation order (mu first, then q = 0..r): the factor is staged
+// once per CTA (coalesced from its column-major storage), tiles of 128 normal
+// rows are staged through padded shared memory with coalesced loads, each
+// thread turns its row into a sample in place (rows r descending, so z[q <= r]
+// is still intact), and the tile is stored back coalesced.
+template <typename T, int D>
+__global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
+    constexpr int LD = D + 1;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *Ls = reinterpret_cast<T *>(smem_raw);  // D x LD, row r = L[r, :]
+    T *mus = Ls + D * LD;
+    T *zt = mus + D;                           // 128 x LD
+    const int d = p.d, k = p.fixed_slot, tid = threadIdx.x;
+    const T *Lk = p.scales + (size_t)k * d * d;
+    for (int e = tid; e < d * d; e += blockDim.x) {
+        const int r = e % d, c = e / d;
+        Ls[r * LD + c] = Lk[e];
+    }
+    for (int r = tid; r < d; r += blockDim.x) mus[r] = p.loc[(size_t)k * d + r];
+    const T dof = p.family == ISSM_STUDENT_T ? p.dofs[k] : T(0);
+    __syncthreads();
+    const int64_t ntiles = (p.n + 127) / 128;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t row0 = tile * 128;
+        const int rows = (int)min((int64_t)128, p.n - row0);
+        const T *nz = p.normals + row0 * d;
+        for (int e = tid; e < rows * d; e += blockDim.x) {
+            const int r = e / d, c = e - r * d;
+            zt[r * LD + c] = nz[e];
+        }
+        __syncthreads();
+        if (tid < rows) {
+            const int64_t i = row0 + tid;
+            T m = T(1);
+            if (p.family == ISSM_STUDENT_T) {
+                uint16_t rr;
+                m = radial_multiplier(dof, p.rnormals + (size_t)i * p.rn_stride,
+                                      p.runiforms ? p.runiforms + (size_t)i * p.ru_stride : nullptr,
+                                      p.runiforms != nullptr && p.ru_stride > 0, &rr);
+                if (rr) {
+                    record_failure(p.failures, p.index_base + i + 1, 0, rr);
+                    m = qnan<T>();
+                }
+            }
+            T *z = zt + tid * LD;
+            if (m != T(1))
+                for (int q = 0; q < d; ++q) z[q] = z[q] * m;
+            bool valid = true;
+            for (int r = d - 1; r >= 0; --r) {
+                T v = mus[r];
+                const T *Lr = Ls + r * LD;
+                for (int q = 0; q <= r; ++q) v += Lr[q] * z[q];
+                z[r] = v;
+                valid &= (bool)isfinite(v);
+            }
+            if (!valid) record_failure(p.failures, p.index_base + i + 1, 0, ISSM_REASON_GENERATED_NONFINITE);
+        }
+        __syncthreads();
+        T *out = p.samples_out + row0 * d;
+        for (int e = tid; e < rows * d; e += blockDim.x) {
+            const int r = e / d, c = e - r * d;
+            out[e] = zt[r * LD + c];
+        }
+        __syncthreads();
+    }
+}
+
 template <typename T, int D, bool FACTOR>
 static int launch_simt(MixParams<T> p, cudaStream_t stream) {
+    if (FACTOR && p.mode == kModeDraw && p.slots == nullptr && p.samples_out != nullptr) {
+        const size_t smem = sizeof(T) * ((size_t)D * (D + 1) + D + (size_t)128 * (D + 1));
+        auto kern = draw_fixed_kernel<T, D>;
+        if (smem > 48 * 1024) {
+            const int e = allow_dynamic_smem((const void *)kern);
+            if (e) return e;
+        }
+        const int64_t tiles = (p.n + 127) / 128;
+        const int blocks = (int)min(tiles, (int64_t)kSMs * 4);
+        if (blocks < 1) return 0;
+        { kern<<<blocks, 128, smem, stream>>>(p); note_launch(); }
+        return (int)cudaGetLastError();
+    }
     using Ly = Layout<D, FACTOR>;
     const size_t per = (size_t)Ly::kStride * sizeof(T);
     const size_t budget = 96 * 1024;

@@ -68,15 +68,15 @@ template <typename T> __device__ Moments3 block_merge3(Moments3 v) {
     return Moments3{M, ts, ts2};
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, int64_t n, double *out,
-                                                      Moments3 *partials, unsigned int *counter) {
+// Per-thread running (max, S, S2). FP64 data accumulates in FP64; FP32 data
+// accumulates in FP32 with Kahan compensation (error about 2 ulp of the
+// thread's sum however many terms it takes, and none of the slow FP64
+// additions per element), then every merge above the thread is FP64.
+template <typename T> struct ThreadSums {
     T m = -num<T>::inf();
     double s = 0.0, s2 = 0.0;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        const T l = lw[i];
-        if (l == -num<T>::inf()) continue;
+    __device__ __forceinline__ void add(T l) {
+        if (l == -num<T>::inf()) return;
         if (l > m) {
             if (m != -num<T>::inf()) {
                 const double r = (double)dexp(m - l);
@@ -89,7 +89,60 @@ __global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, 
         s += e;
         s2 += e * e;
     }
-    Moments3 v = block_merge3<T>(Moments3{(double)m, s, s2});
+    __device__ __forceinline__ Moments3 result() const { return Moments3{(double)m, s, s2}; }
+};
+template <> struct ThreadSums<float> {
+    float m = -INFINITY;
+    float s = 0.f, cs = 0.f, s2 = 0.f, cs2 = 0.f;
+    __device__ __forceinline__ static void kahan(float &sum, float &c, float x) {
+        const float y = x - c;
+        const float t = sum + y;
+        c = (t - sum) - y;
+        sum = t;
+    }
+    __device__ __forceinline__ void add(float l) {
+        if (l == -INFINITY) return;
+        if (l > m) {
+            if (m != -INFINITY) {
+                const float r = expf(m - l);
+                s *= r;
+                cs *= r;
+                s2 *= r * r;
+                cs2 *= r * r;
+            }
+            m = l;
+        }
+        const float e = expf(l - m);
+        kahan(s, cs, e);
+        kahan(s2, cs2, e * e);
+    }
+    __device__ __forceinline__ Moments3 result() const {
+        return Moments3{(double)m, (double)s - (double)cs, (double)s2 - (double)cs2};
+    }
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, int64_t n, double *out,
+                                                      Moments3 *partials, unsigned int *counter) {
+    ThreadSums<T> acc;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (sizeof(T) == 4 && (reinterpret_cast<uintptr_t>(lw) & 15) == 0) {
+        // four weights per load; the tail (< 4 weights) goes to the first threads
+        const int64_t n4 = n >> 2;
+        const float4 *lw4 = reinterpret_cast<const float4 *>(lw);
+        for (int64_t i = t0; i < n4; i += stride) {
+            const float4 q = lw4[i];
+            acc.add((T)q.x);
+            acc.add((T)q.y);
+            acc.add((T)q.z);
+            acc.add((T)q.w);
+        }
+        if (t0 < (n & 3)) acc.add(lw[(n4 << 2) + t0]);
+    } else {
+        for (int64_t i = t0; i < n; i += stride) acc.add(lw[i]);
+    }
+    Moments3 v = block_merge3<T>(acc.result());
     __shared__ bool last;
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = v;
@@ -128,7 +181,7 @@ __global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, 
 }
 
 static int summary_blocks(int64_t n) {
-    int64_t b = (n + 256 * 8 - 1) / (256 * 8);
+    int64_t b = (n + 256 * 16 - 1) / (256 * 16);
     if (b > kSMs * 8) b = kSMs * 8;
     return b < 1 ? 1 : (int)b;
 }
