@@ -124,7 +124,7 @@ template <> struct ThreadSums<float> {
 template <typename T>
 __global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, int64_t n, double *out,
                                                       Moments3 *partials, unsigned int *counter) {
-    ThreadSums<T> acc;
+    ThreadSums<T> ts;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (sizeof(T) == 4 && (reinterpret_cast<uintptr_t>(lw) & 15) == 0) {
@@ -133,16 +133,16 @@ __global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, 
         const float4 *lw4 = reinterpret_cast<const float4 *>(lw);
         for (int64_t i = t0; i < n4; i += stride) {
             const float4 q = lw4[i];
-            acc.add((T)q.x);
-            acc.add((T)q.y);
-            acc.add((T)q.z);
-            acc.add((T)q.w);
+            ts.add((T)q.x);
+            ts.add((T)q.y);
+            ts.add((T)q.z);
+            ts.add((T)q.w);
         }
-        if (t0 < (n & 3)) acc.add(lw[(n4 << 2) + t0]);
+        if (t0 < (n & 3)) ts.add(lw[(n4 << 2) + t0]);
     } else {
-        for (int64_t i = t0; i < n; i += stride) acc.add(lw[i]);
+        for (int64_t i = t0; i < n; i += stride) ts.add(lw[i]);
     }
-    Moments3 v = block_merge3<T>(acc.result());
+    Moments3 v = block_merge3<T>(ts.result());
     __shared__ bool last;
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = v;
