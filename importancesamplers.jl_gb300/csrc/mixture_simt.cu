@@ -543,24 +543,27 @@ __global__ void __launch_bounds__(128) mixture_simt_kernel(MixParams<T> p) {
 
 // Fixed-slot draws from one factor component, x = mu + L (m z) with the
 // reference's summation order (mu first, then q = 0..r): the factor is staged
-// once per CTA (coalesced from its column-major storage), tiles of 128 normal
+// once per CTA in its own column-major order (column q holds L[., q], so the
+// entries of 4 consecutive rows are one 16-byte load), tiles of 128 normal
 // rows are staged through padded shared memory with coalesced loads, each
-// thread turns its row into a sample in place (rows r descending, so z[q <= r]
-// is still intact), and the tile is stored back coalesced.
+// thread holds its row of m z in registers and forms 4 rows of x at a time
+// (4 independent FMA chains), writing them back over the staged tile, which
+// is then stored coalesced.
 template <typename T, int D>
 __global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
-    constexpr int LD = D + 1;
+    constexpr int LC = D + 4;  // column stride of the staged factor (16-byte aligned columns)
+    constexpr int LZ = D + 4;  // row stride of the staged tile
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *Ls = reinterpret_cast<T *>(smem_raw);  // D x LD, row r = L[r, :]
-    T *mus = Ls + D * LD;
-    T *zt = mus + D;                           // 128 x LD
+    T *Lc = reinterpret_cast<T *>(smem_raw);  // D columns of LC
+    T *mus = Lc + D * LC;
+    T *zt = mus + D;                           // 128 x LZ
     const int d = p.d, k = p.fixed_slot, tid = threadIdx.x;
     const T *Lk = p.scales + (size_t)k * d * d;
-    for (int e = tid; e < d * d; e += blockDim.x) {
-        const int r = e % d, c = e / d;
-        Ls[r * LD + c] = Lk[e];
+    for (int e = tid; e < D * LC; e += blockDim.x) {
+        const int q = e / LC, r = e - q * LC;
+        Lc[e] = (q < d && r < d) ? Lk[(size_t)q * d + r] : T(0);
     }
-    for (int r = tid; r < d; r += blockDim.x) mus[r] = p.loc[(size_t)k * d + r];
+    for (int r = tid; r < D; r += blockDim.x) mus[r] = r < d ? p.loc[(size_t)k * d + r] : T(0);
     const T dof = p.family == ISSM_STUDENT_T ? p.dofs[k] : T(0);
     __syncthreads();
     const int64_t ntiles = (p.n + 127) / 128;
@@ -570,7 +573,7 @@ __global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
         const T *nz = p.normals + row0 * d;
         for (int e = tid; e < rows * d; e += blockDim.x) {
             const int r = e / d, c = e - r * d;
-            zt[r * LD + c] = nz[e];
+            zt[r * LZ + c] = nz[e];
         }
         __syncthreads();
         if (tid < rows) {
@@ -586,16 +589,27 @@ __global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
                     m = qnan<T>();
                 }
             }
-            T *z = zt + tid * LD;
-            if (m != T(1))
-                for (int q = 0; q < d; ++q) z[q] = z[q] * m;
+            T *zrow = zt + tid * LZ;
+            T z[D];
+#pragma unroll
+            for (int q = 0; q < D; ++q) z[q] = q < d ? zrow[q] * m : T(0);
             bool valid = true;
-            for (int r = d - 1; r >= 0; --r) {
-                T v = mus[r];
-                const T *Lr = Ls + r * LD;
-                for (int q = 0; q <= r; ++q) v += Lr[q] * z[q];
-                z[r] = v;
-                valid &= (bool)isfinite(v);
+#pragma unroll
+            for (int r0 = 0; r0 < D; r0 += 4) {
+                T v0 = mus[r0], v1 = mus[r0 + 1], v2 = mus[r0 + 2], v3 = mus[r0 + 3];
+#pragma unroll
+                for (int q = 0; q < r0 + 4; ++q) {
+                    const T *col = Lc + q * LC + r0;
+                    const T l0 = col[0], l1 = col[1], l2 = col[2], l3 = col[3];
+                    if (q <= r0) v0 += l0 * z[q];
+                    if (q <= r0 + 1) v1 += l1 * z[q];
+                    if (q <= r0 + 2) v2 += l2 * z[q];
+                    v3 += l3 * z[q];
+                }
+                if (r0 < d) { zrow[r0] = v0; valid &= (bool)isfinite(v0); }
+                if (r0 + 1 < d) { zrow[r0 + 1] = v1; valid &= (bool)isfinite(v1); }
+                if (r0 + 2 < d) { zrow[r0 + 2] = v2; valid &= (bool)isfinite(v2); }
+                if (r0 + 3 < d) { zrow[r0 + 3] = v3; valid &= (bool)isfinite(v3); }
             }
             if (!valid) record_failure(p.failures, p.index_base + i + 1, 0, ISSM_REASON_GENERATED_NONFINITE);
         }
@@ -603,7 +617,7 @@ __global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
         T *out = p.samples_out + row0 * d;
         for (int e = tid; e < rows * d; e += blockDim.x) {
             const int r = e / d, c = e - r * d;
-            out[e] = zt[r * LD + c];
+            out[e] = zt[r * LZ + c];
         }
         __syncthreads();
     }
@@ -612,7 +626,7 @@ __global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
 template <typename T, int D, bool FACTOR>
 static int launch_simt(MixParams<T> p, cudaStream_t stream) {
     if (FACTOR && p.mode == kModeDraw && p.slots == nullptr && p.samples_out != nullptr) {
-        const size_t smem = sizeof(T) * ((size_t)D * (D + 1) + D + (size_t)128 * (D + 1));
+        const size_t smem = sizeof(T) * ((size_t)D * (D + 4) + D + (size_t)128 * (D + 4));
         auto kern = draw_fixed_kernel<T, D>;
         if (smem > 48 * 1024) {
             const int e = allow_dynamic_smem((const void *)kern);
