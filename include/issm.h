@@ -194,14 +194,16 @@ int issm_mixture_logdensity(const issm_bank *bank, const issm_denominator *den,
  * (ISSM_PREC_TF32, ISSM_PREC_BF16 = bf16 split in three products) for
  * factor-Gaussian / factor-Student-t FP32 banks with d <= 64; NATIVE
  * precision runs the SIMT path and ignores the workspace. The workspace
- * holds the per-call inverse factors W_k = L_k^-1 (FP64-formed, stored FP32)
- * and the shift vectors; its last 64 bytes hold a sticky error word that a
- * timed-out tensor-core completion wait sets to 1 (zero the workspace once
- * when it is created). workspace_bytes >= issm_tc_workspace_bytes(K, d). */
+ * holds the per-call MMA operand forms [W_k | -W_k (mu_k - c)] of the slots
+ * (c = the centre slot's mean), the centre, and — when the bank carries no
+ * inverse_factors — the inverse factors formed for the call; its last 64
+ * bytes hold a sticky error word that a timed-out tensor-core completion
+ * wait sets to 1 (zero the workspace once when it is created).
+ * workspace_bytes >= issm_tc_workspace_bytes(K, d). */
 size_t issm_tc_workspace_bytes(int32_t k, int32_t d);
 /* W_k = L_k^-1 for factor slots [first, first + count) of an FP32 or FP64
- * factor bank, formed in FP64 and written as FP32 into out (K x DP x DP,
- * layout of issm_bank.inverse_factors). */
+ * factor bank, formed in FP32 by blocked triangular inversion and written
+ * into out (K x DP x DP, layout of issm_bank.inverse_factors). */
 int issm_invert_factors(const issm_bank *bank, int32_t first, int32_t count,
                         float *out, issm_stream_t stream);
 int issm_mixture_logdensity_ws(const issm_bank *bank, const issm_denominator *den,
