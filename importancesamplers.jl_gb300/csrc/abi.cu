@@ -450,12 +450,13 @@ int issm_target_logdensity(const issm_target *target, const void *x, int64_t n, 
 int issm_tc_selftest(const float *a, const float *b, float *c, int32_t n, int32_t k, int32_t kind,
                      int32_t *status, issm_stream_t stream) {
     if (!a || !b || !c || !status) return ISSM_E_NULL;
-    const int layout = (kind >> 8) & 1;
-    kind &= ~0x100;
+    const int layout = (kind >> 8) & 3;
+    kind &= ~0x300;
     if (kind != ISSM_PREC_BF16 && kind != ISSM_PREC_TF32) return ISSM_E_KIND;
+    if (layout >= 2 && kind != ISSM_PREC_BF16) return ISSM_E_UNSUPPORTED;  // MN-major: 16-bit types only
     if (n < 16 || n > 256 || n % 16 != 0) return ISSM_E_SIZE;
     const int kstep = kind == ISSM_PREC_BF16 ? 16 : 8;
-    if (k < kstep || k > 64 || k % kstep != 0) return ISSM_E_SIZE;
+    if (k < kstep || k > (layout >= 2 ? 128 : 64) || k % kstep != 0) return ISSM_E_SIZE;
     return tc_gemm_selftest(a, b, c, n, k, (kind == ISSM_PREC_BF16 ? 1 : 2) | (layout << 8), status,
                             (cudaStream_t)stream);
 }

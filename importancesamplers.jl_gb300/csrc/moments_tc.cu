@@ -1,42 +1,48 @@
 // moments_tc.cu — tensor-core form of the weighted moments that drive AMIS /
 // N-PMC adaptation (_weighted_moments!, src/adaptive_gaussian_execution.jl:268-273).
 //
-// One streaming pass over the retained samples. For a tile of samples the
-// operand is the 128 x K matrix A whose rows 0..d-1 hold sqrt(w) (x - c)
-// (c = previous proposal mean), row 64 holds sqrt(w), other rows zero; then
+// One streaming pass over the retained samples. For a tile of 128 samples the
+// operand A is 128 rows x 128 samples: rows 0..d-1 hold sqrt(w) (x - c)
+// (c = previous proposal mean), row 64 holds sqrt(w), other rows zero, with
+// the samples along K; then
 //   D[128 x 80] += A A[0:80]^T
-// accumulates S2 = sum w z z^T (rows/cols 0..63), S1 = sum w z (row 64 or
-// col 64) and S0 = sum w (D[64][64]) in FP32 tensor memory over all tiles of
-// the CTA. A and B are the same shared-memory tile (B = its first 80 rows).
-// Two tile buffers alternate so staging overlaps the previous tile's MMAs.
-// Per-CTA partials are summed in FP64 and mean = c + S1/S0,
-// cov = S2/S0 - (S1/S0)(S1/S0)^T.
+// accumulates S2 = sum w z z^T (rows/cols 0..63), S1 = sum w z (row 64) and
+// S0 = sum w (D[64][64]) in FP32 tensor memory over all tiles of the CTA.
+// A is stored MN-major: each sample's 8-coordinate groups are 16-byte chunks,
+// so a thread converts its own sample row straight from the staged tile and
+// no transpose is needed. Both tensor-core forms split A = hi + lo in bf16 and
+// accumulate Ah Ah^T + Al Ah^T + Ah Al^T (about 16 significant bits per
+// product). Sample tiles stream in with cp.async into padded stages two tiles
+// ahead; A is double-buffered so converting tile t+1 overlaps the MMAs of
+// tile t. Per-CTA partials are summed across CTAs (compensated FP32, FP64
+// across lanes) and mean = c + S1/S0, cov = S2/S0 - (S1/S0)(S1/S0)^T in FP64.
 #include "issm_device.cuh"
 #include "issm_internal.h"
 #include "tcgen05.cuh"
 
 namespace issm {
 
-constexpr int kMtThreads = 128;
-constexpr int kMtRows = 128;  // MMA M
-constexpr int kMtCols = 80;   // MMA N (64 dims + sqrt(w) + padding)
+constexpr int kMtThreads = 256;
+constexpr int kMtTile = 128;   // samples per tile = MMA K extent per tile
+constexpr int kMtCols = 80;    // MMA N (64 coordinates + sqrt(w) + padding)
+constexpr int kMtStages = 2;   // staged sample tiles in flight
+constexpr int kMtRS = 68;      // padded row of a staged tile (floats)
+constexpr int kMtRawBytes = kMtTile * kMtRS * 4 + kMtTile * 4;  // rows, then the tile's log weights
+constexpr int kMtPart = 16 * kMtTile * 16;                      // 16 row groups x 128 samples x 16 bytes
+constexpr size_t kMtSmem = (size_t)kMtStages * kMtRawBytes + (size_t)2 * 2 * kMtPart + 256;
 
-template <int KIND>
-__global__ void __launch_bounds__(kMtThreads) moments_tc_kernel(const float *__restrict__ x, int d, int64_t n,
-                                                                 const float *__restrict__ lw,
-                                                                 const double *__restrict__ summary,
-                                                                 const double *__restrict__ center,
-                                                                 float *__restrict__ partial, int *error) {
-    constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
-    constexpr int TS = KIND == tc::kBF16 ? 128 : 64;  // samples per tile = MMA K extent per tile
-    constexpr int PER = 16 / EB;
-    constexpr int KG = TS / PER;                       // 16 core groups per row (256 bytes)
-    constexpr int BUF = kMtRows * TS * EB;             // 32 KB
+__global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *__restrict__ x, int d, int64_t n,
+                                                                    const float *__restrict__ lw,
+                                                                    const double *__restrict__ summary,
+                                                                    const double *__restrict__ center,
+                                                                    float *__restrict__ partial, int *error) {
     extern __shared__ __align__(1024) unsigned char smem[];
+    unsigned char *s_raw = smem;
+    unsigned char *s_a = smem + (size_t)kMtStages * kMtRawBytes;  // [buf][part] x kMtPart
+    float *s_c = reinterpret_cast<float *>(s_a + (size_t)2 * 2 * kMtPart);
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
-    __shared__ float cshift[64];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) tc::tmem_alloc(&tmem_base, 128);
     if (tid == 0) {
@@ -45,103 +51,147 @@ __global__ void __launch_bounds__(kMtThreads) moments_tc_kernel(const float *__r
         tc::fence_mbar_init();
         abort_flag = 0;
     }
-    for (int c = tid; c < 64; c += kMtThreads) cshift[c] = c < d ? (float)center[c] : 0.f;
-    for (int e = tid; e < 2 * BUF / 16; e += kMtThreads) reinterpret_cast<uint4 *>(smem)[e] = make_uint4(0, 0, 0, 0);
+    for (int c = tid; c < 64; c += kMtThreads) s_c[c] = c < d ? (float)center[c] : 0.f;
+    // row groups 9..15 stay zero in every buffer and part
+    for (int e = tid; e < 2 * 2 * 7 * kMtTile; e += kMtThreads) {
+        const int k = e % kMtTile, g = 9 + (e / kMtTile) % 7, bp = e / (7 * kMtTile);
+        *reinterpret_cast<uint4 *>(s_a + (size_t)bp * kMtPart + (size_t)g * kMtTile * 16 + k * 16) =
+            make_uint4(0u, 0u, 0u, 0u);
+    }
     const float m = (float)summary[0];
-    const float inv = (float)(1.0 / summary[1]);
+    const float inv_sqrt_s = (float)(1.0 / sqrt(summary[1]));
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = tmem_base;
-    const int64_t ntiles = (n + TS - 1) / TS;
-    uint32_t uses[2] = {0u, 0u};
-    int it = 0, last_buf = -1;
-    const uint32_t idesc = tc::instr_desc(KIND, kMtRows, kMtCols);
-    // thread -> (sample column, dimension half): TF32 tiles have 64 samples, so
-    // two threads share a sample, each staging 32 dimensions
-    constexpr int HALVES = kMtThreads / TS;   // 1 (bf16) or 2 (tf32)
-    constexpr int DH = 64 / HALVES;           // dimensions per thread
-    const int col = tid % TS, half = tid / TS, j0 = half * DH;
-    const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0);
-    float xr[DH];
-    float lr = -INFINITY;
-    auto load_col = [&](int64_t tile) {
-        const int64_t i = tile * TS + col;
-#pragma unroll
-        for (int c = 0; c < DH; ++c) xr[c] = 0.f;
-        lr = -INFINITY;
-        if (tile < ntiles && i < n) {
-            lr = __ldg(lw + i);
-            const float *xi = x + i * d + j0;
+    const int64_t ntiles = (n + kMtTile - 1) / kMtTile;
+    const int my_tiles = (int)((ntiles - (int64_t)blockIdx.x + gridDim.x - 1) / gridDim.x);
+    const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0) &&
+                     ((reinterpret_cast<uintptr_t>(lw) & 15) == 0);
+    auto tile_of = [&](int it) -> int64_t { return (int64_t)blockIdx.x + (int64_t)it * gridDim.x; };
+
+    auto issue_raw = [&](int it) {
+        if (it < my_tiles) {
+            const int64_t row0 = tile_of(it) * kMtTile;
+            const int rows = (int)min((int64_t)kMtTile, n - row0);
+            float *dst = reinterpret_cast<float *>(s_raw + (size_t)(it % kMtStages) * kMtRawBytes);
+            float *dlw = dst + kMtTile * kMtRS;
+            const float *src = x + row0 * d;
             if (vec) {
-#pragma unroll
-                for (int c = 0; c < DH; c += 4)
-                    if (j0 + c < d) {
-                        const float4 q = __ldg(reinterpret_cast<const float4 *>(xi + c));
-                        xr[c] = q.x; xr[c + 1] = q.y; xr[c + 2] = q.z; xr[c + 3] = q.w;
-                    }
+                const int q4 = d >> 2, total = rows * q4;
+                for (int e = tid; e < total; e += kMtThreads) {
+                    const int r = e / q4, c4 = e - r * q4;
+                    tc::cp_async16(dst + r * kMtRS + c4 * 4, src + (size_t)e * 4);
+                }
+                if (rows == kMtTile) {
+                    if (tid < kMtTile / 4) tc::cp_async16(dlw + tid * 4, lw + row0 + tid * 4);
+                } else {
+                    for (int r = tid; r < rows; r += kMtThreads) tc::cp_async4(dlw + r, lw + row0 + r);
+                }
             } else {
-#pragma unroll
-                for (int c = 0; c < DH; ++c)
-                    if (j0 + c < d) xr[c] = __ldg(xi + c);
+                for (int e = tid; e < rows * d; e += kMtThreads) {
+                    const int r = e / d, c = e - r * d;
+                    tc::cp_async4(dst + r * kMtRS + c, src + (size_t)r * d + c);
+                }
+                for (int r = tid; r < rows; r += kMtThreads) tc::cp_async4(dlw + r, lw + row0 + r);
             }
+        }
+        tc::cp_async_commit();
+    };
+
+    // thread -> (sample k, coordinate half): 4 groups of 8 coordinates each
+    auto convert = [&](int it) {
+        const float *raw = reinterpret_cast<const float *>(s_raw + (size_t)(it % kMtStages) * kMtRawBytes);
+        unsigned char *ah = s_a + (size_t)(it & 1) * 2 * kMtPart;
+        unsigned char *al = ah + kMtPart;
+        const int k = tid & (kMtTile - 1), half = tid >> 7;
+        const int64_t i = tile_of(it) * kMtTile + k;
+        const bool active = i < n;
+        const float l = active ? raw[kMtTile * kMtRS + k] : -INFINITY;
+        const float sw = l == -INFINITY ? 0.f : expf(0.5f * (l - m)) * inv_sqrt_s;
+#pragma unroll
+        for (int gg = 0; gg < 4; ++gg) {
+            const int g = half * 4 + gg, c = g * 8;
+            float v[8];
+            float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f), f1 = f0;
+            if (active) {
+                f0 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c);
+                f1 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c + 4);
+            }
+            const float4 c0 = *reinterpret_cast<const float4 *>(s_c + c), c1 = *reinterpret_cast<const float4 *>(s_c + c + 4);
+            v[0] = (active && c < d) ? sw * (f0.x - c0.x) : 0.f;
+            v[1] = (active && c + 1 < d) ? sw * (f0.y - c0.y) : 0.f;
+            v[2] = (active && c + 2 < d) ? sw * (f0.z - c0.z) : 0.f;
+            v[3] = (active && c + 3 < d) ? sw * (f0.w - c0.w) : 0.f;
+            v[4] = (active && c + 4 < d) ? sw * (f1.x - c1.x) : 0.f;
+            v[5] = (active && c + 5 < d) ? sw * (f1.y - c1.y) : 0.f;
+            v[6] = (active && c + 6 < d) ? sw * (f1.z - c1.z) : 0.f;
+            v[7] = (active && c + 7 < d) ? sw * (f1.w - c1.w) : 0.f;
+            const uint4 hi = make_uint4(tc::pack_bf16x2(v[0], v[1]), tc::pack_bf16x2(v[2], v[3]),
+                                        tc::pack_bf16x2(v[4], v[5]), tc::pack_bf16x2(v[6], v[7]));
+            auto lo2 = [](float a, float b, uint32_t h) {
+                return tc::pack_bf16x2(a - __uint_as_float(h << 16), b - __uint_as_float(h & 0xffff0000u));
+            };
+            const uint4 lo = make_uint4(lo2(v[0], v[1], hi.x), lo2(v[2], v[3], hi.y), lo2(v[4], v[5], hi.z),
+                                        lo2(v[6], v[7], hi.w));
+            *reinterpret_cast<uint4 *>(ah + (size_t)g * kMtTile * 16 + k * 16) = hi;
+            *reinterpret_cast<uint4 *>(al + (size_t)g * kMtTile * 16 + k * 16) = lo;
+        }
+        if (half == 1) {
+            // row group 8: sqrt(w) in row 64
+            const uint32_t h = tc::pack_bf16x2(sw, 0.f);
+            const uint32_t lo = tc::pack_bf16x2(sw - __uint_as_float(h << 16), 0.f);
+            *reinterpret_cast<uint4 *>(ah + (size_t)8 * kMtTile * 16 + k * 16) = make_uint4(h, 0u, 0u, 0u);
+            *reinterpret_cast<uint4 *>(al + (size_t)8 * kMtTile * 16 + k * 16) = make_uint4(lo, 0u, 0u, 0u);
         }
     };
-    load_col(blockIdx.x);
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+
+    const uint32_t idesc = tc::instr_desc(tc::kBF16, 128, kMtCols) | tc::kMajorMN;
+    constexpr uint32_t LBO = kMtTile * 16, SBO = 128;  // MN row-group stride, K group stride
+    uint32_t uses[2] = {0u, 0u};
+    int last_buf = -1;
+    for (int s = 0; s < kMtStages; ++s) issue_raw(s);
+    for (int it = 0; it < my_tiles; ++it) {
         const int buf = it & 1;
-        if (it >= 2) {
-            if (tid == 0 && !tc::mbar_wait(&bar[buf], (uses[buf] - 1) & 1)) {
-                atomicExch(error, 1);
-                abort_flag = 1;
-            }
-            tc::fence_before_sync();
-            __syncthreads();
-            tc::fence_after_sync();
-            if (abort_flag) break;
+        tc::cp_async_wait<kMtStages - 1>();
+        bool ok = true;
+        if (it >= 2 && !tc::mbar_wait(&bar[buf], (uses[buf] - 1) & 1)) ok = false;
+        if (!ok) {
+            atomicExch(error, 1);
+            abort_flag = 1;
         }
-        unsigned char *sa = smem + buf * BUF;
-        // ---- stage this thread's (sample, dimension-half) of the tile ----
-        {
-            const float sw = lr == -INFINITY ? 0.f : sqrtf(expf(lr - m) * inv);
-            float z[DH];
-#pragma unroll
-            for (int c = 0; c < DH; ++c) z[c] = (j0 + c < d) ? sw * (xr[c] - cshift[j0 + c]) : 0.f;
-            load_col(tile + gridDim.x);  // next tile's column is in flight during the stores and MMAs
-            const int kq = col / PER, kr = col % PER;
-#pragma unroll
-            for (int jj = 0; jj <= DH; ++jj) {
-                if (jj == DH && half != HALVES - 1) break;
-                const int j = jj < DH ? j0 + jj : 64;
-                const float v = jj < DH ? z[jj] : sw;
-                const uint32_t off = (uint32_t)((((j >> 3) * KG + kq) << 7) + ((j & 7) << 4) + kr * EB);
-                if (EB == 2) *reinterpret_cast<uint16_t *>(sa + off) = tc::bf16_bits(v);
-                else *reinterpret_cast<float *>(sa + off) = v;
-            }
-        }
-        tc::fence_proxy_async();
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
+        if (abort_flag) break;
+        convert(it);
+        tc::fence_proxy_async();
+        __syncthreads();
+        issue_raw(it + kMtStages);
         if (tid == 0) {
-            const uint32_t a0 = tc::smem_u32(sa);
-            for (int s = 0; s < TS * EB / 32; ++s) {
-                const uint64_t da = tc::smem_desc(a0 + s * 256, 128, KG * 128);
-                if (KIND == tc::kTF32) tc::mma_tf32(tbase, da, da, idesc, it > 0 || s > 0);
-                else tc::mma(tbase, da, da, idesc, it > 0 || s > 0);
+            tc::fence_after_sync();
+            const uint32_t a0 = tc::smem_u32(s_a + (size_t)buf * 2 * kMtPart), a1 = a0 + kMtPart;
+#pragma unroll
+            for (int s = 0; s < kMtTile / 16; ++s) {
+                const uint64_t dh = tc::smem_desc(a0 + s * 256, LBO, SBO);
+                const uint64_t dl = tc::smem_desc(a1 + s * 256, LBO, SBO);
+                tc::mma(tbase, dh, dh, idesc, it > 0 || s > 0);
+                tc::mma(tbase, dl, dh, idesc, true);
+                tc::mma(tbase, dh, dl, idesc, true);
             }
             tc::commit(&bar[buf]);
         }
         uses[buf] += 1;
         last_buf = buf;
     }
-    // ---- wait for the last MMA group (commits track every earlier MMA) ----
+    // ---- the last commit tracks every earlier MMA ----
     if (last_buf >= 0 && !abort_flag) {
-        if (tid == 0 && !tc::mbar_wait(&bar[last_buf], (uses[last_buf] - 1) & 1)) {
+        if (!tc::mbar_wait(&bar[last_buf], (uses[last_buf] - 1) & 1)) {
             atomicExch(error, 1);
             abort_flag = 1;
         }
     }
+    tc::cp_async_wait_all();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -161,6 +211,11 @@ __global__ void __launch_bounds__(kMtThreads) moments_tc_kernel(const float *__r
             }
         }
     }
+    // an aborted CTA still owes its earlier MMAs a completed wait before TMEM is freed
+    if (abort_flag && tid == 0) {
+        for (int b = 0; b < 2; ++b)
+            if (uses[b] > 0) tc::mbar_wait(&bar[b], (uses[b] - 1) & 1);
+    }
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tbase, 128);
@@ -173,9 +228,16 @@ __global__ void moments_tc_reduce_kernel(const float *__restrict__ partial, int 
     __shared__ double acc_s[8][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int e = blockIdx.x * 32 + tx;
-    double acc = 0.0;
+    // compensated FP32 over this lane's blocks (no serial FP64 chain), FP64 across lanes
+    float s = 0.f, cmp = 0.f;
     if (e < 65 * kMtCols)
-        for (int b = ty; b < blocks; b += 8) acc += (double)partial[(size_t)b * 65 * kMtCols + e];
+        for (int b = ty; b < blocks; b += 8) {
+            const float y = partial[(size_t)b * 65 * kMtCols + e] - cmp;
+            const float t = s + y;
+            cmp = (t - s) - y;
+            s = t;
+        }
+    const double acc = (double)s - (double)cmp;
     acc_s[ty][tx] = acc;
     __syncthreads();
     if (ty == 0 && e < 65 * kMtCols) {
@@ -187,48 +249,37 @@ __global__ void moments_tc_reduce_kernel(const float *__restrict__ partial, int 
 
 __global__ void moments_tc_finish_kernel(const double *__restrict__ sums, int d, const double *__restrict__ center,
                                          double *__restrict__ mean, double *__restrict__ cov) {
-    const double s0 = sums[64 * kMtCols + 64];
-    for (int j = threadIdx.x; j < d; j += blockDim.x) mean[j] = center[j] + sums[64 * kMtCols + j] / s0;
+    const double inv = 1.0 / sums[64 * kMtCols + 64];
+    if (blockIdx.x == 0)
+        for (int j = threadIdx.x; j < d; j += blockDim.x) mean[j] = center[j] + sums[64 * kMtCols + j] * inv;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d * d; e += gridDim.x * blockDim.x) {
         const int r = e % d, c = e / d;
-        const double mr = sums[64 * kMtCols + r] / s0, mc = sums[64 * kMtCols + c] / s0;
-        cov[e] = sums[r * kMtCols + c] / s0 - mr * mc;
+        const double mr = sums[64 * kMtCols + r] * inv, mc = sums[64 * kMtCols + c] * inv;
+        cov[e] = sums[r * kMtCols + c] * inv - mr * mc;
     }
 }
 
-static int moments_tc_blocks(int64_t n, int ts) {
-    int64_t t = (n + ts - 1) / ts;
-    int64_t b = kSMs * 2;
-    return (int)(t < b ? (t < 1 ? 1 : t) : b);
+static int moments_tc_blocks(int64_t n) {
+    const int64_t t = (n + kMtTile - 1) / kMtTile;
+    return (int)(t < kSMs ? (t < 1 ? 1 : t) : kSMs);
 }
 
 size_t moments_tc_workspace_bytes(int64_t n) {
-    return sizeof(float) * (size_t)moments_tc_blocks(n, 64) * 65 * kMtCols + sizeof(double) * 65 * kMtCols + 128;
+    return sizeof(float) * (size_t)kSMs * 65 * kMtCols + sizeof(double) * 65 * kMtCols + 128;
 }
 
 int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *summary, const double *shift,
                double *mean, double *cov, int precision, void *ws, size_t ws_bytes, int *error, cudaStream_t stream) {
+    (void)precision;  // both tensor-core forms use the bf16 x3 contraction
     if (d > 64) return ISSM_E_UNSUPPORTED;
     if (ws_bytes < moments_tc_workspace_bytes(n)) return ISSM_E_WORKSPACE;
-    const bool bf16 = precision == ISSM_PREC_BF16;
-    const int ts = bf16 ? 128 : 64;
-    const int blocks = moments_tc_blocks(n, ts);
-    const size_t smem = 2 * (size_t)kMtRows * ts * (bf16 ? 2 : 4);
+    const int blocks = moments_tc_blocks(n);
     float *partial = (float *)ws;
-    if (bf16) {
-        auto kern = moments_tc_kernel<tc::kBF16>;
-        const int e = allow_dynamic_smem((const void *)kern);
-        if (e) return e;
-        { kern<<<blocks, kMtThreads, smem, stream>>>((const float *)x, d, n, (const float *)lw, summary, shift,
-                                                     partial, error); note_launch(); }
-    } else {
-        auto kern = moments_tc_kernel<tc::kTF32>;
-        const int e = allow_dynamic_smem((const void *)kern);
-        if (e) return e;
-        { kern<<<blocks, kMtThreads, smem, stream>>>((const float *)x, d, n, (const float *)lw, summary, shift,
-                                                     partial, error); note_launch(); }
-    }
-    double *sums = reinterpret_cast<double *>(partial + (size_t)moments_tc_blocks(n, 64) * 65 * kMtCols);
+    const int e = allow_dynamic_smem((const void *)moments_tc_kernel);
+    if (e) return e;
+    { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw, summary,
+                                                                shift, partial, error); note_launch(); }
+    double *sums = reinterpret_cast<double *>(partial + (size_t)kSMs * 65 * kMtCols);
     { moments_tc_reduce_kernel<<<(65 * kMtCols + 31) / 32, 256, 0, stream>>>(partial, blocks, sums); note_launch(); }
     { moments_tc_finish_kernel<<<(d * d + 255) / 256, 256, 0, stream>>>(sums, d, shift, mean, cov); note_launch(); }
     return (int)cudaGetLastError();

@@ -8,8 +8,12 @@
 
 namespace issm {
 
-// layout 0: core matrices K-group-major within 8-row groups (tc::kmajor_offset);
-// layout 1: row-contiguous per K group (tc::rowgroup_offset).
+// layout 0: K-major, core matrices K-group-major within 8-row groups (tc::kmajor_offset);
+// layout 1: K-major, row-contiguous per K group (tc::rowgroup_offset);
+// layouts 2 and 3: MN-major (bf16 only): for each group of 8 rows (M or N)
+// the K elements are stored consecutively, 16 bytes (8 rows) each
+// (tc::mn_offset); layout 2 passes the row-group stride as the leading and
+// 128 bytes as the stride byte offset, layout 3 the other way round.
 __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__restrict__ A, const float *__restrict__ B,
                                                                float *__restrict__ C, int n, int k, int kind,
                                                                int layout, int *status) {
@@ -28,13 +32,15 @@ __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__re
     }
     for (int e = threadIdx.x; e < 128 * k; e += blockDim.x) {
         const int r = e / k, c = e % k;
-        const uint32_t off = layout ? tc::rowgroup_offset(r, c, 128, eb) : tc::kmajor_offset(r, c, kg, eb);
+        const uint32_t off = layout >= 2 ? tc::mn_offset(r, c, k) : layout ? tc::rowgroup_offset(r, c, 128, eb)
+                                                                          : tc::kmajor_offset(r, c, kg, eb);
         if (eb == 2) *reinterpret_cast<uint16_t *>(sa + off) = tc::bf16_bits(A[e]);
         else *reinterpret_cast<float *>(sa + off) = A[e];
     }
     for (int e = threadIdx.x; e < n * k; e += blockDim.x) {
         const int r = e / k, c = e % k;
-        const uint32_t off = layout ? tc::rowgroup_offset(r, c, n, eb) : tc::kmajor_offset(r, c, kg, eb);
+        const uint32_t off = layout >= 2 ? tc::mn_offset(r, c, k) : layout ? tc::rowgroup_offset(r, c, n, eb)
+                                                                          : tc::kmajor_offset(r, c, kg, eb);
         if (eb == 2) *reinterpret_cast<uint16_t *>(sb + off) = tc::bf16_bits(B[e]);
         else *reinterpret_cast<float *>(sb + off) = B[e];
     }
@@ -44,13 +50,22 @@ __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__re
     tc::fence_after_sync();
     const uint32_t tbase = tmem_base;
     if (threadIdx.x == 0) {
-        const uint32_t idesc = tc::instr_desc(kind, 128, n);
+        const uint32_t idesc = tc::instr_desc(kind, 128, n) | (layout >= 2 ? tc::kMajorMN : 0u);
         const int steps = k * eb / 32;
         for (int s = 0; s < steps; ++s) {
-            const uint64_t da = layout ? tc::smem_desc(tc::smem_u32(sa) + s * 2 * 128 * 16, 128 * 16, 128)
-                                       : tc::smem_desc(tc::smem_u32(sa) + s * 256, 128, kg * 128);
-            const uint64_t db = layout ? tc::smem_desc(tc::smem_u32(sb) + s * 2 * n * 16, n * 16, 128)
-                                       : tc::smem_desc(tc::smem_u32(sb) + s * 256, 128, kg * 128);
+            uint64_t da, db;
+            if (layout >= 2) {
+                // one K slice (16 bf16) = two 8-element K groups of 128 bytes
+                const uint32_t mn = (uint32_t)k * 16, lbo = layout == 2 ? mn : 128u, sbo = layout == 2 ? 128u : mn;
+                da = tc::smem_desc(tc::smem_u32(sa) + s * 256, lbo, sbo);
+                db = tc::smem_desc(tc::smem_u32(sb) + s * 256, lbo, sbo);
+            } else if (layout == 1) {
+                da = tc::smem_desc(tc::smem_u32(sa) + s * 2 * 128 * 16, 128 * 16, 128);
+                db = tc::smem_desc(tc::smem_u32(sb) + s * 2 * n * 16, n * 16, 128);
+            } else {
+                da = tc::smem_desc(tc::smem_u32(sa) + s * 256, 128, kg * 128);
+                db = tc::smem_desc(tc::smem_u32(sb) + s * 256, 128, kg * 128);
+            }
             if (kind == tc::kBF16) tc::mma(tbase, da, db, idesc, s > 0);
             else tc::mma_tf32(tbase, da, db, idesc, s > 0);
         }
@@ -76,10 +91,12 @@ __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__re
 
 int tc_gemm_selftest(const float *a, const float *b, float *c, int n, int k, int kind, int *status,
                      cudaStream_t stream) {
-    const int layout = (kind >> 8) & 1;
+    const int layout = (kind >> 8) & 3;
     kind &= 0xff;
     const int eb = kind == tc::kBF16 ? 2 : 4;
-    const size_t smem = (size_t)(128 + n) * k * eb;
+    // MN-major runs keep 32 KB of slack after B, so that either stride
+    // assignment reads inside this CTA's allocation
+    const size_t smem = (size_t)(128 + n) * k * eb + (layout >= 2 ? 32768 : 0);
     auto kern = tc_gemm_selftest_kernel;
     if (smem > 48 * 1024) {
         const int e = allow_dynamic_smem((const void *)kern);

@@ -41,6 +41,14 @@ __device__ __forceinline__ uint32_t rowgroup_offset(int row, int k, int rows, in
     return (uint32_t)((k / per) * rows * 16 + row * 16 + (k % per) * elem_bytes);
 }
 
+// MN-major (16-bit elements): element (row, k) of a tile with K extent
+// `kext`; each group of 8 rows stores its K elements consecutively, 16 bytes
+// (the 8 rows) per K index, so one sample's 8 coordinates form one 16-byte
+// chunk and 8 consecutive K indices form one 128-byte core matrix.
+__device__ __forceinline__ uint32_t mn_offset(int row, int k, int kext) {
+    return (uint32_t)((row >> 3) * kext * 16 + k * 16 + (row & 7) * 2);
+}
+
 // 64-bit shared-memory matrix descriptor (version 1, no swizzle).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes, uint32_t sbo_bytes) {
     uint64_t d = 0;
@@ -53,6 +61,8 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes
 }
 
 enum Kind { kBF16 = 1, kTF32 = 2 };
+// instruction-descriptor bits: A and B MN-major ("transposed") instead of K-major
+constexpr uint32_t kMajorMN = (1u << 15) | (1u << 16);
 
 // Instruction descriptor: D = F32, A/B format, both K-major, N >> 3, M >> 4.
 __host__ __device__ constexpr uint32_t instr_desc(int fmt, int m, int n) {

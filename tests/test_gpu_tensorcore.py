@@ -11,6 +11,17 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("kind", ["bf16", "tf32"])
 @pytest.mark.parametrize("n,k", [(16, 16), (64, 32), (80, 64), (128, 48), (192, 64), (256, 64)])
 def test_tc_gemm_selftest_exact(issm, cuda, kind, n, k, layout):
+    _selftest(issm, cuda, kind, n, k, layout)
+
+
+@pytest.mark.parametrize("n,k", [(16, 16), (80, 64), (80, 128), (256, 48)])
+def test_tc_gemm_selftest_mn_major(issm, cuda, n, k):
+    """MN-major bf16 staging (the weighted-moments kernel's layout) with the
+    row-group stride as the leading byte offset."""
+    _selftest(issm, cuda, "bf16", n, k, 2)
+
+
+def _selftest(issm, cuda, kind, n, k, layout):
     prec = (issm.native.PREC_BF16 if kind == "bf16" else issm.native.PREC_TF32) | (layout << 8)
     g = torch.Generator(device=cuda).manual_seed(n * 131 + k)
     a = torch.randint(-4, 5, (128, k), generator=g, device=cuda).float()
@@ -119,7 +130,9 @@ def test_tc_moments_vs_oracle(issm, orc, cuda, prec, d, n):
     issm.ops.check_tensor_core_errors(cuda)
     em, ec, _ = orc.weighted_moments(X.astype(np.float64).reshape(-1), d, lw.astype(np.float64))
     scale = np.sqrt(np.outer(np.diag(ec), np.diag(ec)))
-    tol = 2e-3 if prec == "tf32" else 1e-2
+    # both forms contract bf16 x3 splits (about 16 bits per product) with FP32
+    # accumulation in tensor memory
+    tol = 2e-4
     assert np.max(np.abs(mean.cpu().numpy() - em) / np.sqrt(np.diag(ec))) < tol
     assert np.max(np.abs(cov.cpu().numpy() - ec) / scale) < tol
 
