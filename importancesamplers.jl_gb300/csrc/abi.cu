@@ -453,7 +453,8 @@ int issm_tc_selftest(const float *a, const float *b, float *c, int32_t n, int32_
     const int layout = (kind >> 8) & 3;
     kind &= ~0x300;
     if (kind != ISSM_PREC_BF16 && kind != ISSM_PREC_TF32) return ISSM_E_KIND;
-    if (layout >= 2 && kind != ISSM_PREC_BF16) return ISSM_E_UNSUPPORTED;  // MN-major: 16-bit types only
+    if (layout == 3) return ISSM_E_KIND;
+    if (layout == 2 && kind != ISSM_PREC_BF16) return ISSM_E_UNSUPPORTED;  // MN-major: 16-bit types only
     if (n < 16 || n > 256 || n % 16 != 0) return ISSM_E_SIZE;
     const int kstep = kind == ISSM_PREC_BF16 ? 16 : 8;
     if (k < kstep || k > (layout >= 2 ? 128 : 64) || k % kstep != 0) return ISSM_E_SIZE;

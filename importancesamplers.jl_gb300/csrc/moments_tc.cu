@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
     };
 
     const uint32_t idesc = tc::instr_desc(tc::kBF16, 128, kMtCols) | tc::kMajorMN;
-    constexpr uint32_t LBO = kMtTile * 16, SBO = 128;  // MN row-group stride, K group stride
+    constexpr uint32_t LBO = 128, SBO = kMtTile * 16;  // K-group stride, row-group stride
     uint32_t uses[2] = {0u, 0u};
     int last_buf = -1;
     for (int s = 0; s < kMtStages; ++s) issue_raw(s);

@@ -10,10 +10,10 @@ namespace issm {
 
 // layout 0: K-major, core matrices K-group-major within 8-row groups (tc::kmajor_offset);
 // layout 1: K-major, row-contiguous per K group (tc::rowgroup_offset);
-// layouts 2 and 3: MN-major (bf16 only): for each group of 8 rows (M or N)
-// the K elements are stored consecutively, 16 bytes (8 rows) each
-// (tc::mn_offset); layout 2 passes the row-group stride as the leading and
-// 128 bytes as the stride byte offset, layout 3 the other way round.
+// layout 2: MN-major (bf16 only): for each group of 8 rows (M or N) the K
+// elements are stored consecutively, 16 bytes (8 rows) each (tc::mn_offset);
+// the leading byte offset is the K-group stride (128 bytes) and the stride
+// byte offset the row-group stride, as for the K-major layouts.
 __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__restrict__ A, const float *__restrict__ B,
                                                                float *__restrict__ C, int n, int k, int kind,
                                                                int layout, int *status) {
@@ -56,9 +56,8 @@ __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__re
             uint64_t da, db;
             if (layout >= 2) {
                 // one K slice (16 bf16) = two 8-element K groups of 128 bytes
-                const uint32_t mn = (uint32_t)k * 16, lbo = layout == 2 ? mn : 128u, sbo = layout == 2 ? 128u : mn;
-                da = tc::smem_desc(tc::smem_u32(sa) + s * 256, lbo, sbo);
-                db = tc::smem_desc(tc::smem_u32(sb) + s * 256, lbo, sbo);
+                da = tc::smem_desc(tc::smem_u32(sa) + s * 256, 128, (uint32_t)k * 16);
+                db = tc::smem_desc(tc::smem_u32(sb) + s * 256, 128, (uint32_t)k * 16);
             } else if (layout == 1) {
                 da = tc::smem_desc(tc::smem_u32(sa) + s * 2 * 128 * 16, 128 * 16, 128);
                 db = tc::smem_desc(tc::smem_u32(sb) + s * 2 * n * 16, n * 16, 128);
@@ -92,11 +91,10 @@ __global__ void __launch_bounds__(128) tc_gemm_selftest_kernel(const float *__re
 int tc_gemm_selftest(const float *a, const float *b, float *c, int n, int k, int kind, int *status,
                      cudaStream_t stream) {
     const int layout = (kind >> 8) & 3;
+    if (layout == 3) return ISSM_E_KIND;
     kind &= 0xff;
     const int eb = kind == tc::kBF16 ? 2 : 4;
-    // MN-major runs keep 32 KB of slack after B, so that either stride
-    // assignment reads inside this CTA's allocation
-    const size_t smem = (size_t)(128 + n) * k * eb + (layout >= 2 ? 32768 : 0);
+    const size_t smem = (size_t)(128 + n) * k * eb;
     auto kern = tc_gemm_selftest_kernel;
     if (smem > 48 * 1024) {
         const int e = allow_dynamic_smem((const void *)kern);

@@ -418,10 +418,9 @@ int issm_target_logdensity(const issm_target *target, const void *x, int64_t n,
  * the tensor-core kernels. n in {16, 32, ..., 256}; k a multiple of 16 (bf16)
  * or 8 (tf32), k <= 64 (k <= 128 MN-major). kind | 0x100 stages both operands in the
  * row-contiguous layout (each 16-byte K group holds the rows consecutively)
- * instead of 8-row core-matrix blocks; kind | 0x200 and kind | 0x300 (bf16
- * only) stage them MN-major (8 rows of one K index per 16 bytes) with the
- * two assignments of the leading / stride byte offsets. *status (device
- * int, zeroed by the caller) becomes 1 if the MMA completion wait timed out. */
+ * instead of 8-row core-matrix blocks; kind | 0x200 (bf16 only) stages them
+ * MN-major (8 rows of one K index per 16 bytes). *status (device int,
+ * zeroed by the caller) becomes 1 if the MMA completion wait timed out. */
 int issm_tc_selftest(const float *a, const float *b, float *c, int32_t n,
                      int32_t k, int32_t kind, int32_t *status,
                      issm_stream_t stream);

@@ -16,8 +16,8 @@ def test_tc_gemm_selftest_exact(issm, cuda, kind, n, k, layout):
 
 @pytest.mark.parametrize("n,k", [(16, 16), (80, 64), (80, 128), (256, 48)])
 def test_tc_gemm_selftest_mn_major(issm, cuda, n, k):
-    """MN-major bf16 staging (the weighted-moments kernel's layout) with the
-    row-group stride as the leading byte offset."""
+    """MN-major bf16 staging (the weighted-moments kernel's layout): leading
+    byte offset = K-group stride, stride byte offset = row-group stride."""
     _selftest(issm, cuda, "bf16", n, k, 2)
 
 
