@@ -14,6 +14,7 @@
 // reference's exponent-extended solves (src/student_t_range.jl:82-153).
 #include "issm_device.cuh"
 #include "issm_internal.h"
+#include "tcgen05.cuh"
 
 namespace issm {
 
@@ -565,15 +566,30 @@ __global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
     }
     for (int r = tid; r < D; r += blockDim.x) mus[r] = r < d ? p.loc[(size_t)k * d + r] : T(0);
     const T dof = p.family == ISSM_STUDENT_T ? p.dofs[k] : T(0);
+    // rows of whole 16-byte vectors, both buffers 16-byte aligned
+    const bool vec = (d * sizeof(T)) % 16 == 0 && (reinterpret_cast<uintptr_t>(p.normals) & 15) == 0 &&
+                     (reinterpret_cast<uintptr_t>(p.samples_out) & 15) == 0;
     __syncthreads();
     const int64_t ntiles = (p.n + 127) / 128;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t row0 = tile * 128;
         const int rows = (int)min((int64_t)128, p.n - row0);
         const T *nz = p.normals + row0 * d;
-        for (int e = tid; e < rows * d; e += blockDim.x) {
-            const int r = e / d, c = e - r * d;
-            zt[r * LZ + c] = nz[e];
+        if (vec) {
+            // 16-byte asynchronous copies, all of the tile in flight at once
+            constexpr int V = 16 / sizeof(T);
+            const int dv = d / V;
+            for (int e = tid; e < rows * dv; e += blockDim.x) {
+                const int r = e / dv, c = e - r * dv;
+                tc::cp_async16(zt + r * LZ + c * V, nz + (size_t)e * V);
+            }
+            tc::cp_async_commit();
+            tc::cp_async_wait<0>();
+        } else {
+            for (int e = tid; e < rows * d; e += blockDim.x) {
+                const int r = e / d, c = e - r * d;
+                zt[r * LZ + c] = nz[e];
+            }
         }
         __syncthreads();
         if (tid < rows) {
@@ -615,9 +631,18 @@ __global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
         }
         __syncthreads();
         T *out = p.samples_out + row0 * d;
-        for (int e = tid; e < rows * d; e += blockDim.x) {
-            const int r = e / d, c = e - r * d;
-            out[e] = zt[r * LZ + c];
+        if (vec) {
+            constexpr int V = 16 / sizeof(T);
+            const int dv = d / V;
+            for (int e = tid; e < rows * dv; e += blockDim.x) {
+                const int r = e / dv, c = e - r * dv;
+                *reinterpret_cast<uint4 *>(out + (size_t)e * V) = *reinterpret_cast<const uint4 *>(zt + r * LZ + c * V);
+            }
+        } else {
+            for (int e = tid; e < rows * d; e += blockDim.x) {
+                const int r = e / d, c = e - r * d;
+                out[e] = zt[r * LZ + c];
+            }
         }
         __syncthreads();
     }

@@ -25,21 +25,28 @@ namespace issm {
 constexpr int kMtThreads = 256;
 constexpr int kMtTile = 128;   // samples per tile = MMA K extent per tile
 constexpr int kMtCols = 80;    // MMA N (64 coordinates + sqrt(w) + padding)
-constexpr int kMtStages = 2;   // staged sample tiles in flight
+constexpr int kMtStages = 1;   // staged sample tiles in flight (two CTAs per SM interleave)
 constexpr int kMtRS = 68;      // padded row of a staged tile (floats)
 constexpr int kMtRawBytes = kMtTile * kMtRS * 4 + kMtTile * 4;  // rows, then the tile's log weights
-constexpr int kMtPart = 16 * kMtTile * 16;                      // 16 row groups x 128 samples x 16 bytes
-constexpr size_t kMtSmem = (size_t)kMtStages * kMtRawBytes + (size_t)2 * 2 * kMtPart + 256;
+// Rows 0..71 (9 row groups: 64 coordinates, sqrt(w), zeros) are stored; the
+// MMA's M = 128 also reads row groups 9..15, which land in the next buffer or
+// the staged tile after A: those D rows and the matching columns >= 72 are
+// never read, so their content does not matter.
+constexpr int kMtGroups = 9;
+constexpr int kMtPart = kMtGroups * kMtTile * 16;
+constexpr size_t kMtSmem = (size_t)2 * 2 * kMtPart + (size_t)kMtStages * kMtRawBytes + 256;
+constexpr int kMtCtasPerSm = 2;
+static_assert((size_t)3 * kMtPart + (size_t)16 * kMtTile * 16 <= kMtSmem, "M = 128 reads stay inside the CTA's shared memory");
 
-__global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *__restrict__ x, int d, int64_t n,
+__global__ void __launch_bounds__(kMtThreads, 2) moments_tc_kernel(const float *__restrict__ x, int d, int64_t n,
                                                                     const float *__restrict__ lw,
                                                                     const double *__restrict__ summary,
                                                                     const double *__restrict__ center,
                                                                     float *__restrict__ partial, int *error) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char *s_raw = smem;
-    unsigned char *s_a = smem + (size_t)kMtStages * kMtRawBytes;  // [buf][part] x kMtPart
-    float *s_c = reinterpret_cast<float *>(s_a + (size_t)2 * 2 * kMtPart);
+    unsigned char *s_a = smem;                                    // [buf][part] x kMtPart
+    unsigned char *s_raw = smem + (size_t)2 * 2 * kMtPart;
+    float *s_c = reinterpret_cast<float *>(s_raw + (size_t)kMtStages * kMtRawBytes);
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag;
@@ -52,12 +59,6 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
         abort_flag = 0;
     }
     for (int c = tid; c < 64; c += kMtThreads) s_c[c] = c < d ? (float)center[c] : 0.f;
-    // row groups 9..15 stay zero in every buffer and part
-    for (int e = tid; e < 2 * 2 * 7 * kMtTile; e += kMtThreads) {
-        const int k = e % kMtTile, g = 9 + (e / kMtTile) % 7, bp = e / (7 * kMtTile);
-        *reinterpret_cast<uint4 *>(s_a + (size_t)bp * kMtPart + (size_t)g * kMtTile * 16 + k * 16) =
-            make_uint4(0u, 0u, 0u, 0u);
-    }
     const float m = (float)summary[0];
     const float inv_sqrt_s = (float)(1.0 / sqrt(summary[1]));
     tc::fence_before_sync();
@@ -153,7 +154,7 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
     for (int s = 0; s < kMtStages; ++s) issue_raw(s);
     for (int it = 0; it < my_tiles; ++it) {
         const int buf = it & 1;
-        tc::cp_async_wait<kMtStages - 1>();
+        tc::cp_async_wait<0>();
         bool ok = true;
         if (it >= 2 && !tc::mbar_wait(&bar[buf], (uses[buf] - 1) & 1)) ok = false;
         if (!ok) {
@@ -260,12 +261,12 @@ __global__ void moments_tc_finish_kernel(const double *__restrict__ sums, int d,
 }
 
 static int moments_tc_blocks(int64_t n) {
-    const int64_t t = (n + kMtTile - 1) / kMtTile;
-    return (int)(t < kSMs ? (t < 1 ? 1 : t) : kSMs);
+    const int64_t t = (n + kMtTile - 1) / kMtTile, cap = (int64_t)kSMs * kMtCtasPerSm;
+    return (int)(t < cap ? (t < 1 ? 1 : t) : cap);
 }
 
 size_t moments_tc_workspace_bytes(int64_t n) {
-    return sizeof(float) * (size_t)kSMs * 65 * kMtCols + sizeof(double) * 65 * kMtCols + 128;
+    return sizeof(float) * (size_t)kSMs * kMtCtasPerSm * 65 * kMtCols + sizeof(double) * 65 * kMtCols + 128;
 }
 
 int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *summary, const double *shift,
@@ -279,7 +280,7 @@ int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *su
     if (e) return e;
     { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw, summary,
                                                                 shift, partial, error); note_launch(); }
-    double *sums = reinterpret_cast<double *>(partial + (size_t)kSMs * 65 * kMtCols);
+    double *sums = reinterpret_cast<double *>(partial + (size_t)kSMs * kMtCtasPerSm * 65 * kMtCols);
     { moments_tc_reduce_kernel<<<(65 * kMtCols + 31) / 32, 256, 0, stream>>>(partial, blocks, sums); note_launch(); }
     { moments_tc_finish_kernel<<<(d * d + 255) / 256, 256, 0, stream>>>(sums, d, shift, mean, cov); note_launch(); }
     return (int)cudaGetLastError();
