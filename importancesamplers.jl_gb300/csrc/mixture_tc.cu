@@ -39,7 +39,6 @@
 
 namespace issm {
 
-constexpr int kTcThreads = 256;
 constexpr int kTcTile = 128;
 constexpr size_t kTcMaxSmem = 232448 - 1024;  // dynamic shared memory per CTA, static part reserved
 
@@ -128,13 +127,20 @@ struct TcParams {
     int *error;
 };
 
+// Warp roles of mixture_tc_kernel.
+constexpr int kConvWarps = 8;  // stage sample tiles and build the A operand
+constexpr int kEpiWarps = 4;   // one per TMEM lane quadrant
+constexpr int kConvThreads = 32 * kConvWarps;
+constexpr int kFirstEpiWarp = 1 + kConvWarps;
+constexpr int kTcThreads = 32 * (1 + kConvWarps + kEpiWarps);
+
 template <int KIND, int SPLIT, int DP>
 __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
     constexpr int PER = 16 / EB;              // elements per 16-byte K group
     constexpr int KG = DP / PER;              // K groups of the sample coordinates
     constexpr int KGX = KG + 2;               // plus the constant-1 column and padding
-    constexpr int QH = KG / 2;                // K groups converted per thread
+    constexpr int QH = KG / 2;                // K groups converted per thread (two threads per row)
     constexpr int NPART = SPLIT == 3 ? 2 : 1;
     constexpr int RS = DP + 4;                // padded raw row (floats): conflict-free row reads
     constexpr int RAW_BYTES = kTcTile * RS * 4;
@@ -142,33 +148,32 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     constexpr int B_COMP = DP * KGX * 16;
     constexpr int KSTEPS = KGX / 2;           // MMA K slices of 32 bytes
     constexpr uint32_t LBO_A = kTcTile * 16;
-    constexpr int HALF = DP / 2;              // columns per warp half when one component is split
     const int chunk = p.chunk, nchunks = p.nchunks, S = p.raw_stages;
     const int nbufB = nchunks > 1 ? 2 : 1;
     const uint32_t LBO_B = (uint32_t)(chunk * DP * 16);
-    // one component per tile: both warp halves share it, by column halves
-    const bool split_cols = (nchunks == 1 && chunk == 1);
 
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *s_raw = smem;
     unsigned char *s_a = s_raw + (size_t)S * RAW_BYTES;
     unsigned char *s_b = s_a + (size_t)2 * NPART * A_PART;
-    float *s_x = reinterpret_cast<float *>(s_b + (size_t)nbufB * NPART * chunk * B_COMP);
-    float *s_c = s_x + 4 * kTcTile;
-    __shared__ __align__(8) uint64_t bar_mma[2];
-    __shared__ __align__(8) uint64_t bar_b[2];
+    float *s_c = reinterpret_cast<float *>(s_b + (size_t)nbufB * NPART * chunk * B_COMP);
+    __shared__ __align__(8) uint64_t a_full[2], a_empty[2], b_full[2], b_empty[2], d_full[2], d_empty[2];
     __shared__ uint32_t tmem_base;
-    __shared__ int abort_flag;
+    __shared__ volatile int abort_flag;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int NW = chunk * DP;  // TMEM columns of one accumulator
     const uint32_t ncols = 2 * NW <= 32 ? 32 : 2 * NW <= 64 ? 64 : 2 * NW <= 128 ? 128 : 2 * NW <= 256 ? 256 : 512;
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     if (tid == 0) {
-        tc::mbar_init(&bar_mma[0], 1);
-        tc::mbar_init(&bar_mma[1], 1);
-        tc::mbar_init(&bar_b[0], 1);
-        tc::mbar_init(&bar_b[1], 1);
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&a_full[b], kConvWarps);
+            tc::mbar_init(&a_empty[b], 1);
+            tc::mbar_init(&b_full[b], 1);
+            tc::mbar_init(&b_empty[b], 1);
+            tc::mbar_init(&d_full[b], 1);
+            tc::mbar_init(&d_empty[b], kEpiWarps);
+        }
         tc::fence_mbar_init();
         abort_flag = 0;
     }
@@ -182,6 +187,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
         *reinterpret_cast<uint4 *>(s_a + (size_t)(buf * NPART + part) * A_PART + (size_t)(KG + g) * LBO_A +
                                    row * 16) = make_uint4(first, 0u, 0u, 0u);
     }
+    tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -189,238 +195,238 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
 
     const int my_tiles = (p.ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
     const int J = my_tiles * nchunks;
-    const bool vec = (p.d % 4 == 0) && ((reinterpret_cast<uintptr_t>(p.x) & 15) == 0);
-    const int ggen = (p.den_kind == ISSM_DENOM_PARTIAL) ? p.group[p.fixed_slot] : 0;
-
     auto tile_of = [&](int it) -> int64_t { return (int64_t)blockIdx.x + (int64_t)it * gridDim.x; };
     auto chunk_range = [&](int ch, int &k0, int &cnt) {
         k0 = p.first_slot + ch * chunk;
         cnt = min(chunk, p.last_slot - k0 + 1);
     };
+    // bounded wait that gives up at once after any role has timed out
+    auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
+        if (abort_flag) return false;
+        if (tc::mbar_wait(bar, parity)) return true;
+        atomicExch(p.error, 1);
+        abort_flag = 1;
+        return false;
+    };
 
-    // ---- raw sample tiles: cp.async into stage it % S, one commit group per tile
-    auto issue_raw = [&](int it) {
-        if (it < my_tiles) {
-            const int64_t row0 = tile_of(it) * kTcTile;
-            const int rows = (int)min((int64_t)kTcTile, p.n - row0);
-            float *dst = reinterpret_cast<float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
-            const float *src = p.x + row0 * p.d;
-            if (vec && p.d == DP) {
-                constexpr int Q4 = DP / 4;
-                const int total = rows * Q4;
-                for (int e = tid; e < total; e += kTcThreads) {
-                    const int r = e / Q4, c4 = e % Q4;
-                    tc::cp_async16(dst + r * RS + c4 * 4, src + (size_t)e * 4);
+    if (warp == 0) {
+        // ================= issuer: component operands and MMAs =================
+        int b_issued = 0, b_waited = 0;
+        auto issue_b = [&](int j) {
+            int k0, cnt;
+            chunk_range(j % nchunks, k0, cnt);
+            const int buf = nbufB == 1 ? 0 : (j & 1);
+            const uint32_t bytes = (uint32_t)(NPART * KGX * cnt * DP * 16);
+            if (lane == 0) tc::mbar_arrive_expect_tx(&b_full[buf], bytes);
+            __syncwarp();
+            unsigned char *dstb = s_b + (size_t)buf * NPART * chunk * B_COMP;
+            for (int e = lane; e < NPART * KGX * cnt; e += 32) {
+                const int part = e / (KGX * cnt), rem = e - part * KGX * cnt, q = rem / cnt, kk = rem - q * cnt;
+                const unsigned char *src = p.ops + ((size_t)(k0 + kk) * NPART + part) * B_COMP + (size_t)q * DP * 16;
+                unsigned char *dst = dstb + (size_t)part * chunk * B_COMP + (size_t)q * LBO_B + (size_t)kk * DP * 16;
+                tc::bulk_copy_g2s(dst, src, DP * 16, &b_full[buf]);
+            }
+            __syncwarp();
+            ++b_issued;
+        };
+        if (J > 0) issue_b(0);
+        if (nchunks > 1 && J > 1) issue_b(1);
+        for (int j = 0; j < J; ++j) {
+            const int it = j / nchunks, ch = j - it * nchunks;
+            int ok = 1;
+            if (lane == 0) {
+                if (ch == 0 && !wait(&a_full[it & 1], (uint32_t)((it >> 1) & 1))) ok = 0;
+                if (nchunks > 1 || j == 0) {
+                    if (!wait(&b_full[nbufB == 1 ? 0 : (j & 1)], nbufB == 1 ? 0u : (uint32_t)((j >> 1) & 1))) ok = 0;
+                    else b_waited = j + 1;
                 }
-            } else if (vec) {
-                const int q4 = p.d >> 2, total = rows * q4;
-                for (int e = tid; e < total; e += kTcThreads) {
-                    const int r = e / q4, c4 = e - r * q4;
-                    tc::cp_async16(dst + r * RS + c4 * 4, src + (size_t)r * p.d + c4 * 4);
+                if (j >= 2 && !wait(&d_empty[j & 1], (uint32_t)(((j - 2) >> 1) & 1))) ok = 0;
+                tc::fence_after_sync();
+                if (ok) {
+                    int k0, cnt;
+                    chunk_range(ch, k0, cnt);
+                    const int bbuf = nbufB == 1 ? 0 : (j & 1);
+                    const uint32_t d_tmem = tbase + (uint32_t)((j & 1) * NW);
+                    const uint32_t idesc = tc::instr_desc(KIND, kTcTile, cnt * DP);
+                    const uint32_t a0 = tc::smem_u32(s_a + (size_t)(it & 1) * NPART * A_PART);
+                    const uint32_t b0 = tc::smem_u32(s_b + (size_t)bbuf * NPART * chunk * B_COMP);
+#pragma unroll
+                    for (int s = 0; s < KSTEPS; ++s) {
+                        const uint64_t da = tc::smem_desc(a0 + s * 2 * LBO_A, LBO_A, 128);
+                        const uint64_t db = tc::smem_desc(b0 + s * 2 * LBO_B, LBO_B, 128);
+                        if (KIND == tc::kTF32) {
+                            tc::mma_tf32(d_tmem, da, db, idesc, s > 0);
+                        } else {
+                            tc::mma(d_tmem, da, db, idesc, s > 0);
+                            if (SPLIT == 3) {
+                                const uint64_t dal = tc::smem_desc(a0 + A_PART + s * 2 * LBO_A, LBO_A, 128);
+                                const uint64_t dbl = tc::smem_desc(b0 + chunk * B_COMP + s * 2 * LBO_B, LBO_B, 128);
+                                tc::mma(d_tmem, dal, db, idesc, true);
+                                tc::mma(d_tmem, da, dbl, idesc, true);
+                            }
+                        }
+                    }
                 }
-            } else {
-                const int total = rows * p.d;
-                for (int e = tid; e < total; e += kTcThreads) {
-                    const int r = e / p.d, c = e - r * p.d;
-                    tc::cp_async4(dst + r * RS + c, src + (size_t)r * p.d + c);
-                }
+                // commits arrive when every earlier MMA has completed, issued or not
+                tc::commit(&d_full[j & 1]);
+                if (nbufB == 2) tc::commit(&b_empty[j & 1]);
+                if (ch == nchunks - 1) tc::commit(&a_empty[it & 1]);
+            }
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            // operands of item j + 1 go into the buffer MMA j - 1 has finished with
+            if (nchunks > 1 && j >= 1 && j + 1 < J) {
+                int fine = 1;
+                if (lane == 0 && !wait(&b_empty[(j + 1) & 1], (uint32_t)(((j - 1) >> 1) & 1))) fine = 0;
+                fine = __shfl_sync(0xffffffffu, fine, 0);
+                if (fine) issue_b(j + 1);
             }
         }
-        tc::cp_async_commit();
-    };
-    auto wait_raw = [&]() {
-        if (S == 1) tc::cp_async_wait<0>();
-        else if (S == 2) tc::cp_async_wait<1>();
-        else tc::cp_async_wait<2>();
-    };
-
-    // ---- component operands of item j: bulk copies on bar_b (warp 0 only)
-    int b_issued = 0;  // items whose operands were requested (warp 0)
-    auto issue_b = [&](int j) {
-        int k0, cnt;
-        chunk_range(j % nchunks, k0, cnt);
-        const int buf = nbufB == 1 ? 0 : (j & 1);
-        const uint32_t bytes = (uint32_t)(NPART * KGX * cnt * DP * 16);
-        if (lane == 0) tc::mbar_arrive_expect_tx(&bar_b[buf], bytes);
-        __syncwarp();
-        unsigned char *dstb = s_b + (size_t)buf * NPART * chunk * B_COMP;
-        for (int e = lane; e < NPART * KGX * cnt; e += 32) {
-            const int part = e / (KGX * cnt), rem = e - part * KGX * cnt, q = rem / cnt, kk = rem - q * cnt;
-            const unsigned char *src = p.ops + ((size_t)(k0 + kk) * NPART + part) * B_COMP + (size_t)q * DP * 16;
-            unsigned char *dst = dstb + (size_t)part * chunk * B_COMP + (size_t)q * LBO_B + (size_t)kk * DP * 16;
-            tc::bulk_copy_g2s(dst, src, DP * 16, &bar_b[buf]);
-        }
-        ++b_issued;
-    };
-
-    // ---- centre, round and split tile it into A buffer it & 1
-    float ln_pref0 = 0.f, ln_pref1 = 0.f;
-    auto convert = [&](int it) {
-        const float *raw = reinterpret_cast<const float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
-        unsigned char *a = s_a + (size_t)(it & 1) * NPART * A_PART;
-        const int row = tid & (kTcTile - 1), half = tid >> 7;
-        const int64_t i = tile_of(it) * kTcTile + row;
-        const bool active = i < p.n;
-#pragma unroll
-        for (int qq = 0; qq < QH; ++qq) {
-            const int q = half * QH + qq;
-            float v[PER];
-#pragma unroll
-            for (int m = 0; m < PER; m += 4) {
-                const int c = q * PER + m;
-                float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (active) f = *reinterpret_cast<const float4 *>(raw + row * RS + c);
-                const float4 cc = *reinterpret_cast<const float4 *>(s_c + c);
-                v[m] = (active && c < p.d) ? f.x - cc.x : 0.f;
-                v[m + 1] = (active && c + 1 < p.d) ? f.y - cc.y : 0.f;
-                v[m + 2] = (active && c + 2 < p.d) ? f.z - cc.z : 0.f;
-                v[m + 3] = (active && c + 3 < p.d) ? f.w - cc.w : 0.f;
-            }
-            const uint4 hi = pack_hi<KIND>(v);
-            *reinterpret_cast<uint4 *>(a + (size_t)q * LBO_A + row * 16) = hi;
-            if (NPART == 2) *reinterpret_cast<uint4 *>(a + A_PART + (size_t)q * LBO_A + row * 16) = pack_lo(v, hi);
-        }
-        if (p.mode == 1 && half == 0) {
-            const float l = active ? p.lognum[i] : 0.f;
-            if (it & 1) ln_pref1 = l;
-            else ln_pref0 = l;
-        }
-    };
-
-    // ---- MMAs of item j (one thread)
-    int mma_issued = 0, mma_waited = 0;  // thread 0 bookkeeping for the drain
-    auto issue_mma = [&](int j, int abuf) {
-        int k0, cnt;
-        chunk_range(j % nchunks, k0, cnt);
-        const int bbuf = nbufB == 1 ? 0 : (j & 1);
-        const uint32_t d_tmem = tbase + (uint32_t)((j & 1) * NW);
-        const uint32_t idesc = tc::instr_desc(KIND, kTcTile, cnt * DP);
-        const uint32_t a0 = tc::smem_u32(s_a + (size_t)abuf * NPART * A_PART);
-        const uint32_t b0 = tc::smem_u32(s_b + (size_t)bbuf * NPART * chunk * B_COMP);
-#pragma unroll
-        for (int s = 0; s < KSTEPS; ++s) {
-            const uint64_t da = tc::smem_desc(a0 + s * 2 * LBO_A, LBO_A, 128);
-            const uint64_t db = tc::smem_desc(b0 + s * 2 * LBO_B, LBO_B, 128);
-            if (KIND == tc::kTF32) {
-                tc::mma_tf32(d_tmem, da, db, idesc, s > 0);
-            } else {
-                tc::mma(d_tmem, da, db, idesc, s > 0);
-                if (SPLIT == 3) {
-                    const uint64_t dal = tc::smem_desc(a0 + A_PART + s * 2 * LBO_A, LBO_A, 128);
-                    const uint64_t dbl = tc::smem_desc(b0 + chunk * B_COMP + s * 2 * LBO_B, LBO_B, 128);
-                    tc::mma(d_tmem, dal, db, idesc, true);
-                    tc::mma(d_tmem, da, dbl, idesc, true);
-                }
-            }
-        }
-        tc::commit(&bar_mma[j & 1]);
-        ++mma_issued;
-    };
-
-    // ---- epilogue of item j: radial densities and the log-sum-exp
-    const int qd = warp & 3, h = warp >> 2;
-    const int erow = 32 * qd + lane;
-    LseState<float> lse;
-    float gen_lq = 0.f, last_lq = 0.f, r2_half = 0.f;
-    bool has_gen = false;
-    auto radial = [&](int k, float r2) -> float {
-        if (p.family == ISSM_GAUSSIAN) return p.lognorm[k] - 0.5f * r2;
-        const float nu = p.dofs[k];
-        return p.lognorm[k] - (nu + (float)p.d) * 0.5f * log1pf(r2 / nu);
-    };
-    auto take = [&](int k, float lq) {
-        bool member = true;
-        if (p.den_kind == ISSM_DENOM_GENERATING) member = (k == p.fixed_slot);
-        else if (p.den_kind == ISSM_DENOM_PARTIAL) member = (p.group[k] == ggen);
-        if (k == p.fixed_slot) {
-            gen_lq = lq;
-            has_gen = true;
-        }
-        last_lq = lq;
-        if (member) lse.add((p.coef ? p.coef[k] : 0.f) + lq);
-    };
-    auto epilogue = [&](int j, bool good) {
-        const int it = j / nchunks, ch = j - it * nchunks;
-        int k0, cnt;
-        chunk_range(ch, k0, cnt);
-        if (good) {
-            const uint32_t lane_base = tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)((j & 1) * NW);
-            if (split_cols) {
-                float r2 = 0.f;
-                if (HALF >= 16) {
-#pragma unroll
-                    for (int c0 = 0; c0 < HALF; c0 += 16) {
-                        float v[16];
-                        tc::tmem_ld16(lane_base + (uint32_t)(h * HALF + c0), v);
-#pragma unroll
-                        for (int q = 0; q < 16; ++q) r2 = fmaf(v[q], v[q], r2);
+        // drain: every requested copy has landed before the CTA exits
+        if (lane == 0)
+            for (int q = b_waited; q < b_issued; ++q)
+                tc::mbar_wait(&b_full[nbufB == 1 ? 0 : (q & 1)], nbufB == 1 ? 0u : (uint32_t)((q >> 1) & 1));
+    } else if (warp < kFirstEpiWarp) {
+        // ================= converters: sample tiles -> A operand =================
+        const int ctid = tid - 32;
+        const bool vec = (p.d % 4 == 0) && ((reinterpret_cast<uintptr_t>(p.x) & 15) == 0);
+        auto issue_raw = [&](int it) {
+            if (it < my_tiles) {
+                const int64_t row0 = tile_of(it) * kTcTile;
+                const int rows = (int)min((int64_t)kTcTile, p.n - row0);
+                float *dst = reinterpret_cast<float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
+                const float *src = p.x + row0 * p.d;
+                if (vec && p.d == DP) {
+                    constexpr int Q4 = DP / 4;
+                    const int total = rows * Q4;
+                    for (int e = ctid; e < total; e += kConvThreads) {
+                        const int r = e / Q4, c4 = e % Q4;
+                        tc::cp_async16(dst + r * RS + c4 * 4, src + (size_t)e * 4);
+                    }
+                } else if (vec) {
+                    const int q4 = p.d >> 2, total = rows * q4;
+                    for (int e = ctid; e < total; e += kConvThreads) {
+                        const int r = e / q4, c4 = e - r * q4;
+                        tc::cp_async16(dst + r * RS + c4 * 4, src + (size_t)r * p.d + c4 * 4);
                     }
                 } else {
-                    float v[8];
-                    tc::tmem_ld8(lane_base + (uint32_t)(h * HALF), v);
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) r2 = fmaf(v[q], v[q], r2);
+                    const int total = rows * p.d;
+                    for (int e = ctid; e < total; e += kConvThreads) {
+                        const int r = e / p.d, c = e - r * p.d;
+                        tc::cp_async4(dst + r * RS + c, src + (size_t)r * p.d + c);
+                    }
                 }
-                r2_half = r2;
-            } else {
-                for (int kk = h; kk < cnt; kk += 2) {
-                    float r2 = 0.f;
+            }
+            tc::cp_async_commit();
+        };
+        for (int s = 0; s < S; ++s) issue_raw(s);
+        const int row = ctid & (kTcTile - 1), half = ctid >> 7;
+        for (int it = 0; it < my_tiles; ++it) {
+            if (S == 1) tc::cp_async_wait<0>();
+            else if (S == 2) tc::cp_async_wait<1>();
+            else tc::cp_async_wait<2>();
+            tc::named_sync(1, kConvThreads);
+            bool ok = true;
+            if (it >= 2) {
+                if (lane == 0) ok = wait(&a_empty[it & 1], (uint32_t)(((it - 2) >> 1) & 1));
+                ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
+            }
+            if (ok) {
+                const float *raw = reinterpret_cast<const float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
+                unsigned char *a = s_a + (size_t)(it & 1) * NPART * A_PART;
+                const int64_t i = tile_of(it) * kTcTile + row;
+                const bool active = i < p.n;
+                const bool full = active && p.d == DP;
+#pragma unroll
+                for (int qq = 0; qq < QH; ++qq) {
+                    const int q = half * QH + qq;
+                    float v[PER];
+#pragma unroll
+                    for (int m = 0; m < PER; m += 4) {
+                        const int c = q * PER + m;
+                        const float4 cc = *reinterpret_cast<const float4 *>(s_c + c);
+                        if (full) {
+                            const float4 f = *reinterpret_cast<const float4 *>(raw + row * RS + c);
+                            v[m] = f.x - cc.x;
+                            v[m + 1] = f.y - cc.y;
+                            v[m + 2] = f.z - cc.z;
+                            v[m + 3] = f.w - cc.w;
+                        } else {
+                            float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+                            if (active) f = *reinterpret_cast<const float4 *>(raw + row * RS + c);
+                            v[m] = (active && c < p.d) ? f.x - cc.x : 0.f;
+                            v[m + 1] = (active && c + 1 < p.d) ? f.y - cc.y : 0.f;
+                            v[m + 2] = (active && c + 2 < p.d) ? f.z - cc.z : 0.f;
+                            v[m + 3] = (active && c + 3 < p.d) ? f.w - cc.w : 0.f;
+                        }
+                    }
+                    const uint4 hi = pack_hi<KIND>(v);
+                    *reinterpret_cast<uint4 *>(a + (size_t)q * LBO_A + row * 16) = hi;
+                    if (NPART == 2)
+                        *reinterpret_cast<uint4 *>(a + A_PART + (size_t)q * LBO_A + row * 16) = pack_lo(v, hi);
+                }
+            }
+            tc::fence_proxy_async();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&a_full[it & 1]);
+            tc::named_sync(1, kConvThreads);  // the stage is consumed: refill it
+            issue_raw(it + S);
+        }
+        tc::cp_async_wait_all();
+    } else {
+        // ================= epilogue: radial densities and the log-sum-exp =================
+        const int qd = warp & 3;
+        const int erow = 32 * qd + lane;
+        const int ggen = (p.den_kind == ISSM_DENOM_PARTIAL) ? p.group[p.fixed_slot] : 0;
+        LseState<float> lse;
+        float gen_lq = 0.f, last_lq = 0.f, prev_ln = 0.f;
+        for (int j = 0; j < J; ++j) {
+            const int it = j / nchunks, ch = j - it * nchunks;
+            const int64_t i = tile_of(it) * kTcTile + erow;
+            if (ch == 0 && p.mode == 1) prev_ln = i < p.n ? p.lognum[i] : 0.f;
+            const bool ok = __all_sync(0xffffffffu, wait(&d_full[j & 1], (uint32_t)((j >> 1) & 1)));
+            tc::fence_after_sync();
+            if (ok) {
+                int k0, cnt;
+                chunk_range(ch, k0, cnt);
+                const uint32_t lane_base = tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)((j & 1) * NW);
+                for (int kk = 0; kk < cnt; ++kk) {
+                    float r2a = 0.f, r2b = 0.f;
 #pragma unroll
                     for (int c0 = 0; c0 < DP; c0 += 16) {
                         float v[16];
                         tc::tmem_ld16(lane_base + (uint32_t)(kk * DP + c0), v);
 #pragma unroll
-                        for (int q = 0; q < 16; ++q) r2 = fmaf(v[q], v[q], r2);
+                        for (int q = 0; q < 16; q += 2) {
+                            r2a = fmaf(v[q], v[q], r2a);
+                            r2b = fmaf(v[q + 1], v[q + 1], r2b);
+                        }
                     }
-                    take(k0 + kk, radial(k0 + kk, r2));
-                }
-            }
-        }
-        if (ch != nchunks - 1) return;
-        // tile complete: the upper half hands its state to the lower half
-        if (h == 1) {
-            if (split_cols) {
-                s_x[erow] = r2_half;
-            } else {
-                s_x[erow] = lse.m;
-                s_x[kTcTile + erow] = lse.s;
-                s_x[2 * kTcTile + erow] = gen_lq;
-                s_x[3 * kTcTile + erow] = (float)((lse.nan ? 2 : 0) | (has_gen ? 1 : 0));
-            }
-        }
-        __syncthreads();
-        if (h == 0 && good) {
-            if (split_cols) {
-                take(k0, radial(k0, r2_half + s_x[erow]));
-            } else {
-                const float om = s_x[erow], os = s_x[kTcTile + erow];
-                const int of = (int)s_x[3 * kTcTile + erow];
-                if (of & 2) lse.nan = true;
-                if (of & 1) {
-                    gen_lq = s_x[2 * kTcTile + erow];
-                    has_gen = true;
-                }
-                if (om != -INFINITY) {
-                    if (lse.m == -INFINITY) {
-                        lse.m = om;
-                        lse.s = os;
-                    } else if (om > lse.m) {
-                        lse.s = lse.s * expf(lse.m - om) + os;
-                        lse.m = om;
-                    } else if (om == lse.m) {
-                        lse.s += os;
+                    const float r2 = r2a + r2b;
+                    const int k = k0 + kk;
+                    float lq;
+                    if (p.family == ISSM_GAUSSIAN) {
+                        lq = p.lognorm[k] - 0.5f * r2;
                     } else {
-                        lse.s += os * expf(om - lse.m);
+                        const float nu = p.dofs[k];
+                        lq = p.lognorm[k] - (nu + (float)p.d) * 0.5f * log1pf(r2 / nu);
                     }
+                    bool member = true;
+                    if (p.den_kind == ISSM_DENOM_GENERATING) member = (k == p.fixed_slot);
+                    else if (p.den_kind == ISSM_DENOM_PARTIAL) member = (p.group[k] == ggen);
+                    if (k == p.fixed_slot) gen_lq = lq;
+                    last_lq = lq;
+                    if (member) lse.add((p.coef ? p.coef[k] : 0.f) + lq);
                 }
             }
-            const int64_t i = tile_of(it) * kTcTile + erow;
-            if (i < p.n) {
+            tc::fence_before_sync();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&d_empty[j & 1]);
+            if (ch != nchunks - 1) continue;
+            if (ok && i < p.n) {
                 if (p.mode == 1) {
-                    const float prev = (it & 1) ? ln_pref1 : ln_pref0;
                     uint16_t reason = isnan(last_lq) ? ISSM_REASON_PROPOSAL_INVALID : 0;
                     if (!reason) {
-                        const float v = logaddexp(prev, p.coef[p.first_slot] + last_lq);
+                        const float v = logaddexp(prev_ln, p.coef[p.first_slot] + last_lq);
                         if (isnan(v) || v == -INFINITY) reason = ISSM_REASON_PROPOSAL_INVALID;
                         else p.lognum[i] = v;
                     }
@@ -436,84 +442,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
                     if (p.out_generating) p.out_generating[i] = bad ? -INFINITY : gen_lq;
                 }
             }
+            lse = LseState<float>();
+            gen_lq = 0.f;
+            last_lq = 0.f;
         }
-        lse = LseState<float>();
-        gen_lq = 0.f;
-        last_lq = 0.f;
-        r2_half = 0.f;
-        has_gen = false;
-    };
-
-    auto fail = [&]() {
-        atomicExch(p.error, 1);
-        abort_flag = 1;
-    };
-
-    // ---- prologue
-    for (int s = 0; s < S; ++s) issue_raw(s);
-    if (warp == 0 && J > 0) {
-        issue_b(0);
-        if (nchunks > 1 && J > 1) issue_b(1);
     }
-    int b_waited = 0;  // items whose operands this thread has seen land
-    bool good = true;
-
-    for (int j = 0; j < J; ++j) {
-        const int it = j / nchunks, ch = j - it * nchunks;
-        if (ch == 0) {
-            wait_raw();
-            __syncthreads();
-            convert(it);
-            tc::fence_proxy_async();
-            __syncthreads();
-            issue_raw(it + S);  // into the stage just consumed
-        }
-        if (nchunks > 1 || j == 0) {
-            const int buf = nbufB == 1 ? 0 : (j & 1);
-            const uint32_t par = nbufB == 1 ? 0u : (uint32_t)((j >> 1) & 1);
-            if (!tc::mbar_wait(&bar_b[buf], par)) {
-                good = false;
-                fail();
-            }
-            b_waited = j + 1;
-        }
-        if (tid == 0 && good) {
-            tc::fence_after_sync();
-            issue_mma(j, it & 1);
-        }
-        if (j > 0) {
-            if (!tc::mbar_wait(&bar_mma[(j - 1) & 1], (uint32_t)(((j - 1) >> 1) & 1))) {
-                good = false;
-                fail();
-            }
-            mma_waited = j;
-            good = __all_sync(0xffffffffu, good);
-            tc::fence_after_sync();
-            if (warp == 0 && nchunks > 1 && j + 1 < J && good) issue_b(j + 1);
-            epilogue(j - 1, good);
-        }
-        tc::fence_before_sync();
-        __syncthreads();
-        if (abort_flag) break;
-    }
-    if (!abort_flag && J > 0) {
-        if (!tc::mbar_wait(&bar_mma[(J - 1) & 1], (uint32_t)(((J - 1) >> 1) & 1))) {
-            good = false;
-            fail();
-        }
-        mma_waited = J;
-        good = __all_sync(0xffffffffu, good);
-        tc::fence_after_sync();
-        epilogue(J - 1, good);
-    }
-    // drain: no copy or MMA may still target this CTA's memory at exit
-    tc::cp_async_wait_all();
-    if (tid == 0) {
-        for (int q = b_waited; q < b_issued; ++q)
-            tc::mbar_wait(&bar_b[nbufB == 1 ? 0 : (q & 1)], nbufB == 1 ? 0u : (uint32_t)((q >> 1) & 1));
-        for (int q = mma_waited; q < mma_issued; ++q) tc::mbar_wait(&bar_mma[q & 1], (uint32_t)((q >> 1) & 1));
-    }
+    // ---- every role is done; in-flight MMAs have completed before TMEM is freed ----
     tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    if (tid == 0 && abort_flag && J > 0) tc::mbar_wait(&d_full[(J - 1) & 1], (uint32_t)(((J - 1) >> 1) & 1));
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tbase, ncols);
 }
@@ -587,7 +525,7 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
         const int nbufB = nch > 1 ? 2 : 1;
         for (; stages >= 1; --stages) {
             smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)nbufB * NPART * chunk * B_COMP +
-                   (size_t)4 * kTcTile * 4 + (size_t)DP * 4;
+                   (size_t)DP * 4;
             if (smem <= kTcMaxSmem) break;
         }
         if (stages >= 1 || chunk == 1) break;
