@@ -67,12 +67,14 @@ __device__ __forceinline__ uint4 pack_lo(const float *v, uint4 hi) {
 // Operand form of slot k: the DP x (DP + X) matrix [W_k | -b_k | 0], X = 16
 // bf16 or 8 tf32 elements (two extra 16-byte K groups), so the MMA yields
 // z = W_k (x - c) - b_k directly against samples extended by a constant 1.
-// NPART parts of KGX = KG + 2 groups: part p, K group q, row j at byte
-//   p * DP*KGX*16 + q * DP*16 + j * 16.
+// Slots are grouped in chunks of `chunk` consecutive slots; chunk g holds
+// NPART parts of KGX = KG + 2 K groups: part p, K group q, slot kk, row j at
+//   g * NPART*chunk*B + p * chunk*B + q * chunk*DP*16 + kk * DP*16 + j * 16
+// (B = DP*KGX*16), the shared-memory layout of one chunk.
 template <int KIND, int SPLIT, int DP>
 __global__ void __launch_bounds__(256) tc_prepare_kernel(const float *__restrict__ w, const float *__restrict__ loc,
-                                                         int d, int first, int cslot, unsigned char *__restrict__ ops,
-                                                         float *__restrict__ center) {
+                                                         int d, int first, int chunk, int cslot,
+                                                         unsigned char *__restrict__ ops, float *__restrict__ center) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
     constexpr int PER = 16 / EB;
     constexpr int KG = DP / PER;
@@ -99,7 +101,10 @@ __global__ void __launch_bounds__(256) tc_prepare_kernel(const float *__restrict
         nb[j] = -acc;
     }
     __syncthreads();
-    unsigned char *okp = ops + (size_t)k * NPART * B_COMP;
+    // chunk-contiguous: the operands of slots first + g*chunk .. are one block
+    // laid out as the MMA reads them (part, K group, slot in chunk, row)
+    const int g = (int)blockIdx.x / chunk, kk = (int)blockIdx.x % chunk;
+    unsigned char *okp = ops + (size_t)g * NPART * chunk * B_COMP + (size_t)kk * DP * 16;
     for (int e = threadIdx.x; e < KGX * DP; e += blockDim.x) {
         const int q = e / DP, j = e - q * DP;
         float v[PER];
@@ -107,8 +112,9 @@ __global__ void __launch_bounds__(256) tc_prepare_kernel(const float *__restrict
         for (int m = 0; m < PER; ++m)
             v[m] = q < KG ? ws[j * LD + q * PER + m] : (q == KG && m == 0 ? nb[j] : 0.f);
         const uint4 hi = pack_hi<KIND>(v);
-        *reinterpret_cast<uint4 *>(okp + (size_t)q * DP * 16 + (size_t)j * 16) = hi;
-        if (NPART == 2) *reinterpret_cast<uint4 *>(okp + B_COMP + (size_t)q * DP * 16 + (size_t)j * 16) = pack_lo(v, hi);
+        const size_t off = (size_t)q * chunk * DP * 16 + (size_t)j * 16;
+        *reinterpret_cast<uint4 *>(okp + off) = hi;
+        if (NPART == 2) *reinterpret_cast<uint4 *>(okp + (size_t)chunk * B_COMP + off) = pack_lo(v, hi);
     }
 }
 
@@ -133,6 +139,7 @@ constexpr int kEpiWarps = 4;   // one per TMEM lane quadrant
 constexpr int kConvThreads = 32 * kConvWarps;
 constexpr int kFirstEpiWarp = 1 + kConvWarps;
 constexpr int kTcThreads = 32 * (1 + kConvWarps + kEpiWarps);
+constexpr int kBRing = 3;      // operand buffers in flight when a tile needs several chunks
 
 template <int KIND, int SPLIT, int DP>
 __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
@@ -149,15 +156,20 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     constexpr int KSTEPS = KGX / 2;           // MMA K slices of 32 bytes
     constexpr uint32_t LBO_A = kTcTile * 16;
     const int chunk = p.chunk, nchunks = p.nchunks, S = p.raw_stages;
-    const int nbufB = nchunks > 1 ? 2 : 1;
+    // one component chunk: A double-buffered, the chunk's operands loaded once;
+    // several chunks: one A buffer (a tile is converted once per nchunks items)
+    // and a ring of kBRing operand buffers filled kBRing - 1 items ahead
+    const int nbufA = nchunks > 1 ? 1 : 2;
+    const int nbufB = nchunks > 1 ? kBRing : 1;
     const uint32_t LBO_B = (uint32_t)(chunk * DP * 16);
+    const uint32_t CHUNK_BYTES = (uint32_t)(NPART * chunk * B_COMP);
 
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *s_raw = smem;
     unsigned char *s_a = s_raw + (size_t)S * RAW_BYTES;
-    unsigned char *s_b = s_a + (size_t)2 * NPART * A_PART;
-    float *s_c = reinterpret_cast<float *>(s_b + (size_t)nbufB * NPART * chunk * B_COMP);
-    __shared__ __align__(8) uint64_t a_full[2], a_empty[2], b_full[2], b_empty[2], d_full[2], d_empty[2];
+    unsigned char *s_b = s_a + (size_t)nbufA * NPART * A_PART;
+    float *s_c = reinterpret_cast<float *>(s_b + (size_t)nbufB * CHUNK_BYTES);
+    __shared__ __align__(8) uint64_t a_full[2], a_empty[2], b_full[kBRing], b_empty[kBRing], d_full[2], d_empty[2];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_flag;
 
@@ -169,17 +181,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&a_full[b], kConvWarps);
             tc::mbar_init(&a_empty[b], 1);
-            tc::mbar_init(&b_full[b], 1);
-            tc::mbar_init(&b_empty[b], 1);
             tc::mbar_init(&d_full[b], 1);
             tc::mbar_init(&d_empty[b], kEpiWarps);
+        }
+        for (int b = 0; b < kBRing; ++b) {
+            tc::mbar_init(&b_full[b], 1);
+            tc::mbar_init(&b_empty[b], 1);
         }
         tc::fence_mbar_init();
         abort_flag = 0;
     }
     for (int c = tid; c < DP; c += kTcThreads) s_c[c] = p.center[c];
-    // constant K groups of both A buffers: a 1 in column DP (hi part), zeros elsewhere
-    for (int e = tid; e < 2 * NPART * 2 * kTcTile; e += kTcThreads) {
+    // constant K groups of the A buffers: a 1 in column DP (hi part), zeros elsewhere
+    for (int e = tid; e < nbufA * NPART * 2 * kTcTile; e += kTcThreads) {
         const int row = e % kTcTile, g = (e / kTcTile) & 1, part = (e / (2 * kTcTile)) % NPART,
                   buf = e / (2 * kTcTile * NPART);
         const uint32_t one = KIND == tc::kTF32 ? 0x3F800000u : 0x3F80u;
@@ -212,32 +226,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     if (warp == 0) {
         // ================= issuer: component operands and MMAs =================
         int b_issued = 0, b_waited = 0;
+        // the chunk's operands are one contiguous block in the workspace, laid
+        // out as in shared memory: one bulk copy per item
         auto issue_b = [&](int j) {
-            int k0, cnt;
-            chunk_range(j % nchunks, k0, cnt);
-            const int buf = nbufB == 1 ? 0 : (j & 1);
-            const uint32_t bytes = (uint32_t)(NPART * KGX * cnt * DP * 16);
-            if (lane == 0) tc::mbar_arrive_expect_tx(&b_full[buf], bytes);
-            __syncwarp();
-            unsigned char *dstb = s_b + (size_t)buf * NPART * chunk * B_COMP;
-            for (int e = lane; e < NPART * KGX * cnt; e += 32) {
-                const int part = e / (KGX * cnt), rem = e - part * KGX * cnt, q = rem / cnt, kk = rem - q * cnt;
-                const unsigned char *src = p.ops + ((size_t)(k0 + kk) * NPART + part) * B_COMP + (size_t)q * DP * 16;
-                unsigned char *dst = dstb + (size_t)part * chunk * B_COMP + (size_t)q * LBO_B + (size_t)kk * DP * 16;
-                tc::bulk_copy_g2s(dst, src, DP * 16, &b_full[buf]);
+            const int buf = j % nbufB;
+            if (lane == 0) {
+                tc::mbar_arrive_expect_tx(&b_full[buf], CHUNK_BYTES);
+                tc::bulk_copy_g2s(s_b + (size_t)buf * CHUNK_BYTES, p.ops + (size_t)(j % nchunks) * CHUNK_BYTES,
+                                  CHUNK_BYTES, &b_full[buf]);
             }
             __syncwarp();
             ++b_issued;
         };
-        if (J > 0) issue_b(0);
-        if (nchunks > 1 && J > 1) issue_b(1);
+        // single chunk: its operands once; several: fill the ring
+        for (int q = 0; q < nbufB && q < J; ++q) issue_b(q);
         for (int j = 0; j < J; ++j) {
             const int it = j / nchunks, ch = j - it * nchunks;
+            const int abuf = it % nbufA;
             int ok = 1;
             if (lane == 0) {
-                if (ch == 0 && !wait(&a_full[it & 1], (uint32_t)((it >> 1) & 1))) ok = 0;
+                if (ch == 0 && !wait(&a_full[abuf], (uint32_t)((it / nbufA) & 1))) ok = 0;
                 if (nchunks > 1 || j == 0) {
-                    if (!wait(&b_full[nbufB == 1 ? 0 : (j & 1)], nbufB == 1 ? 0u : (uint32_t)((j >> 1) & 1))) ok = 0;
+                    if (!wait(&b_full[j % nbufB], (uint32_t)((j / nbufB) & 1))) ok = 0;
                     else b_waited = j + 1;
                 }
                 if (j >= 2 && !wait(&d_empty[j & 1], (uint32_t)(((j - 2) >> 1) & 1))) ok = 0;
@@ -245,11 +255,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
                 if (ok) {
                     int k0, cnt;
                     chunk_range(ch, k0, cnt);
-                    const int bbuf = nbufB == 1 ? 0 : (j & 1);
                     const uint32_t d_tmem = tbase + (uint32_t)((j & 1) * NW);
                     const uint32_t idesc = tc::instr_desc(KIND, kTcTile, cnt * DP);
-                    const uint32_t a0 = tc::smem_u32(s_a + (size_t)(it & 1) * NPART * A_PART);
-                    const uint32_t b0 = tc::smem_u32(s_b + (size_t)bbuf * NPART * chunk * B_COMP);
+                    const uint32_t a0 = tc::smem_u32(s_a + (size_t)abuf * NPART * A_PART);
+                    const uint32_t b0 = tc::smem_u32(s_b + (size_t)(j % nbufB) * CHUNK_BYTES);
 #pragma unroll
                     for (int s = 0; s < KSTEPS; ++s) {
                         const uint64_t da = tc::smem_desc(a0 + s * 2 * LBO_A, LBO_A, 128);
@@ -269,22 +278,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
                 }
                 // commits arrive when every earlier MMA has completed, issued or not
                 tc::commit(&d_full[j & 1]);
-                if (nbufB == 2) tc::commit(&b_empty[j & 1]);
-                if (ch == nchunks - 1) tc::commit(&a_empty[it & 1]);
+                if (nchunks > 1) tc::commit(&b_empty[j % nbufB]);
+                if (ch == nchunks - 1) tc::commit(&a_empty[abuf]);
             }
             ok = __shfl_sync(0xffffffffu, ok, 0);
-            // operands of item j + 1 go into the buffer MMA j - 1 has finished with
-            if (nchunks > 1 && j >= 1 && j + 1 < J) {
+            // operands of item j + nbufB - 1 go into the buffer MMA j - 1 has finished with
+            const int jn = j + nbufB - 1;
+            if (nchunks > 1 && j >= 1 && jn < J) {
                 int fine = 1;
-                if (lane == 0 && !wait(&b_empty[(j + 1) & 1], (uint32_t)(((j - 1) >> 1) & 1))) fine = 0;
+                if (lane == 0 && !wait(&b_empty[jn % nbufB], (uint32_t)(((jn - nbufB) / nbufB) & 1))) fine = 0;
                 fine = __shfl_sync(0xffffffffu, fine, 0);
-                if (fine) issue_b(j + 1);
+                if (fine) issue_b(jn);
             }
         }
         // drain: every requested copy has landed before the CTA exits
         if (lane == 0)
-            for (int q = b_waited; q < b_issued; ++q)
-                tc::mbar_wait(&b_full[nbufB == 1 ? 0 : (q & 1)], nbufB == 1 ? 0u : (uint32_t)((q >> 1) & 1));
+            for (int q = b_waited; q < b_issued; ++q) tc::mbar_wait(&b_full[q % nbufB], (uint32_t)((q / nbufB) & 1));
     } else if (warp < kFirstEpiWarp) {
         // ================= converters: sample tiles -> A operand =================
         const int ctid = tid - 32;
@@ -326,13 +335,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
             else tc::cp_async_wait<2>();
             tc::named_sync(1, kConvThreads);
             bool ok = true;
-            if (it >= 2) {
-                if (lane == 0) ok = wait(&a_empty[it & 1], (uint32_t)(((it - 2) >> 1) & 1));
+            const int abuf = it % nbufA;
+            if (it >= nbufA) {
+                if (lane == 0) ok = wait(&a_empty[abuf], (uint32_t)(((it - nbufA) / nbufA) & 1));
                 ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
             }
             if (ok) {
                 const float *raw = reinterpret_cast<const float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
-                unsigned char *a = s_a + (size_t)(it & 1) * NPART * A_PART;
+                unsigned char *a = s_a + (size_t)abuf * NPART * A_PART;
                 const int64_t i = tile_of(it) * kTcTile + row;
                 const bool active = i < p.n;
                 const bool full = active && p.d == DP;
@@ -367,7 +377,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
             }
             tc::fence_proxy_async();
             __syncwarp();
-            if (lane == 0) tc::mbar_arrive(&a_full[it & 1]);
+            if (lane == 0) tc::mbar_arrive(&a_full[it % nbufA]);
             tc::named_sync(1, kConvThreads);  // the stage is consumed: refill it
             issue_raw(it + S);
         }
@@ -495,14 +505,16 @@ int invert_factors(const issm_bank *bk, int first, int count, float *out, cudaSt
     return (int)cudaGetLastError();
 }
 
-// Workspace: operand forms K x DP * (4 DP + 64) bytes | centre (256 bytes) |
-// inverse factors K x DP * DP floats (only when the bank has none).
+// Workspace: operand forms (K + 256/DP - 1) x DP * (4 DP + 64) bytes (room
+// for the last, partial chunk) | centre (256 bytes) | inverse factors
+// K x DP * DP floats (only when the bank has none).
 static int dp_of(int d) { return d <= 16 ? 16 : d <= 32 ? 32 : 64; }
 static size_t ops_slot_bytes(int DP) { return (size_t)DP * (4 * DP + 64); }
+static size_t ops_bytes(int k, int DP) { return (size_t)(k + 256 / DP - 1) * ops_slot_bytes(DP); }
 
 size_t tc_workspace_bytes(int k, int d) {
     const int DP = dp_of(d);
-    return (size_t)k * ops_slot_bytes(DP) + 256 + (size_t)k * DP * DP * 4 + 64;
+    return ops_bytes(k, DP) + 256 + (size_t)k * DP * DP * 4 + 64;
 }
 
 template <int KIND, int SPLIT, int DP>
@@ -516,26 +528,28 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     constexpr size_t B_COMP = (size_t)DP * KGX * 16;
     static_assert(NPART * B_COMP <= (size_t)DP * (4 * DP + 64), "operand form exceeds its workspace slot");
     const int nslots = p.last_slot - p.first_slot + 1;
-    int chunk = min(nslots, 256 / DP);
+    // largest chunk (<= 256 TMEM columns) whose buffers fit: one chunk keeps
+    // three staged tiles and two A buffers; several chunks keep one staged
+    // tile, one A buffer and a ring of kBRing chunk buffers
+    int chunk = min(nslots, 256 / DP), nch = 1, stages = 1;
     size_t smem = 0;
-    int nch = 1, stages = 1;
-    for (;;) {
+    for (; chunk >= 1; --chunk) {
         nch = (nslots + chunk - 1) / chunk;
-        stages = nch == 1 ? 3 : 1;
-        const int nbufB = nch > 1 ? 2 : 1;
-        for (; stages >= 1; --stages) {
-            smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)nbufB * NPART * chunk * B_COMP +
-                   (size_t)DP * 4;
-            if (smem <= kTcMaxSmem) break;
+        if (nch == 1) {
+            stages = 3;
+            smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)NPART * chunk * B_COMP + (size_t)DP * 4;
+        } else {
+            stages = 1;
+            smem = stages * RAW_BYTES + NPART * A_PART + (size_t)kBRing * NPART * chunk * B_COMP + (size_t)DP * 4;
         }
-        if (stages >= 1 || chunk == 1) break;
-        --chunk;
+        if (smem <= kTcMaxSmem) break;
     }
-    if (stages < 1) return ISSM_E_UNSUPPORTED;
+    if (chunk < 1) return ISSM_E_UNSUPPORTED;
     p.chunk = chunk;
     p.nchunks = nch;
     p.raw_stages = stages;
-    { tc_prepare_kernel<KIND, SPLIT, DP><<<nslots, 256, 0, stream>>>(w, loc, p.d, p.first_slot, cslot, ops, center);
+    { tc_prepare_kernel<KIND, SPLIT, DP><<<nslots, 256, 0, stream>>>(w, loc, p.d, p.first_slot, chunk, cslot, ops,
+                                                                       center);
       note_launch(); }
     auto kern = mixture_tc_kernel<KIND, SPLIT, DP>;
     const int st = allow_dynamic_smem((const void *)kern);
@@ -565,7 +579,7 @@ int tc_mixture(const issm_bank *bk, const issm_denominator *den, int mode, int f
     const int K = bk->count;
     if (ws_bytes < tc_workspace_bytes(K, d)) return ISSM_E_WORKSPACE;
     unsigned char *ops = (unsigned char *)ws;
-    float *center = (float *)(ops + (size_t)K * ops_slot_bytes(DP));
+    float *center = (float *)(ops + ops_bytes(K, DP));
     float *winv = (float *)((unsigned char *)center + 256);
     const int den_kind = den ? den->kind : ISSM_DENOM_FULL;
     // only the generating slot contributes to a generating-only denominator
