@@ -148,19 +148,21 @@ int weighted_moments(const void *x, int d, int64_t n, const void *lw, int dtype,
 // right-looking Cholesky in FP64; factor *= sqrt(1/c_nu) for Student-t
 // (src/proposals.jl:73-80); zero upper triangle; lognormalizer and validity
 // (:493-528).
-// 1 / sqrt(a) in FP64 without the long FP64 square-root and division
-// sequences on the factorisation's critical path: an FP32 seed refined by two
-// Newton-Raphson steps r <- r (3 - a r^2) / 2 (quadratic convergence: about
-// 22 -> 44 -> full double bits). Inputs outside the FP32 seed's range, zero,
-// negative or non-finite values take the exact route (and give the same
-// NaN/Inf as it would).
-__device__ __forceinline__ double rsqrt_nr(double a) {
-    if (!(a > 1e-30 && a < 1e30)) return 1.0 / sqrt(a);
-    double r = (double)rsqrtf((float)a);
-    const double ha = 0.5 * a;
-    r = r * fma(-ha * r, r, 1.5);
-    r = r * fma(-ha * r, r, 1.5);
-    return r;
+// 1 / a in FP64 with few FP64 instructions: an FP32 reciprocal seed refined
+// by two Newton-Raphson steps r <- r + r (1 - a r) (about 24 -> 48 -> full
+// double bits). Each FP64 instruction occupies a warp's FP64 pipe for about
+// 64 cycles on this GPU (and takes as long to complete), so the factorisation's
+// sequential chain is built from as few of them as possible. Values outside
+// the FP32 seed's range, zero, negative or non-finite values take the exact
+// division (and give its NaN / Inf).
+__device__ __forceinline__ double rcp_nr(double a) {
+    const float af = (float)a;
+    if (!(af > 1e-30f && af < 1e30f)) return 1.0 / a;
+    double r = (double)__frcp_rn(af);
+    double e = fma(-a, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-a, r, 1.0);
+    return fma(r, e, r);
 }
 
 template <typename T>
@@ -174,13 +176,15 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
     __shared__ double red[256];
     __shared__ int bad;
     const double mult = dof > 0.0 ? dof / (dof - 2.0) : 1.0;
-    double tr = 0.0;
+    // tr(L_prev L_prev^T) accumulated in the factor's precision, as the
+    // reference does (_factor_scale_aware_ridge), then merged in FP64
+    T tr = T(0);
     for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
         const int r = e % d, c = e / d;
-        if (r >= c) { const double v = (double)prev[e]; tr += v * v; }
+        if (r >= c) { const T v = prev[e]; tr += v * v; }
         A[e] = cov[e];
     }
-    red[threadIdx.x] = tr;
+    red[threadIdx.x] = (double)tr;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
     for (int off = 128; off > 0; off >>= 1) {
@@ -208,74 +212,69 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
     }
     for (int c = threadIdx.x; c < d; c += blockDim.x) A[c + c * d] += ridge;
     __syncthreads();
-    // Blocked right-looking Cholesky (8-column panels): factor the diagonal
-    // block in one warp, solve the panel below it one row per thread, then
-    // the rank-8 trailing update; three barriers per panel. FP64 throughput is
-    // low on this GPU, so the sequential part is kept to the 8 x 8 blocks.
-    __shared__ double inv_diag[8];
-    for (int kb = 0; kb < d; kb += 8) {
-        const int nb = min(8, d - kb);
-        if (threadIdx.x < 32) {
-            const int lane = threadIdx.x;
-            for (int j = kb; j < kb + nb; ++j) {
-                const double djj = A[j + j * d];
-                const double rl = rsqrt_nr(djj);
-                const double ljj = djj * rl;
-                if (lane == 0) {
-                    if (!(djj > 0.0) || !isfinite(djj)) bad = 1;
-                    inv_diag[j - kb] = rl;
-                }
-                const int rows = kb + nb - 1 - j;
-                if (lane < rows) A[(j + 1 + lane) + j * d] *= rl;
-                __syncwarp();
-                if (lane == 0) A[j + j * d] = ljj;
-                // update the rest of the diagonal block (rows, cols > j)
-                for (int e = lane; e < rows * rows; e += 32) {
-                    const int i = e % rows, c = e / rows;
-                    if (i >= c) A[(j + 1 + i) + (j + 1 + c) * d] -= A[(j + 1 + i) + j * d] * A[(j + 1 + c) + j * d];
-                }
-                __syncwarp();
+    // Right-looking LDL^T factorisation, A = L D L^T with unit lower L: per
+    // column j, warp 0 forms 1/d_j (four FP64 instructions after an FP32 seed)
+    // and scales the column below the pivot, keeping the unscaled column in
+    // u; then all eight warps apply the rank-1 update A_ik -= l_ij u_k to the
+    // trailing lower triangle, mapped onto column pairs (k, m-1-k) so every
+    // thread gets the same number of elements. The Cholesky factor is
+    // L diag(sqrt(d)), formed afterwards in parallel; its pivots fail exactly
+    // when Cholesky's would (d_j <= 0 or not finite).
+    __shared__ double s_u[64];
+    __shared__ double s_dg[64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int j = 0; j < d; ++j) {
+        if (warp == 0) {
+            const double dj = A[j + j * d];
+            const double rj = rcp_nr(dj);
+            if (lane == 0) {
+                if (!(dj > 0.0) || !isfinite(dj)) bad = 1;
+                s_dg[j] = dj;
+            }
+            for (int i = j + 1 + lane; i < d; i += 32) {
+                const double u = A[i + j * d];
+                s_u[i] = u;
+                A[i + j * d] = u * rj;
             }
         }
         __syncthreads();
-        // panel: rows below the block, L[i, kb:kb+nb] = A[i, kb:kb+nb] L_bb^-T
-        for (int i = kb + nb + threadIdx.x; i < d; i += blockDim.x) {
-            for (int c = 0; c < nb; ++c) {
-                double v = A[i + (kb + c) * d];
-                for (int q = 0; q < c; ++q) v -= A[i + (kb + q) * d] * A[(kb + c) + (kb + q) * d];
-                A[i + (kb + c) * d] = v * inv_diag[c];
+        const int m = d - j - 1, base = j + 1;
+        const int half = (m + 1) >> 1;
+        for (int e = threadIdx.x; e < half * (m + 1); e += blockDim.x) {
+            const int c = e / (m + 1), r = e - c * (m + 1);
+            int i, k;
+            if (r < m - c) {
+                k = c;
+                i = c + r;
+            } else {
+                k = m - 1 - c;
+                i = k + (r - (m - c));
+                if (k == c || i >= m) continue;
             }
-        }
-        __syncthreads();
-        // trailing rank-nb update of the lower triangle, 16 x 16 thread tile
-        const int m = d - kb - nb, base = kb + nb;
-        const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-        for (int c = ty; c < m; c += 16) {
-            double lc[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) lc[q] = q < nb ? A[(base + c) + (kb + q) * d] : 0.0;
-            for (int i = c + ((tx - c) & 15); i < m; i += 16) {
-                double acc = A[(base + i) + (base + c) * d];
-#pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    if (q < nb) acc -= A[(base + i) + (kb + q) * d] * lc[q];
-                A[(base + i) + (base + c) * d] = acc;
-            }
+            A[(base + i) + (base + k) * d] -= A[(base + i) + j * d] * s_u[base + k];
         }
         __syncthreads();
     }
-    // Student-t scaling, rounding to T, validity and log|L| as block reductions
+    // column scales sqrt(d_j) times the Student-t factor; the factor is L s
+    __shared__ double s_scale[64];
     const double f = dof > 0.0 ? sqrt(1.0 / mult) : 1.0;
+    for (int c = threadIdx.x; c < d; c += blockDim.x) s_scale[c] = sqrt(s_dg[c]) * f;
+    __syncthreads();
+    // rounding to T, validity and log|L| as block reductions
     double logdet = 0.0;
     int invalid = 0;
+    // the FP32 copy of the stored factor for the inverse (after A in shared memory)
+    constexpr int LDI = 65;
+    float *Lf = reinterpret_cast<float *>(A + d * d);
     for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
         const int r = e % d, c = e / d;
-        const T v = r >= c ? (T)(A[e] * f) : T(0);
+        const T v = r > c ? (T)(A[e] * s_scale[c]) : r == c ? (T)s_scale[c] : T(0);
         out_factor[e] = v;
+        if (out_inverse != nullptr) Lf[r * LDI + c] = (float)v;
         if (r >= c) {
-            invalid |= !isfinite((double)v);
+            invalid |= !isfinite(v);
             if (r == c) {
-                invalid |= !((double)v > 0.0);
+                invalid |= !(v > T(0));
                 // log|L_jj| in the factor's own precision, summed in FP64
                 logdet += (double)dlog(fabs(v));
             }
@@ -303,19 +302,13 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
     // inverse factor for the tensor-core forms: W = (stored factor)^-1 in
     // FP32, DP x DP row-major zero padded
     if (out_inverse != nullptr) {
-        constexpr int LD = 65;
-        float *Lf = reinterpret_cast<float *>(A + d * d);
-        float *Wf = Lf + 64 * LD;
-        for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
-            const int r = e % d, c = e / d;
-            Lf[r * LD + c] = r >= c ? (float)(T)(A[e] * f) : 0.f;
-        }
+        float *Wf = Lf + 64 * LDI;
         __syncthreads();
-        invert_lower_f32(Lf, Wf, d, LD);
+        invert_lower_f32(Lf, Wf, d, LDI);
         const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
         for (int e = threadIdx.x; e < DP * DP; e += blockDim.x) {
             const int j = e / DP, c = e % DP;
-            out_inverse[e] = (j < d && c < d) ? Wf[j * LD + c] : 0.f;
+            out_inverse[e] = (j < d && c < d) ? Wf[j * LDI + c] : 0.f;
         }
     }
 }
