@@ -303,6 +303,16 @@ int issm_amis_form(const void *logtargets, const void *lognumerators, const int6
                      (cudaStream_t)stream);
 }
 
+int issm_amis_form_summary(const void *logtargets, const void *lognumerators, const int64_t *round_ids,
+                           double logtotal, int64_t n, int32_t dtype, void *logweights, uint64_t *failures,
+                           double *summary, void *workspace, size_t workspace_bytes, issm_stream_t stream) {
+    if (n < 1) return ISSM_E_SIZE;
+    if (!logtargets || !lognumerators || !logweights || !summary || !workspace) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return amis_form_summary(logtargets, lognumerators, round_ids, logtotal, n, dtype, logweights, failures, summary,
+                             workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
 size_t issm_reduce_workspace_bytes(int64_t n) { return reduce_workspace_bytes(n < 1 ? 1 : n); }
 
 int issm_logweight_summary(const void *logweights, int64_t n, int32_t dtype, double *out, void *workspace,

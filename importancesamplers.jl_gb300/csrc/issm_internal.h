@@ -28,6 +28,9 @@ size_t reduce_workspace_bytes(int64_t n);
 int logweight_summary(const void *lw, int64_t n, int dtype, double *out, void *ws, size_t ws_bytes,
                       cudaStream_t stream);
 int normalize(const void *lw, int64_t n, int dtype, const double *summary, void *w, cudaStream_t stream);
+int amis_form_summary(const void *lt, const void *lnum, const int64_t *round_ids, double logtotal, int64_t n,
+                      int dtype, void *lw, uint64_t *failures, double *out, void *ws, size_t ws_bytes,
+                      cudaStream_t stream);
 int resampling_cdf(const void *lw, int64_t n, int dtype, void *cdf, void *ws, size_t ws_bytes,
                    cudaStream_t stream);
 

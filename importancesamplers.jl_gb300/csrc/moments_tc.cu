@@ -117,7 +117,16 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
                 float *dst = reinterpret_cast<float *>(s_raw + (size_t)(it % kMtStages) * kMtRawBytes);
                 float *dlw = dst + kMtTile * kMtRS;
                 const float *src = x + row0 * d;
-                if (vec) {
+                if (vec && d == 64) {
+                    const int total = rows * 16;
+                    for (int e = ctid; e < total; e += kMtConvThreads)
+                        tc::cp_async16(dst + (e >> 4) * kMtRS + (e & 15) * 4, src + (size_t)e * 4);
+                    if (rows == kMtTile) {
+                        if (ctid < kMtTile / 4) tc::cp_async16(dlw + ctid * 4, lw + row0 + ctid * 4);
+                    } else {
+                        for (int r = ctid; r < rows; r += kMtConvThreads) tc::cp_async4(dlw + r, lw + row0 + r);
+                    }
+                } else if (vec) {
                     const int q4 = d >> 2, total = rows * q4;
                     for (int e = ctid; e < total; e += kMtConvThreads) {
                         const int r = e / q4, c4 = e - r * q4;
@@ -157,25 +166,39 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
                 const bool active = i < n;
                 const float l = active ? raw[kMtTile * kMtRS + k] : -INFINITY;
                 const float sw = l == -INFINITY ? 0.f : expf(0.5f * (l - m)) * inv_sqrt_s;
+                const bool full = active && d == 64;
 #pragma unroll
                 for (int gg = 0; gg < 4; ++gg) {
                     const int g = half * 4 + gg, c = g * 8;
                     float v[8];
-                    float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f), f1 = f0;
-                    if (active) {
-                        f0 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c);
-                        f1 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c + 4);
-                    }
                     const float4 c0 = *reinterpret_cast<const float4 *>(s_c + c),
                                  c1 = *reinterpret_cast<const float4 *>(s_c + c + 4);
-                    v[0] = (active && c < d) ? sw * (f0.x - c0.x) : 0.f;
-                    v[1] = (active && c + 1 < d) ? sw * (f0.y - c0.y) : 0.f;
-                    v[2] = (active && c + 2 < d) ? sw * (f0.z - c0.z) : 0.f;
-                    v[3] = (active && c + 3 < d) ? sw * (f0.w - c0.w) : 0.f;
-                    v[4] = (active && c + 4 < d) ? sw * (f1.x - c1.x) : 0.f;
-                    v[5] = (active && c + 5 < d) ? sw * (f1.y - c1.y) : 0.f;
-                    v[6] = (active && c + 6 < d) ? sw * (f1.z - c1.z) : 0.f;
-                    v[7] = (active && c + 7 < d) ? sw * (f1.w - c1.w) : 0.f;
+                    if (full) {
+                        const float4 f0 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c);
+                        const float4 f1 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c + 4);
+                        v[0] = sw * (f0.x - c0.x);
+                        v[1] = sw * (f0.y - c0.y);
+                        v[2] = sw * (f0.z - c0.z);
+                        v[3] = sw * (f0.w - c0.w);
+                        v[4] = sw * (f1.x - c1.x);
+                        v[5] = sw * (f1.y - c1.y);
+                        v[6] = sw * (f1.z - c1.z);
+                        v[7] = sw * (f1.w - c1.w);
+                    } else {
+                        float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f), f1 = f0;
+                        if (active) {
+                            f0 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c);
+                            f1 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c + 4);
+                        }
+                        v[0] = (active && c < d) ? sw * (f0.x - c0.x) : 0.f;
+                        v[1] = (active && c + 1 < d) ? sw * (f0.y - c0.y) : 0.f;
+                        v[2] = (active && c + 2 < d) ? sw * (f0.z - c0.z) : 0.f;
+                        v[3] = (active && c + 3 < d) ? sw * (f0.w - c0.w) : 0.f;
+                        v[4] = (active && c + 4 < d) ? sw * (f1.x - c1.x) : 0.f;
+                        v[5] = (active && c + 5 < d) ? sw * (f1.y - c1.y) : 0.f;
+                        v[6] = (active && c + 6 < d) ? sw * (f1.z - c1.z) : 0.f;
+                        v[7] = (active && c + 7 < d) ? sw * (f1.w - c1.w) : 0.f;
+                    }
                     const uint4 hi = make_uint4(tc::pack_bf16x2(v[0], v[1]), tc::pack_bf16x2(v[2], v[3]),
                                                 tc::pack_bf16x2(v[4], v[5]), tc::pack_bf16x2(v[6], v[7]));
                     auto lo2 = [](float a, float b, uint32_t h) {

@@ -121,28 +121,11 @@ template <> struct ThreadSums<float> {
     }
 };
 
+// Block merge of the threads' (max, S, S2), then the last block to finish
+// merges the per-block partials in the same launch and writes the FP64 words.
 template <typename T>
-__global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, int64_t n, double *out,
-                                                      Moments3 *partials, unsigned int *counter) {
-    ThreadSums<T> ts;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (sizeof(T) == 4 && (reinterpret_cast<uintptr_t>(lw) & 15) == 0) {
-        // four weights per load; the tail (< 4 weights) goes to the first threads
-        const int64_t n4 = n >> 2;
-        const float4 *lw4 = reinterpret_cast<const float4 *>(lw);
-        for (int64_t i = t0; i < n4; i += stride) {
-            const float4 q = lw4[i];
-            ts.add((T)q.x);
-            ts.add((T)q.y);
-            ts.add((T)q.z);
-            ts.add((T)q.w);
-        }
-        if (t0 < (n & 3)) ts.add(lw[(n4 << 2) + t0]);
-    } else {
-        for (int64_t i = t0; i < n; i += stride) ts.add(lw[i]);
-    }
-    Moments3 v = block_merge3<T>(ts.result());
+__device__ void summary_finish(Moments3 thread_sums, double *out, Moments3 *partials, unsigned int *counter) {
+    Moments3 v = block_merge3<T>(thread_sums);
     __shared__ bool last;
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = v;
@@ -180,6 +163,56 @@ __global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, 
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, int64_t n, double *out,
+                                                      Moments3 *partials, unsigned int *counter) {
+    ThreadSums<T> ts;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (sizeof(T) == 4 && (reinterpret_cast<uintptr_t>(lw) & 15) == 0) {
+        // four weights per load; the tail (< 4 weights) goes to the first threads
+        const int64_t n4 = n >> 2;
+        const float4 *lw4 = reinterpret_cast<const float4 *>(lw);
+        for (int64_t i = t0; i < n4; i += stride) {
+            const float4 q = lw4[i];
+            ts.add((T)q.x);
+            ts.add((T)q.y);
+            ts.add((T)q.z);
+            ts.add((T)q.w);
+        }
+        if (t0 < (n & 3)) ts.add(lw[(n4 << 2) + t0]);
+    } else {
+        for (int64_t i = t0; i < n; i += stride) ts.add(lw[i]);
+    }
+    summary_finish<T>(ts.result(), out, partials, counter);
+}
+
+// AMIS log weights of rounds 1..t and their summary in one pass
+// (_form_amis_logweights_kernel!, src/amis_execution.jl:107-134, then
+// _logweight_summary): logw_i = logtarget_i - (lognum_i - logtotal) for
+// round_ids[i] != 0, recording invalid weights; only the weights written
+// enter the summary.
+template <typename T>
+__global__ void __launch_bounds__(256) form_summary_kernel(const T *__restrict__ lt, const T *__restrict__ lnum,
+                                                           const int64_t *__restrict__ round_ids, T logtotal,
+                                                           int64_t n, T *__restrict__ lw, uint64_t *failures,
+                                                           double *out, Moments3 *partials, unsigned int *counter) {
+    ThreadSums<T> ts;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (round_ids && round_ids[i] == 0) continue;
+        T v;
+        const uint16_t r = subtract_logweight(lt[i], lnum[i] - logtotal, &v);
+        if (r) {
+            record_failure(failures, i + 1, 0, r);
+        } else {
+            lw[i] = v;
+            ts.add(v);
+        }
+    }
+    summary_finish<T>(ts.result(), out, partials, counter);
+}
+
 static int summary_blocks(int64_t n) {
     int64_t b = (n + 256 * 16 - 1) / (256 * 16);
     if (b > kSMs * 8) b = kSMs * 8;
@@ -214,6 +247,26 @@ int logweight_summary(const void *lw, int64_t n, int dtype, double *out, void *w
                       cudaStream_t stream) {
     if (ws_bytes < reduce_workspace_bytes(n)) return ISSM_E_WORKSPACE;
     return summary_launch(lw, n, dtype, out, ws, stream);
+}
+
+int amis_form_summary(const void *lt, const void *lnum, const int64_t *round_ids, double logtotal, int64_t n,
+                      int dtype, void *lw, uint64_t *failures, double *out, void *ws, size_t ws_bytes,
+                      cudaStream_t stream) {
+    if (ws_bytes < reduce_workspace_bytes(n)) return ISSM_E_WORKSPACE;
+    unsigned int *counter = (unsigned int *)ws;
+    Moments3 *partials = (Moments3 *)((char *)ws + 256);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), stream);
+    if (e != cudaSuccess) return (int)e;
+    const int blocks = summary_blocks(n);
+    if (dtype == ISSM_F32)
+        { form_summary_kernel<float><<<blocks, 256, 0, stream>>>((const float *)lt, (const float *)lnum, round_ids,
+                                                               (float)logtotal, n, (float *)lw, failures, out,
+                                                               partials, counter); note_launch(); }
+    else
+        { form_summary_kernel<double><<<blocks, 256, 0, stream>>>((const double *)lt, (const double *)lnum,
+                                                                round_ids, logtotal, n, (double *)lw, failures,
+                                                                out, partials, counter); note_launch(); }
+    return (int)cudaGetLastError();
 }
 
 template <typename T>

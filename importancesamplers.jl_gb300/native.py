@@ -79,6 +79,7 @@ SIGNATURES = [
     ("issm_check_target_values", C.c_int, [_p, _i64, _i32, _p, _p, _i64, _p]),
     ("issm_amis_append", C.c_int, [_bank, _i32, _p, _p, _i64, _p, _p, _i32, _p]),
     ("issm_amis_form", C.c_int, [_p, _p, _p, _d, _i64, _i32, _p, _p, _p]),
+    ("issm_amis_form_summary", C.c_int, [_p, _p, _p, _d, _i64, _i32, _p, _p, _p, _p, _sz, _p]),
     ("issm_reduce_workspace_bytes", _sz, [_i64]),
     ("issm_logweight_summary", C.c_int, [_p, _i64, _i32, _p, _p, _sz, _p]),
     ("issm_normalize", C.c_int, [_p, _i64, _i32, _p, _p, _p]),

@@ -155,6 +155,17 @@ def amis_form(logtargets, lognum, logtotal, logweights, round_ids=None, failures
     return logweights
 
 
+def amis_form_summary(logtargets, lognum, logtotal, logweights, out, round_ids=None, failures=None):
+    """amis_form and logweight_summary in one pass (summary of the weights written)."""
+    n = logtargets.numel()
+    nb = native.lib().issm_reduce_workspace_bytes(n)
+    ws = native.workspace(nb, logtargets.device, "reduce")
+    native.call("issm_amis_form_summary", native.ptr(logtargets), native.ptr(lognum), native.ptr(round_ids),
+                float(logtotal), n, _dt(logtargets), native.ptr(logweights), native.ptr(failures), native.ptr(out),
+                native.ptr(ws), ws.numel(), _s())
+    return out
+
+
 def logweight_summary(logweights, out=None):
     n = logweights.numel()
     out = torch.empty(3, dtype=torch.float64, device=logweights.device) if out is None else out

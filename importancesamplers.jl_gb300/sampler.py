@@ -369,12 +369,12 @@ def _moment_body(s, is_npmc):
             with _Span(s, "mixture_new", n_new * (d + 1) * es + (t + 1) * d * d * es):
                 ops.mixture_logdensity(h, den, x_new, fixed_slot=t, failures=fail, out=s.lognum[n_old:n_tot],
                                        bank_ref=view, precision=s.precision)
-            with _Span(s, "form_summary", n_tot * 4 * es):
-                ops.amis_form(s.logtargets[:n_tot], s.lognum[:n_tot], math.log(n_tot), s.logweights[:n_tot],
-                              round_ids=s.round_ids[:n_tot], failures=fail)
+            with _Span(s, "form_summary", n_tot * (3 * es + 8)):
+                fit_summary = ops.amis_form_summary(s.logtargets[:n_tot], s.lognum[:n_tot], math.log(n_tot),
+                                                    s.logweights[:n_tot], s.summaries[t],
+                                                    round_ids=s.round_ids[:n_tot], failures=fail)
                 lw_fit = s.logweights[:n_tot]
                 x_fit = s.samples[:n_tot]
-                fit_summary = ops.logweight_summary(lw_fit, out=s.summaries[t])
         with _Span(s, "moments", 2 * x_fit.shape[0] * (d + 1) * es):
             s.shift.copy_(h.locations[t])
             ops.weighted_moments(x_fit, lw_fit, fit_summary, s.shift, s.mean, s.cov, precision=s.precision)

@@ -271,6 +271,15 @@ int issm_amis_form(const void *logtargets, const void *lognumerators,
                    int32_t dtype, void *logweights, uint64_t *failures,
                    issm_stream_t stream);
 
+/* issm_amis_form and issm_logweight_summary in one pass: the summary covers
+ * the log weights this call writes (samples with round_ids[i] != 0 and a
+ * valid weight). workspace: issm_reduce_workspace_bytes(n) bytes. */
+int issm_amis_form_summary(const void *logtargets, const void *lognumerators,
+                           const int64_t *round_ids, double logtotal, int64_t n,
+                           int32_t dtype, void *logweights, uint64_t *failures,
+                           double *summary, void *workspace,
+                           size_t workspace_bytes, issm_stream_t stream);
+
 /* ---- log-weight reductions (src/execution.jl:103-186, src/results.jl:6-36,560-626) */
 /* out[0..2] = (max, sum exp(l-max), sum exp(2(l-max))) in FP64 over n log
  * weights, merged as _merge_logweight_moments. out is 3 FP64 device words.
