@@ -212,47 +212,108 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
     }
     for (int c = threadIdx.x; c < d; c += blockDim.x) A[c + c * d] += ridge;
     __syncthreads();
-    // Right-looking LDL^T factorisation, A = L D L^T with unit lower L: per
-    // column j, warp 0 forms 1/d_j (four FP64 instructions after an FP32 seed)
-    // and scales the column below the pivot, keeping the unscaled column in
-    // u; then all eight warps apply the rank-1 update A_ik -= l_ij u_k to the
-    // trailing lower triangle, mapped onto column pairs (k, m-1-k) so every
-    // thread gets the same number of elements. The Cholesky factor is
-    // L diag(sqrt(d)), formed afterwards in parallel; its pivots fail exactly
-    // when Cholesky's would (d_j <= 0 or not finite).
-    __shared__ double s_u[64];
+    // Blocked right-looking LDL^T factorisation, A = L D L^T with unit lower
+    // L, in 8-column panels. Each FP64 instruction holds a warp's FP64 pipe for
+    // about 64 cycles on this GPU, so the work is arranged around that:
+    //  * warp 0 factors the 8 x 8 diagonal block column by column; the only
+    //    sequential FP64 chain is 1/d_j (an FP32 seed and two Newton steps);
+    //  * one thread per row below the block solves its panel row
+    //    (l_ic = (a_ic - sum_q l_iq d_q l_cq) / d_c);
+    //  * all warps apply the rank-8 trailing update, each thread holding up to
+    //    eight independent elements of the trailing lower triangle (column
+    //    pairs (k, m-1-k) balance the work), so the pipe, not latency, bounds it.
+    // The Cholesky factor is L diag(sqrt(d)), formed afterwards in parallel;
+    // the pivots fail exactly when Cholesky's would (d_j <= 0 or not finite).
     __shared__ double s_dg[64];
+    __shared__ double s_rinv[8];
+    __shared__ double s_w[8][64];  // w_c[i] = l_ic d_c of the current panel
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int j = 0; j < d; ++j) {
+    for (int kb = 0; kb < d; kb += 8) {
+        const int nb = min(8, d - kb);
         if (warp == 0) {
-            const double dj = A[j + j * d];
-            const double rj = rcp_nr(dj);
-            if (lane == 0) {
-                if (!(dj > 0.0) || !isfinite(dj)) bad = 1;
-                s_dg[j] = dj;
-            }
-            for (int i = j + 1 + lane; i < d; i += 32) {
-                const double u = A[i + j * d];
-                s_u[i] = u;
-                A[i + j * d] = u * rj;
+            for (int j = kb; j < kb + nb; ++j) {
+                const double dj = A[j + j * d];
+                const double rj = rcp_nr(dj);
+                if (lane == 0) {
+                    if (!(dj > 0.0) || !isfinite(dj)) bad = 1;
+                    s_dg[j] = dj;
+                    s_rinv[j - kb] = rj;
+                }
+                const int rows = kb + nb - 1 - j;
+                // lanes 0..rows-1 scale column j inside the block; w keeps the unscaled value
+                double u = 0.0;
+                if (lane < rows) {
+                    u = A[(j + 1 + lane) + j * d];
+                    s_w[j - kb][j + 1 + lane] = u;
+                    A[(j + 1 + lane) + j * d] = u * rj;
+                }
+                __syncwarp();
+                // rank-1 update of the rest of the block (at most 28 elements)
+                if (lane < rows * (rows + 1) / 2) {
+                    int c = 0, t = lane;
+                    while (t >= rows - c) { t -= rows - c; ++c; }
+                    const int i = c + t;
+                    A[(j + 1 + i) + (j + 1 + c) * d] -= A[(j + 1 + i) + j * d] * s_w[j - kb][j + 1 + c];
+                }
+                __syncwarp();
             }
         }
         __syncthreads();
-        const int m = d - j - 1, base = j + 1;
-        const int half = (m + 1) >> 1;
-        for (int e = threadIdx.x; e < half * (m + 1); e += blockDim.x) {
-            const int c = e / (m + 1), r = e - c * (m + 1);
-            int i, k;
-            if (r < m - c) {
-                k = c;
-                i = c + r;
-            } else {
-                k = m - 1 - c;
-                i = k + (r - (m - c));
-                if (k == c || i >= m) continue;
+        const int base = kb + nb, m = d - base;
+        if (m <= 0) break;
+        // panel: one thread per row i below the block
+        for (int r = threadIdx.x; r < m; r += blockDim.x) {
+            const int i = base + r;
+            double w[8];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+                if (c < nb) {
+                    double v = A[i + (kb + c) * d];
+#pragma unroll
+                    for (int q = 0; q < 8; ++q)
+                        if (q < c) v = fma(-w[q], A[(kb + c) + (kb + q) * d], v);
+                    w[c] = v;                            // l_ic d_c
+                    A[i + (kb + c) * d] = v * s_rinv[c];  // l_ic
+                    s_w[c][i] = v;
+                } else {
+                    w[c] = 0.0;
+                }
             }
-            A[(base + i) + (base + k) * d] -= A[(base + i) + j * d] * s_u[base + k];
         }
+        __syncthreads();
+        // rank-nb trailing update: A_ik -= sum_c l_ic w_c[k], kb+nb <= k <= i < d
+        const int half = (m + 1) >> 1, total = half * (m + 1);
+        int ei[8], ek[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            ei[t] = -1;
+            ek[t] = 0;
+            const int e = threadIdx.x + t * blockDim.x;
+            if (e < total) {
+                const int c = e / (m + 1), r = e - c * (m + 1);
+                if (r < m - c) {
+                    ek[t] = c;
+                    ei[t] = c + r;
+                } else {
+                    const int k2 = m - 1 - c;
+                    if (k2 != c) {
+                        ek[t] = k2;
+                        ei[t] = k2 + (r - (m - c));
+                    }
+                }
+            }
+        }
+        double acc[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) acc[t] = ei[t] >= 0 ? A[(base + ei[t]) + (base + ek[t]) * d] : 0.0;
+        for (int c = 0; c < nb; ++c) {
+#pragma unroll
+            for (int t = 0; t < 8; ++t)
+                if (ei[t] >= 0) acc[t] = fma(-A[(base + ei[t]) + (kb + c) * d], s_w[c][base + ek[t]], acc[t]);
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t)
+            if (ei[t] >= 0) A[(base + ei[t]) + (base + ek[t]) * d] = acc[t];
         __syncthreads();
     }
     // column scales sqrt(d_j) times the Student-t factor; the factor is L s

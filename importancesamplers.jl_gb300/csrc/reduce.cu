@@ -199,16 +199,43 @@ __global__ void __launch_bounds__(256) form_summary_kernel(const T *__restrict__
                                                            double *out, Moments3 *partials, unsigned int *counter) {
     ThreadSums<T> ts;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        if (round_ids && round_ids[i] == 0) continue;
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    auto one = [&](int64_t i, T target, T num) {
         T v;
-        const uint16_t r = subtract_logweight(lt[i], lnum[i] - logtotal, &v);
+        const uint16_t r = subtract_logweight(target, num - logtotal, &v);
         if (r) {
             record_failure(failures, i + 1, 0, r);
         } else {
             lw[i] = v;
             ts.add(v);
         }
+    };
+    const bool vec = sizeof(T) == 4 && ((reinterpret_cast<uintptr_t>(lt) | reinterpret_cast<uintptr_t>(lnum) |
+                                         reinterpret_cast<uintptr_t>(lw) | reinterpret_cast<uintptr_t>(round_ids)) & 15) == 0;
+    int64_t done = 0;
+    if (vec) {
+        // four samples per iteration: 16-byte loads of both inputs and the round ids
+        const int64_t n4 = n >> 2;
+        for (int64_t q = t0; q < n4; q += stride) {
+            const float4 a = reinterpret_cast<const float4 *>(lt)[q];
+            const float4 b = reinterpret_cast<const float4 *>(lnum)[q];
+            bool keep[4] = {true, true, true, true};
+            if (round_ids) {
+                const longlong2 r0 = reinterpret_cast<const longlong2 *>(round_ids)[2 * q];
+                const longlong2 r1 = reinterpret_cast<const longlong2 *>(round_ids)[2 * q + 1];
+                keep[0] = r0.x != 0; keep[1] = r0.y != 0; keep[2] = r1.x != 0; keep[3] = r1.y != 0;
+            }
+            const int64_t i = q << 2;
+            if (keep[0]) one(i, (T)a.x, (T)b.x);
+            if (keep[1]) one(i + 1, (T)a.y, (T)b.y);
+            if (keep[2]) one(i + 2, (T)a.z, (T)b.z);
+            if (keep[3]) one(i + 3, (T)a.w, (T)b.w);
+        }
+        done = n4 << 2;
+    }
+    for (int64_t i = done + t0; i < n; i += stride) {
+        if (round_ids && round_ids[i] == 0) continue;
+        one(i, lt[i], lnum[i]);
     }
     summary_finish<T>(ts.result(), out, partials, counter);
 }
