@@ -165,104 +165,140 @@ __device__ __forceinline__ double rcp_nr(double a) {
     return fma(r, e, r);
 }
 
+template <typename V> __device__ __forceinline__ V warp_sum_all(V v) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+// Candidate fit of one moment round (src/adaptive_gaussian_execution.jl:283-528):
+// cov + ridge I with ridge = reg tr(L_prev L_prev^T) c_nu / d (reg = sqrt(eps(T)),
+// c_nu = nu/(nu-2) for Student-t, 1 for Gaussian; when that product is not
+// finite the ridge is summed from the scaled factor, as the reference does),
+// an FP64 factorisation, Student-t scaling of the factor by sqrt((nu-2)/nu),
+// rounding to T, the validity rule and the lognormalizer, plus (optionally)
+// the FP32 inverse of the stored factor for the tensor-core forms.
+//
+// The factorisation is a blocked right-looking LDL^T, A = L D L^T with unit
+// lower L, in 8-column panels; the Cholesky factor is L diag(sqrt(d)). Each
+// FP64 instruction holds a warp's FP64 pipe for about 64 cycles on this GPU
+// (and takes as long to complete), so:
+//  * the sequential chain per column is only 1/d_j (an FP32 seed and two
+//    Newton steps), run by warp 0 on the 8 x 8 diagonal block;
+//  * one thread per row solves its panel row, l_ic = (a_ic - sum_q l_iq d_q
+//    l_cq) / d_c;
+//  * while warp 0 updates and factors the next diagonal block (lookahead),
+//    warps 1..7 apply the rank-8 update to the rest of the trailing lower
+//    triangle, each thread holding up to eight independent elements (column
+//    pairs (k, m-1-k) balance the work), so the pipe, not latency, bounds it.
+// The pivots fail exactly when Cholesky's would (d_j <= 0 or not finite).
 template <typename T>
 __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restrict__ mean,
                                                          const double *__restrict__ cov, int d,
-                                                         const T *__restrict__ prev, double dof, double logconst,
-                                                         double reg, T *out_loc, T *out_factor, T *out_lognorm,
+                                                         const T *__restrict__ prev, double ridge_scale,
+                                                         double ridge_fallback_scale, double lognorm_const,
+                                                         double tscale, T *out_loc, T *out_factor, T *out_lognorm,
                                                          uint64_t *failures, int64_t failure_index,
                                                          float *out_inverse) {
     extern __shared__ __align__(16) double A[];  // d x d column-major
-    __shared__ double red[256];
-    __shared__ int bad;
-    const double mult = dof > 0.0 ? dof / (dof - 2.0) : 1.0;
-    // tr(L_prev L_prev^T) accumulated in the factor's precision, as the
-    // reference does (_factor_scale_aware_ridge), then merged in FP64
-    T tr = T(0);
-    for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
-        const int r = e % d, c = e / d;
-        if (r >= c) { const T v = prev[e]; tr += v * v; }
-        A[e] = cov[e];
-    }
-    red[threadIdx.x] = (double)tr;
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
-    for (int off = 128; off > 0; off >>= 1) {
-        if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
-        __syncthreads();
-    }
-    double ridge = reg * (red[0] * mult) / (double)d;
-    __syncthreads();
-    if (!isfinite(ridge)) {
-        double acc = 0.0;
-        if (reg != 0.0) {
-            const double sc = sqrt(reg) * sqrt(mult / (double)d);
-            for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
-                const int r = e % d, c = e / d;
-                if (r >= c) { const double v = (double)prev[e] * sc; acc += v * v; }
-            }
-        }
-        red[threadIdx.x] = acc;
-        __syncthreads();
-        for (int off = 128; off > 0; off >>= 1) {
-            if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
-            __syncthreads();
-        }
-        ridge = red[0];
-    }
-    for (int c = threadIdx.x; c < d; c += blockDim.x) A[c + c * d] += ridge;
-    __syncthreads();
-    // Blocked right-looking LDL^T factorisation, A = L D L^T with unit lower
-    // L, in 8-column panels. Each FP64 instruction holds a warp's FP64 pipe for
-    // about 64 cycles on this GPU, so the work is arranged around that:
-    //  * warp 0 factors the 8 x 8 diagonal block column by column; the only
-    //    sequential FP64 chain is 1/d_j (an FP32 seed and two Newton steps);
-    //  * one thread per row below the block solves its panel row
-    //    (l_ic = (a_ic - sum_q l_iq d_q l_cq) / d_c);
-    //  * all warps apply the rank-8 trailing update, each thread holding up to
-    //    eight independent elements of the trailing lower triangle (column
-    //    pairs (k, m-1-k) balance the work), so the pipe, not latency, bounds it.
-    // The Cholesky factor is L diag(sqrt(d)), formed afterwards in parallel;
-    // the pivots fail exactly when Cholesky's would (d_j <= 0 or not finite).
+    __shared__ double s_red[8];
+    __shared__ double s_ridge;
     __shared__ double s_dg[64];
     __shared__ double s_rinv[8];
-    __shared__ double s_w[8][64];  // w_c[i] = l_ic d_c of the current panel
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int kb = 0; kb < d; kb += 8) {
-        const int nb = min(8, d - kb);
-        if (warp == 0) {
-            for (int j = kb; j < kb + nb; ++j) {
-                const double dj = A[j + j * d];
-                const double rj = rcp_nr(dj);
-                if (lane == 0) {
-                    if (!(dj > 0.0) || !isfinite(dj)) bad = 1;
-                    s_dg[j] = dj;
-                    s_rinv[j - kb] = rj;
-                }
-                const int rows = kb + nb - 1 - j;
-                // lanes 0..rows-1 scale column j inside the block; w keeps the unscaled value
-                double u = 0.0;
-                if (lane < rows) {
-                    u = A[(j + 1 + lane) + j * d];
-                    s_w[j - kb][j + 1 + lane] = u;
-                    A[(j + 1 + lane) + j * d] = u * rj;
-                }
-                __syncwarp();
-                // rank-1 update of the rest of the block (at most 28 elements)
-                if (lane < rows * (rows + 1) / 2) {
-                    int c = 0, t = lane;
-                    while (t >= rows - c) { t -= rows - c; ++c; }
-                    const int i = c + t;
-                    A[(j + 1 + i) + (j + 1 + c) * d] -= A[(j + 1 + i) + j * d] * s_w[j - kb][j + 1 + c];
-                }
-                __syncwarp();
+    __shared__ double s_w[2][8][64];  // w_c[i] = l_ic d_c of a panel (double-buffered by panel)
+    __shared__ double s_scale[64];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int dd = d * d;
+    // ---- stage the covariance with all loads in flight; trace of the previous factor ----
+    T tr = T(0);
+    for (int e0 = tid; e0 < dd; e0 += 256 * 8) {
+        double v[8];
+        T pv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int e = e0 + 256 * u;
+            v[u] = e < dd ? cov[e] : 0.0;
+            pv[u] = e < dd ? prev[e] : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int e = e0 + 256 * u;
+            if (e < dd) {
+                A[e] = v[u];
+                if (e % d >= e / d) tr += pv[u] * pv[u];  // lower triangle, in T as the reference sums it
             }
         }
+    }
+    tr = warp_sum_all(tr);
+    if (lane == 0) s_red[warp] = (double)tr;
+    __syncthreads();
+    if (tid == 0) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += s_red[w];
+        s_ridge = t * ridge_scale;
+    }
+    __syncthreads();
+    double ridge = s_ridge;
+    if (!isfinite(ridge)) {
+        // the scaled-factor route of _factor_scale_aware_ridge (rare)
+        double acc = 0.0;
+        if (ridge_fallback_scale != 0.0)
+            for (int e = tid; e < dd; e += 256)
+                if (e % d >= e / d) {
+                    const double v = (double)prev[e] * ridge_fallback_scale;
+                    acc += v * v;
+                }
+        acc = warp_sum_all(acc);
         __syncthreads();
-        const int base = kb + nb, m = d - base;
+        if (lane == 0) s_red[warp] = acc;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0.0;
+            for (int w = 0; w < 8; ++w) t += s_red[w];
+            s_ridge = t;
+        }
+        __syncthreads();
+        ridge = s_ridge;
+    }
+    for (int c = tid; c < d; c += 256) A[c + c * d] += ridge;
+    __syncthreads();
+
+    // ---- blocked LDL^T ----
+    auto factor_diag = [&](int kb, int nb, double (*w)[64]) {  // warp 0
+        for (int j = kb; j < kb + nb; ++j) {
+            const double dj = A[j + j * d];
+            const double rj = rcp_nr(dj);
+            if (lane == 0) {
+                s_dg[j] = dj;
+                s_rinv[j - kb] = rj;
+            }
+            const int rows = kb + nb - 1 - j;
+            if (lane < rows) {
+                const double u = A[(j + 1 + lane) + j * d];
+                w[j - kb][j + 1 + lane] = u;
+                A[(j + 1 + lane) + j * d] = u * rj;
+            }
+            __syncwarp();
+            if (lane < rows * (rows + 1) / 2) {
+                int c = 0, t = lane;
+                while (t >= rows - c) {
+                    t -= rows - c;
+                    ++c;
+                }
+                const int i = c + t;
+                A[(j + 1 + i) + (j + 1 + c) * d] -= A[(j + 1 + i) + j * d] * w[j - kb][j + 1 + c];
+            }
+            __syncwarp();
+        }
+    };
+    if (warp == 0) factor_diag(0, min(8, d), s_w[0]);
+    __syncthreads();
+    for (int kb = 0; kb < d; kb += 8) {
+        const int nb = min(8, d - kb), base = kb + nb, m = d - base;
         if (m <= 0) break;
-        // panel: one thread per row i below the block
-        for (int r = threadIdx.x; r < m; r += blockDim.x) {
+        double (*wc)[64] = s_w[(kb >> 3) & 1];
+        double (*wn)[64] = s_w[((kb >> 3) + 1) & 1];
+        // panel: one thread per row i below the diagonal block
+        for (int r = tid; r < m; r += 256) {
             const int i = base + r;
             double w[8];
 #pragma unroll
@@ -274,90 +310,110 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
                         if (q < c) v = fma(-w[q], A[(kb + c) + (kb + q) * d], v);
                     w[c] = v;                            // l_ic d_c
                     A[i + (kb + c) * d] = v * s_rinv[c];  // l_ic
-                    s_w[c][i] = v;
+                    wc[c][i] = v;
                 } else {
                     w[c] = 0.0;
                 }
             }
         }
         __syncthreads();
-        // rank-nb trailing update: A_ik -= sum_c l_ic w_c[k], kb+nb <= k <= i < d
-        const int half = (m + 1) >> 1, total = half * (m + 1);
-        int ei[8], ek[8];
+        const int nbn = min(8, m);
+        if (warp == 0) {
+            // lookahead: the next diagonal block gets its rank-nb update first, then is factored
+            for (int e = lane; e < nbn * (nbn + 1) / 2; e += 32) {
+                int c = 0, t = e;
+                while (t >= nbn - c) {
+                    t -= nbn - c;
+                    ++c;
+                }
+                const int i = c + t;
+                double acc = A[(base + i) + (base + c) * d];
+                for (int q = 0; q < nb; ++q) acc = fma(-A[(base + i) + (kb + q) * d], wc[q][base + c], acc);
+                A[(base + i) + (base + c) * d] = acc;
+            }
+            __syncwarp();
+            factor_diag(base, nbn, wn);
+        } else {
+            // rank-nb update of the trailing lower triangle outside the next diagonal block
+            const int wt = tid - 32, half = (m + 1) >> 1, total = half * (m + 1);
+            int ei[8], ek[8];
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            ei[t] = -1;
-            ek[t] = 0;
-            const int e = threadIdx.x + t * blockDim.x;
-            if (e < total) {
-                const int c = e / (m + 1), r = e - c * (m + 1);
-                if (r < m - c) {
-                    ek[t] = c;
-                    ei[t] = c + r;
-                } else {
-                    const int k2 = m - 1 - c;
-                    if (k2 != c) {
-                        ek[t] = k2;
-                        ei[t] = k2 + (r - (m - c));
+            for (int t = 0; t < 8; ++t) {
+                ei[t] = -1;
+                ek[t] = 0;
+                const int e = wt + t * 224;
+                if (e < total) {
+                    const int c = e / (m + 1), r = e - c * (m + 1);
+                    int i = -1, k = 0;
+                    if (r < m - c) {
+                        k = c;
+                        i = c + r;
+                    } else {
+                        const int k2 = m - 1 - c;
+                        if (k2 != c) {
+                            k = k2;
+                            i = k2 + (r - (m - c));
+                        }
+                    }
+                    if (i >= 0 && !(i < nbn && k < nbn)) {
+                        ei[t] = i;
+                        ek[t] = k;
                     }
                 }
             }
-        }
-        double acc[8];
+            double acc[8];
 #pragma unroll
-        for (int t = 0; t < 8; ++t) acc[t] = ei[t] >= 0 ? A[(base + ei[t]) + (base + ek[t]) * d] : 0.0;
-        for (int c = 0; c < nb; ++c) {
+            for (int t = 0; t < 8; ++t) acc[t] = ei[t] >= 0 ? A[(base + ei[t]) + (base + ek[t]) * d] : 0.0;
+            for (int c = 0; c < nb; ++c) {
+#pragma unroll
+                for (int t = 0; t < 8; ++t)
+                    if (ei[t] >= 0) acc[t] = fma(-A[(base + ei[t]) + (kb + c) * d], wc[c][base + ek[t]], acc[t]);
+            }
 #pragma unroll
             for (int t = 0; t < 8; ++t)
-                if (ei[t] >= 0) acc[t] = fma(-A[(base + ei[t]) + (kb + c) * d], s_w[c][base + ek[t]], acc[t]);
+                if (ei[t] >= 0) A[(base + ei[t]) + (base + ek[t]) * d] = acc[t];
         }
-#pragma unroll
-        for (int t = 0; t < 8; ++t)
-            if (ei[t] >= 0) A[(base + ei[t]) + (base + ek[t]) * d] = acc[t];
         __syncthreads();
     }
-    // column scales sqrt(d_j) times the Student-t factor; the factor is L s
-    __shared__ double s_scale[64];
-    const double f = dof > 0.0 ? sqrt(1.0 / mult) : 1.0;
-    for (int c = threadIdx.x; c < d; c += blockDim.x) s_scale[c] = sqrt(s_dg[c]) * f;
-    __syncthreads();
-    // rounding to T, validity and log|L| as block reductions
-    double logdet = 0.0;
+
+    // ---- factor = L diag(sqrt(d)) * Student-t scale, rounded to T ----
     int invalid = 0;
-    // the FP32 copy of the stored factor for the inverse (after A in shared memory)
+    for (int c = tid; c < d; c += 256) {
+        const double dg = s_dg[c];
+        invalid |= !(dg > 0.0) || !isfinite(dg);
+        s_scale[c] = sqrt(dg) * tscale;
+    }
+    __syncthreads();
     constexpr int LDI = 65;
-    float *Lf = reinterpret_cast<float *>(A + d * d);
-    for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+    float *Lf = reinterpret_cast<float *>(A + dd);  // FP32 copy of the stored factor for the inverse
+    for (int e = tid; e < dd; e += 256) {
         const int r = e % d, c = e / d;
         const T v = r > c ? (T)(A[e] * s_scale[c]) : r == c ? (T)s_scale[c] : T(0);
         out_factor[e] = v;
         if (out_inverse != nullptr) Lf[r * LDI + c] = (float)v;
-        if (r >= c) {
-            invalid |= !isfinite(v);
-            if (r == c) {
-                invalid |= !(v > T(0));
-                // log|L_jj| in the factor's own precision, summed in FP64
-                logdet += (double)dlog(fabs(v));
-            }
-        }
+        if (r > c) invalid |= !isfinite(v);
     }
-    for (int c = threadIdx.x; c < d; c += blockDim.x) {
+    // log|L_jj| in the factor's own precision, summed across lanes then in FP64
+    T lg = T(0);
+    for (int c = tid; c < d; c += 256) {
+        const T v = (T)s_scale[c];
+        invalid |= !isfinite(v) || !(v > T(0));
+        lg += dlog(fabs(v));
+    }
+    for (int c = tid; c < d; c += 256) {
         const T v = (T)mean[c];
         out_loc[c] = v;
-        invalid |= !isfinite((double)v);
+        invalid |= !isfinite(v);
     }
-    red[threadIdx.x] = logdet;
+    lg = warp_sum_all(lg);
+    if (lane == 0) s_red[warp] = (double)lg;
     invalid = __syncthreads_or(invalid);
-    for (int off = 128; off > 0; off >>= 1) {
-        if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const double logabsdet = red[0];
-        const double ln = dof > 0.0 ? logconst - logabsdet
-                                    : -0.5 * (double)d * log(2.0 * 3.14159265358979323846) - logabsdet;
+    if (tid == 0) {
+        double logabsdet = 0.0;
+        for (int w = 0; w < 8; ++w) logabsdet += s_red[w];
+        const double ln = lognorm_const - logabsdet;
         *out_lognorm = (T)ln;
-        const bool valid = !bad && !invalid && isfinite((double)(T)ln);
+        const bool valid = !invalid && isfinite((T)ln);
         if (!valid) record_failure(failures, failure_index, 0, ISSM_REASON_MOMENT_FIT_INVALID);
     }
     // inverse factor for the tensor-core forms: W = (stored factor)^-1 in
@@ -367,7 +423,7 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
         __syncthreads();
         invert_lower_f32(Lf, Wf, d, LDI);
         const int DP = d <= 16 ? 16 : d <= 32 ? 32 : 64;
-        for (int e = threadIdx.x; e < DP * DP; e += blockDim.x) {
+        for (int e = tid; e < DP * DP; e += 256) {
             const int j = e / DP, c = e % DP;
             out_inverse[e] = (j < d && c < d) ? Wf[j * LDI + c] : 0.f;
         }
@@ -385,16 +441,24 @@ int fit_factor(const double *mean, const double *cov, int d, const void *prev, d
                                                            : (const void *)fit_factor_kernel<double>);
         if (e) return e;
     }
+    // scalar constants formed once on the host
+    const double mult = dof > 0.0 ? dof / (dof - 2.0) : 1.0;
+    const double reg = dtype == ISSM_F32 ? sqrt((double)FLT_EPSILON) : sqrt(DBL_EPSILON);
+    const double ridge_scale = reg * mult / (double)d;
+    const double ridge_fallback = reg != 0.0 ? sqrt(reg) * sqrt(mult / (double)d) : 0.0;
+    const double lognorm_const = dof > 0.0 ? logconst : -0.5 * (double)d * log(2.0 * 3.14159265358979323846);
+    const double tscale = dof > 0.0 ? sqrt(1.0 / mult) : 1.0;
     if (dtype == ISSM_F32) {
-        const double reg = sqrt((double)FLT_EPSILON);
-        { fit_factor_kernel<float><<<1, 256, smem, stream>>>(mean, cov, d, (const float *)prev, dof, logconst, reg,
-                                                           (float *)out_loc, (float *)out_factor,
-                                                           (float *)out_lognorm, failures, failure_index, out_inverse); note_launch(); }
+        { fit_factor_kernel<float><<<1, 256, smem, stream>>>(mean, cov, d, (const float *)prev, ridge_scale,
+                                                           ridge_fallback, lognorm_const, tscale, (float *)out_loc,
+                                                           (float *)out_factor, (float *)out_lognorm, failures,
+                                                           failure_index, out_inverse); note_launch(); }
     } else {
-        const double reg = sqrt(DBL_EPSILON);
-        { fit_factor_kernel<double><<<1, 256, smem, stream>>>(mean, cov, d, (const double *)prev, dof, logconst,
-                                                            reg, (double *)out_loc, (double *)out_factor,
-                                                            (double *)out_lognorm, failures, failure_index, out_inverse); note_launch(); }
+        { fit_factor_kernel<double><<<1, 256, smem, stream>>>(mean, cov, d, (const double *)prev, ridge_scale,
+                                                            ridge_fallback, lognorm_const, tscale,
+                                                            (double *)out_loc, (double *)out_factor,
+                                                            (double *)out_lognorm, failures, failure_index,
+                                                            out_inverse); note_launch(); }
     }
     return (int)cudaGetLastError();
 }
