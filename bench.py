@@ -3,7 +3,11 @@ workload (40 rounds x 50,000 samples, 2,000,000 retained weighted samples),
 through the public sampler API, with the log-Z and posterior-mean error
 reported beside the rate.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp32|tf32|bf16] [--impl gb300|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision bf16|tf32|fp32] [--impl gb300|reference]
+
+The headline line is the BF16 x3 tensor-core form (Mahalanobis contraction and
+moments on tcgen05, FP64 Cholesky and log-Z sums); "forms" reports the plain
+FP32 form on the same GPU and workload beside it.
 
 One step = one complete AMIS run (draw, target, retrospective
 balance-heuristic denominators, weights, summaries, weighted moments and FP64
@@ -156,6 +160,14 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+# DRAM bytes per sample of the streaming kernels, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on the 12-round case of this
+# workload and divided by the samples each launch processed: the append pass
+# (550,000 retained samples) and the moments pass (600,000).
+TRAFFIC_PER_SAMPLE = {"amis_append": 268.0, "moments": 265.7}
+SPAN_SAMPLES = {"amis_append": lambda t, n: t * n, "moments": lambda t, n: (t + 1) * n}
+
+
 def run_gb300(args):
     import torch
 
@@ -171,53 +183,62 @@ def run_gb300(args):
 
     issm = ge.load_package()
     issm.native.require()
-    precision = {"fp32": issm.native.PREC_NATIVE, "tf32": issm.native.PREC_TF32,
-                 "bf16": issm.native.PREC_BF16}[args.precision]
+    codes = {"fp32": issm.native.PREC_NATIVE, "tf32": issm.native.PREC_TF32, "bf16": issm.native.PREC_BF16}
     loc, L, p_loc, p_fac = problem()
     target = issm.StudentTTarget(loc, L, DOF)
-    proposal = issm.FactorGaussian(p_loc.astype(np.float32), p_fac.astype(np.float32))
     rounds, round_size = args.rounds, args.round_size
-    alg = issm.AMIS(proposal, rounds=rounds, round_size=round_size)
-    sampler = issm.prepare_sampler(1234 + rank, target, alg, device=dev, precision=precision)
-
-    def step():
-        # each step restarts from the same initial proposal (no carried adaptation)
-        if hasattr(sampler, "initial"):
-            for dst, src in zip(sampler.committed, sampler.initial):
-                dst.copy_(src)
-        return issm.importance_sample_(sampler)
-
-    sampler.initial = tuple(t.clone() for t in sampler.committed)
-    for _ in range(max(args.warmup, 3)):
-        res = step()
-    torch.cuda.synchronize()
+    total = rounds * round_size
     barrier = (lambda: torch.distributed.barrier()) if world > 1 else (lambda: None)
     stream = torch.cuda.current_stream()
-    with ClockSampler(dev.index) as clocks:
+
+    def make(form):
+        proposal = issm.FactorGaussian(p_loc.astype(np.float32), p_fac.astype(np.float32))
+        alg = issm.AMIS(proposal, rounds=rounds, round_size=round_size)
+        smp = issm.prepare_sampler(1234 + rank, target, alg, device=dev, precision=codes[form])
+        smp.initial = tuple(t.clone() for t in smp.committed)
+
+        def step():
+            # each step restarts from the same initial proposal (no carried adaptation)
+            for dst, src in zip(smp.committed, smp.initial):
+                dst.copy_(src)
+            return issm.importance_sample_(smp)
+        return smp, step
+
+    def measure(step, steps, warmup, clocks=None):
+        for _ in range(warmup):
+            res = step()
+        torch.cuda.synchronize()
         barrier()
         torch.cuda.synchronize()
         l0 = issm.native.launches()
         start = torch.cuda.Event(enable_timing=True)
         end = torch.cuda.Event(enable_timing=True)
         start.record(stream)
-        for _ in range(args.steps):
+        for _ in range(steps):
             res = step()
         end.record(stream)
         torch.cuda.synchronize()
         barrier()
         l1 = issm.native.launches()
-    ms = start.elapsed_time(end) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    total = rounds * round_size
-    value = total * world / (ms / 1e3)
-    logz = float(res.diagnostics["round_lognormalizers"][-1])
-    post_mean = issm.mean(res).cpu().numpy()
+        ms = start.elapsed_time(end) / steps
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        logz = float(res.diagnostics["round_lognormalizers"][-1])
+        post_mean = issm.mean(res).cpu().numpy()
+        return {"ms": ms, "value": total * world / (ms / 1e3), "launches": int((l1 - l0) // steps), "logz": logz,
+                "post_mean_err": float(np.max(np.abs(post_mean - loc)))}
 
-    # per-kernel profile of one extra run (events on the launching stream)
+    sampler, step = make(args.precision)
+    warmup = max(args.warmup, 3)
+    with ClockSampler(dev.index) as clocks:
+        head = measure(step, args.steps, warmup)
+
+    # per-kernel profile of one extra run: a spin kernel first lets the host
+    # queue the whole run, so every span's events time only its kernels
     sampler.profile = []
+    torch.cuda._sleep(int(5e7))
     step()
     torch.cuda.synchronize()
     groups = {}
@@ -232,13 +253,23 @@ def run_gb300(args):
     hbm, tflops, src = read_peaks()
     achieved = (nbytes / cnt) / ((tms / cnt) / 1e3) / 1e9
     share = {k: round(v[0] / sum(x[0] for x in groups.values()), 4) for k, v in groups.items()}
+    traffic = None
+    if dominant in TRAFFIC_PER_SAMPLE:
+        samples = sum(SPAN_SAMPLES[dominant](t, round_size) for t in range(rounds) if dominant != "amis_append" or t > 0)
+        traffic = TRAFFIC_PER_SAMPLE[dominant] * samples / cnt
+
+    # the plain FP32 form (the drop-in SIMT path) on the same GPU, same seed and workload
+    forms = {}
+    if not args.quick and args.precision != "fp32":
+        _, step32 = make("fp32")
+        forms["fp32"] = measure(step32, 2, 1)
 
     # e2e: host arrays in, summaries and posterior mean out, through the public API
     def e2e_step():
         tgt = issm.StudentTTarget(loc, L, DOF)
         prop = issm.FactorGaussian(p_loc.astype(np.float32), p_fac.astype(np.float32))
         smp = issm.prepare_sampler(99 + rank, tgt, issm.AMIS(prop, rounds=rounds, round_size=round_size),
-                                   device=dev, precision=precision)
+                                   device=dev, precision=codes[args.precision])
         r = issm.importance_sample_(smp)
         pm = issm.mean(r).cpu().numpy()
         return r, pm
@@ -270,25 +301,30 @@ def run_gb300(args):
     if not args.quick:
         cpu_value, cores, _ = cpu_amis_rate(reps=1)
     line = {
-        "metric": METRIC, "value": value, "unit": "weighted samples/s", "n_gpus": world, "steps": args.steps,
-        "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": {"fp32": "f32", "tf32": "tf32", "bf16": "bf16"}[args.precision],
+        "metric": METRIC, "value": head["value"], "unit": "weighted samples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": warmup, "ms_per_step": head["ms"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp32": "f32", "tf32": "tf32", "bf16": "bf16"}[args.precision],
         "data": "synthetic (seeded C4 inputs)",
         "config": {"workload": WORKLOAD if (rounds, round_size) == (ROUNDS, ROUND_SIZE) else
                    f"AMIS d=64, Student-t target (nu=5), {rounds} rounds x {round_size} samples (reduced case)",
                    "d": D, "rounds": rounds, "round_size": round_size,
-                   "precision": args.precision, "parallelism": f"replicas x{world}",
+                   "precision": args.precision + (" (bf16 x3 split)" if args.precision == "bf16" else ""),
+                   "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2: 512 MiB retained samples re-read every round"},
-        "accuracy": {"logz_hat": logz, "abs_logz_error": abs(logz), "posterior_mean_max_abs_error":
-                     float(np.max(np.abs(post_mean - loc)))},
+        "accuracy": {"logz_hat": head["logz"], "abs_logz_error": abs(head["logz"]),
+                     "posterior_mean_max_abs_error": head["post_mean_err"]},
+        "forms": {k: {"value": v["value"], "ms_per_step": v["ms"], "abs_logz_error": abs(v["logz"]),
+                      "posterior_mean_max_abs_error": v["post_mean_err"],
+                      "abs_logz_diff_vs_headline": abs(v["logz"] - head["logz"])} for k, v in forms.items()},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "peak_source": f"{src} hbm_gbs", "traffic": None,
+                     "frac": achieved / hbm, "peak_source": f"{src} hbm_gbs", "traffic": traffic,
                      "kernel_share": share},
         "cpu_baseline": {"value": cpu_value, "unit": "weighted samples/s", "cores": cores, "kind": "port",
                          "sample": f"40 rounds x {CPU_ROUND_SIZE} samples (d=64), FP64 oracle AMIS"},
         "e2e": {"value": total * world / (e2e_ms / 1e3), "unit": "weighted samples/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-        "gpu_launches": int((l1 - l0) // args.steps),
+        "gpu_launches": head["launches"],
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -299,7 +335,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--precision", default="fp32", choices=["fp32", "tf32", "bf16"])
+    ap.add_argument("--precision", default="bf16", choices=["fp32", "tf32", "bf16"],
+                    help="bf16: the BF16 x3 tensor-core form (default); fp32: the plain FP32 drop-in form")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--rounds", type=int, default=ROUNDS)
     ap.add_argument("--round-size", type=int, default=ROUND_SIZE)
