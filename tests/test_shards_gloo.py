@@ -65,7 +65,8 @@ def test_two_rank_gloo_merge(issm):
     lw = rng.normal(size=4_001) * 3 + 2.0
     lw[:17] = -np.inf
     port = _free_port()
-    with mp.Manager() as manager:
+    # spawn, never fork: the test process may already hold a CUDA context
+    with mp.get_context("spawn").Manager() as manager:
         out = manager.dict()
         mp.spawn(_worker, args=(2, port, lw, out), nprocs=2, join=True)
         results = dict(out)
