@@ -330,6 +330,66 @@ def run_gb300(args):
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args):
+    """Serving mix (C5 shapes): independent Bayesian linear-regression
+    posteriors, d ~ U{2..64}, n_obs log-uniform in [50, 5000], sample budget
+    log-uniform in [1k, 100k] over 4 AMIS rounds, Poisson arrivals at each
+    rate of the sweep; p50/p99 latency, retained weighted samples/s, and the
+    worst errors against the conjugate analytic posteriors."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    issm = ge.load_package()
+    issm.native.require()
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(55)
+
+    def make(count):
+        reqs, truth = [], {}
+        for rid in range(count):
+            d = int(rng.integers(2, 65))
+            n_obs = int(np.exp(rng.uniform(np.log(50), np.log(5000))))
+            budget = int(np.exp(rng.uniform(np.log(1000), np.log(100_000))))
+            X = rng.normal(size=(n_obs, d))
+            beta = rng.normal(size=d)
+            y = X @ beta + 0.5 * rng.normal(size=n_obs)
+            tgt = issm.LinearRegressionTarget(X, y, sigma=0.5, prior_var=1.0)
+            mean, logz = tgt.analytic()
+            sd = np.sqrt(np.diag(np.linalg.inv(X.T @ X / 0.25 + np.eye(d))))
+            truth[rid] = (mean, sd, logz)
+            p = issm.FactorGaussian(np.zeros(d, dtype=np.float32), np.eye(d, dtype=np.float32))
+            reqs.append(issm.serving.ServeRequest(rid, tgt, p, rounds=4, round_size=max(budget // 4, 64),
+                                                  seed=rid))
+        return reqs, truth
+
+    # warm-up: compile-free, but first launches and allocations
+    warm, _ = make(8)
+    issm.serving.ServeLoop(dev, max_inflight=args.inflight).run(warm)
+    sweep = []
+    for rate in args.rates:
+        reqs, truth = make(args.requests)
+        t = 0.0
+        for r in reqs:
+            t += rng.exponential(1.0 / rate)
+            r.arrival = t
+        t0 = time.perf_counter()
+        out = issm.serving.ServeLoop(dev, max_inflight=args.inflight).run(reqs)
+        wall = time.perf_counter() - t0
+        lat = np.array([r.latency for r in out])
+        samples = sum(r.samples for r in reqs)
+        lz = max(abs(r.logz - truth[r.rid][2]) for r in out)
+        me = max(float(np.max(np.abs(r.posterior_mean - truth[r.rid][0]) / truth[r.rid][1])) for r in out)
+        sweep.append({"rate_per_s": rate, "requests": len(out), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                      "p99_ms": 1e3 * float(np.percentile(lat, 99)), "samples_per_s": samples / wall,
+                      "wall_s": wall, "max_abs_logz_error": lz, "max_posterior_mean_error_sd": me})
+    line = {"metric": "serving mix p50/p99 latency and weighted samples/s", "impl": "gb300",
+            "workload": "Bayesian linear regression posteriors, d~U{2..64}, n_obs log-uniform 50-5000, "
+                        "budget log-uniform 1k-100k, AMIS 4 rounds, Poisson arrivals",
+            "precision": "bf16 (bf16 x3 split)", "max_inflight": args.inflight, "sweep": sweep}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -341,7 +401,15 @@ def main():
     ap.add_argument("--rounds", type=int, default=ROUNDS)
     ap.add_argument("--round-size", type=int, default=ROUND_SIZE)
     ap.add_argument("--quick", action="store_true", help="skip the e2e and CPU-baseline legs (profiling runs)")
+    ap.add_argument("--workload", default="amis", choices=["amis", "serve"],
+                    help="amis: the headline AMIS d=64 run; serve: the serving-mix latency sweep")
+    ap.add_argument("--requests", type=int, default=200, help="serve: requests per arrival rate")
+    ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0], help="serve: arrivals per second")
+    ap.add_argument("--inflight", type=int, default=8, help="serve: concurrent runs (streams)")
     args = ap.parse_args()
+    if args.workload == "serve":
+        run_serve(args)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -6,7 +6,7 @@ reference's public interface: proposals, banks, algorithm configurations,
 prepare_sampler / importance_sample! / importance_sample, WeightedSamples and
 its reductions and resampling.
 """
-from . import native, ops, shards
+from . import native, ops, serving, shards
 from .bank import DeviceBank, DeviceHistory, ProposalBank, pack, pack_proposals
 from .methods import (AMIS, NPMC, DeterministicMixturePMC, GlobalResampling, ImportanceSampling, LocalResampling,
                       MultinomialResampling, PartialDeterministicMixture, RandomMixture, StandardMIS,

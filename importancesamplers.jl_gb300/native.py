@@ -5,8 +5,10 @@ fallback: if the library or a CUDA device is missing, `require()` raises.
 Tensors are passed as raw device pointers; the current torch stream is used
 unless a stream is given.
 """
+import contextlib
 import ctypes as C
 import os
+import threading
 
 import torch
 
@@ -192,13 +194,33 @@ def launches():
 
 _workspaces = {}
 _retired = []  # outgrown workspaces stay allocated: a recorded CUDA graph may still address them
+_scope = threading.local()
+
+
+@contextlib.contextmanager
+def workspace_scope(name):
+    """Give the launches inside the block their own scratch buffers (keyed by
+    `name`), so work running concurrently on other streams never shares one."""
+    prev = getattr(_scope, "name", None)
+    _scope.name = name
+    try:
+        yield
+    finally:
+        _scope.name = prev
+
+
+def release_scope(name):
+    """Free the scratch buffers of a scope once its work has completed."""
+    for key in [k for k in _workspaces if k[2] == name]:
+        del _workspaces[key]
 
 
 def workspace(nbytes, device=None, tag="default", zero=False):
-    """A cached device scratch buffer of at least nbytes (per device, per tag);
-    zero=True allocates it zero-filled (sticky error words live at its end)."""
+    """A cached device scratch buffer of at least nbytes (per device, tag and
+    workspace scope); zero=True allocates it zero-filled (sticky error words
+    live at its end)."""
     device = device or torch.device("cuda", torch.cuda.current_device())
-    key = (str(device), tag)
+    key = (str(device), tag, getattr(_scope, "name", None))
     buf = _workspaces.get(key)
     if buf is None or buf.numel() < nbytes:
         if buf is not None:
@@ -209,10 +231,15 @@ def workspace(nbytes, device=None, tag="default", zero=False):
     return buf
 
 
+def scoped_workspace(device, tag):
+    """The current scope's buffer for `tag`, or None."""
+    return _workspaces.get((str(device), tag, getattr(_scope, "name", None)))
+
+
 def tc_error(device=None):
     """The sticky tensor-core wait-timeout word of the device's tc workspace."""
     device = device or torch.device("cuda", torch.cuda.current_device())
-    buf = _workspaces.get((str(device), "tc"))
+    buf = scoped_workspace(device, "tc")
     if buf is None:
         return 0
     return int(buf[-64:-60].view(torch.int32).item())

@@ -275,7 +275,7 @@ def check_tensor_core_errors(device):
     """Raise if a tensor-core kernel reported a timed-out completion wait (the
     sticky words at the end of the tc and moments workspaces)."""
     for tag in ("tc", "moments"):
-        buf = native._workspaces.get((str(device), tag))
+        buf = native.scoped_workspace(device, tag)
         if buf is not None and int(buf[-64:-60].view(torch.int32).item()) != 0:
             raise RuntimeError(f"a tensor-core kernel ({tag}) timed out waiting for MMA completion")
 
