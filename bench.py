@@ -356,16 +356,21 @@ def run_serve(args):
             y = X @ beta + 0.5 * rng.normal(size=n_obs)
             tgt = issm.LinearRegressionTarget(X, y, sigma=0.5, prior_var=1.0)
             mean, logz = tgt.analytic()
-            sd = np.sqrt(np.diag(np.linalg.inv(X.T @ X / 0.25 + np.eye(d))))
-            truth[rid] = (mean, sd, logz)
-            p = issm.FactorGaussian(np.zeros(d, dtype=np.float32), np.eye(d, dtype=np.float32))
+            post_cov = np.linalg.inv(X.T @ X / 0.25 + np.eye(d))
+            truth[rid] = (mean, np.sqrt(np.diag(post_cov)), logz)
+            # warm start: the Laplace form displaced and widened by 0.5/sqrt(d) of its scale
+            Lp = np.linalg.cholesky(post_cov)
+            f = 0.5 / np.sqrt(d)
+            p = issm.FactorGaussian((mean + f * Lp @ rng.normal(size=d)).astype(np.float32),
+                                    ((1 + f) * Lp).astype(np.float32))
             reqs.append(issm.serving.ServeRequest(rid, tgt, p, rounds=4, round_size=max(budget // 4, 64),
                                                   seed=rid))
         return reqs, truth
 
     # warm-up: compile-free, but first launches and allocations
+    prec = {"fp32": issm.native.PREC_NATIVE, "tf32": issm.native.PREC_TF32, "bf16": issm.native.PREC_BF16}[args.precision]
     warm, _ = make(8)
-    issm.serving.ServeLoop(dev, max_inflight=args.inflight).run(warm)
+    issm.serving.ServeLoop(dev, max_inflight=args.inflight, precision=prec).run(warm)
     sweep = []
     for rate in args.rates:
         reqs, truth = make(args.requests)
@@ -374,19 +379,25 @@ def run_serve(args):
             t += rng.exponential(1.0 / rate)
             r.arrival = t
         t0 = time.perf_counter()
-        out = issm.serving.ServeLoop(dev, max_inflight=args.inflight).run(reqs)
+        out = issm.serving.ServeLoop(dev, max_inflight=args.inflight, precision=prec).run(reqs)
         wall = time.perf_counter() - t0
         lat = np.array([r.latency for r in out])
         samples = sum(r.samples for r in reqs)
-        lz = max(abs(r.logz - truth[r.rid][2]) for r in out)
-        me = max(float(np.max(np.abs(r.posterior_mean - truth[r.rid][0]) / truth[r.rid][1])) for r in out)
+        lz = np.array([abs(r.logz - truth[r.rid][2]) for r in out])
+        me = np.array([float(np.max(np.abs(r.posterior_mean - truth[r.rid][0]) / truth[r.rid][1])) for r in out])
         sweep.append({"rate_per_s": rate, "requests": len(out), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
                       "p99_ms": 1e3 * float(np.percentile(lat, 99)), "samples_per_s": samples / wall,
-                      "wall_s": wall, "max_abs_logz_error": lz, "max_posterior_mean_error_sd": me})
+                      "runs_per_s": len(out) / wall, "wall_s": wall,
+                      "abs_logz_error": {"p50": float(np.median(lz)), "p90": float(np.percentile(lz, 90)),
+                                         "max": float(lz.max())},
+                      "posterior_mean_error_sd": {"p50": float(np.median(me)), "p90": float(np.percentile(me, 90)),
+                                                  "max": float(me.max())}})
     line = {"metric": "serving mix p50/p99 latency and weighted samples/s", "impl": "gb300",
             "workload": "Bayesian linear regression posteriors, d~U{2..64}, n_obs log-uniform 50-5000, "
-                        "budget log-uniform 1k-100k, AMIS 4 rounds, Poisson arrivals",
-            "precision": "bf16 (bf16 x3 split)", "max_inflight": args.inflight, "sweep": sweep}
+                        "budget log-uniform 1k-100k, AMIS 4 rounds, Poisson arrivals; initial proposal the "
+                        "posterior's Laplace form displaced and widened by 0.5/sqrt(d) of its scale",
+            "precision": {"bf16": "bf16 (bf16 x3 split)", "tf32": "tf32", "fp32": "fp32"}[args.precision],
+            "max_inflight": args.inflight, "sweep": sweep}
     print(json.dumps(line), flush=True)
 
 

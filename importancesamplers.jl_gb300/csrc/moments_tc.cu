@@ -7,9 +7,12 @@
 // K; A A^T then holds S2 = sum w z z^T (rows/cols 0..63), S1 = sum w z
 // (row 64) and S0 = sum w (D[64][64]). A is split A = Ah + Al in bf16 and
 // A A^T ~ Ah Ah^T + X + X^T with X = Al Ah^T, so two accumulators in tensor
-// memory (H += Ah Ah^T, X += Al Ah^T) give the three-product accuracy (about
-// 16 significant bits per product) with two MMAs per K slice; the transpose
-// is added when the sums are finished.
+// memory (H += Ah Ah^T + Al Al^T, X += Al Ah^T) give the four products with
+// three MMAs per K slice; the transpose of X is added when the sums are
+// finished. With Al Al^T included, S = (Ah + Al)(Ah + Al)^T is the Gram matrix
+// of the split operand, positive semidefinite up to FP32 accumulation, so the
+// covariance of a low-ESS sample stays semidefinite (the regularising ridge
+// then keeps the fit positive definite).
 //
 // A is stored MN-major: each sample's 8-coordinate groups are 16-byte chunks,
 // so a thread converts its own sample row straight from the staged tile. Warp
@@ -46,7 +49,9 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
                                                                     const float *__restrict__ lw,
                                                                     const double *__restrict__ summary,
                                                                     const double *__restrict__ center,
-                                                                    float *__restrict__ partial, int *error) {
+                                                                    float *__restrict__ partial, int *error,
+                                                                    const int *__restrict__ gate) {
+    if (gate != nullptr && *gate == 0) return;  // refinement pass not needed
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *s_a = smem;                                    // [buf][part] x kMtPart
     unsigned char *s_raw = smem + (size_t)2 * 2 * kMtPart;
@@ -83,7 +88,7 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
     };
 
     if (warp == 0) {
-        // ---- issuer: H += Ah Ah^T, X += Al Ah^T per K slice ----
+        // ---- issuer: H += Ah Ah^T + Al Al^T, X += Al Ah^T per K slice ----
         const uint32_t idesc = tc::instr_desc(tc::kBF16, 128, kMtCols) | tc::kMajorMN;
         constexpr uint32_t LBO = 128, SBO = kMtTile * 16;  // K-group stride, row-group stride
         for (int it = 0; it < my_tiles; ++it) {
@@ -99,6 +104,7 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
                         const uint64_t dl = tc::smem_desc(a1 + s * 256, LBO, SBO);
                         tc::mma(tbase, dh, dh, idesc, it > 0 || s > 0);
                         tc::mma(tbase + 128, dl, dh, idesc, it > 0 || s > 0);
+                        tc::mma(tbase, dl, dl, idesc, true);
                     }
                 }
                 tc::commit(&a_empty[buf]);
@@ -265,7 +271,9 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
 // Partials are [block][2][65][80] FP32 (H, X); stage 1 sums them over blocks
 // (32 entries x 8 block-strided lanes per CTA, coalesced), stage 2 forms
 // S = H + X + X^T and from it the mean and covariance.
-__global__ void moments_tc_reduce_kernel(const float *__restrict__ partial, int blocks, double *__restrict__ sums) {
+__global__ void moments_tc_reduce_kernel(const float *__restrict__ partial, int blocks, double *__restrict__ sums,
+                                         const int *__restrict__ gate) {
+    if (gate != nullptr && *gate == 0) return;
     __shared__ double acc_s[8][33];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int e = blockIdx.x * 32 + tx;
@@ -288,18 +296,32 @@ __global__ void moments_tc_reduce_kernel(const float *__restrict__ partial, int 
     }
 }
 
-__global__ void moments_tc_finish_kernel(const double *__restrict__ sums, int d, const double *__restrict__ center,
-                                         double *__restrict__ mean, double *__restrict__ cov) {
+// mean = c + S1/S0, cov = S2/S0 - (S1/S0)(S1/S0)^T with S = H + X + X^T (c as
+// the FP32 value the pass subtracted; `center` and `mean` may be the same
+// array, each entry read before it is written). When
+// the new mean lies far from the centre c relative to the spread, S2/S0 and
+// the mean's outer product nearly cancel and the bf16-split sums lose their
+// accuracy: a diagonal variance below 2^-6 of its second moment about c (six
+// bits or more cancelled) sets *refine, and a second pass centred at the new
+// mean (gated on that flag) replaces the result.
+__global__ void moments_tc_finish_kernel(const double *__restrict__ sums, int d, const double *center,
+                                         double *mean, double *__restrict__ cov,
+                                         const int *__restrict__ gate, int *__restrict__ refine) {
+    if (gate != nullptr && *gate == 0) return;
     const double *H = sums, *X = sums + 65 * kMtCols;
     auto S = [&](int r, int c) { return H[r * kMtCols + c] + X[r * kMtCols + c] + X[c * kMtCols + r]; };
     const double inv = 1.0 / S(64, 64);
-    if (blockIdx.x == 0)
-        for (int j = threadIdx.x; j < d; j += blockDim.x) mean[j] = center[j] + S(64, j) * inv;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d * d; e += gridDim.x * blockDim.x) {
         const int r = e % d, c = e / d;
         const double mr = S(64, r) * inv, mc = S(64, c) * inv;
-        cov[e] = S(r, c) * inv - mr * mc;
+        const double s2 = S(r, c) * inv, v = s2 - mr * mc;
+        cov[e] = v;
+        if (refine != nullptr && r == c && !(v > s2 * 0.015625)) atomicExch(refine, 1);
     }
+    // the mean last: the refinement pass reads this call's mean as its centre
+    __syncthreads();
+    if (blockIdx.x == 0)
+        for (int j = threadIdx.x; j < d; j += blockDim.x) mean[j] = (double)(float)center[j] + S(64, j) * inv;
 }
 
 static int moments_tc_blocks(int64_t n) {
@@ -309,7 +331,7 @@ static int moments_tc_blocks(int64_t n) {
 
 size_t moments_tc_workspace_bytes(int64_t n) {
     (void)n;
-    return sizeof(float) * (size_t)kSMs * kMtPartial + sizeof(double) * kMtPartial + 128;
+    return sizeof(float) * (size_t)kSMs * kMtPartial + sizeof(double) * kMtPartial + 256;
 }
 
 int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *summary, const double *shift,
@@ -321,11 +343,22 @@ int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *su
     float *partial = (float *)ws;
     const int e = allow_dynamic_smem((const void *)moments_tc_kernel);
     if (e) return e;
-    { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw, summary,
-                                                                shift, partial, error); note_launch(); }
     double *sums = reinterpret_cast<double *>(partial + (size_t)kSMs * kMtPartial);
-    { moments_tc_reduce_kernel<<<(kMtPartial + 31) / 32, 256, 0, stream>>>(partial, blocks, sums); note_launch(); }
-    { moments_tc_finish_kernel<<<(d * d + 255) / 256, 256, 0, stream>>>(sums, d, shift, mean, cov); note_launch(); }
+    int *refine = reinterpret_cast<int *>(sums + kMtPartial);
+    cudaError_t ce = cudaMemsetAsync(refine, 0, sizeof(int), stream);
+    if (ce != cudaSuccess) return (int)ce;
+    // pass 1 about `shift`
+    { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw, summary,
+                                                                shift, partial, error, nullptr); note_launch(); }
+    { moments_tc_reduce_kernel<<<(kMtPartial + 31) / 32, 256, 0, stream>>>(partial, blocks, sums, nullptr);
+      note_launch(); }
+    { moments_tc_finish_kernel<<<1, 256, 0, stream>>>(sums, d, shift, mean, cov, nullptr, refine); note_launch(); }
+    // pass 2 about the new mean, only when pass 1 cancelled too many bits (kernels exit on the flag)
+    { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw, summary,
+                                                                mean, partial, error, refine); note_launch(); }
+    { moments_tc_reduce_kernel<<<(kMtPartial + 31) / 32, 256, 0, stream>>>(partial, blocks, sums, refine);
+      note_launch(); }
+    { moments_tc_finish_kernel<<<1, 256, 0, stream>>>(sums, d, mean, mean, cov, refine, nullptr); note_launch(); }
     return (int)cudaGetLastError();
 }
 

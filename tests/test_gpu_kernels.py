@@ -413,7 +413,7 @@ def test_golden_literal_moments(issm, orc, cuda, golden, dtype):
     assert int(fail[0].item()) == 0
 
 
-@pytest.mark.parametrize("d", [1, 5, 16, 64])
+@pytest.mark.parametrize("d", [1, 5, 9, 16, 33, 47, 64])
 def test_moments_and_fit_vs_oracle(issm, orc, cuda, d):
     rng = np.random.default_rng(d)
     n = 20011

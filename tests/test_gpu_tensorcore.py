@@ -137,6 +137,35 @@ def test_tc_moments_vs_oracle(issm, orc, cuda, prec, d, n):
     assert np.max(np.abs(cov.cpu().numpy() - ec) / scale) < tol
 
 
+@pytest.mark.parametrize("d", [9, 33, 64])
+def test_tc_moments_far_centre_and_low_ess(issm, orc, cuda, d):
+    """A centre hundreds of standard deviations from the weighted mean (the
+    one-pass sums cancel; the centred second pass must take over) and a
+    weighted covariance of rank below d (a handful of samples carry the
+    weight): the covariance matches the oracle on the spread's scale and
+    stays semidefinite to FP32 rounding of the Gram sums."""
+    rng = np.random.default_rng(d)
+    n = 40_000
+    X = (rng.normal(size=(n, d)) * 0.02 + 0.7).astype(np.float32)
+    for case in ("far", "low_ess"):
+        lw = (rng.normal(size=n) * 0.5).astype(np.float32)
+        if case == "low_ess":
+            lw = np.full(n, -60.0, dtype=np.float32)
+            lw[rng.choice(n, d // 3 + 1, replace=False)] = rng.normal(size=d // 3 + 1).astype(np.float32)
+        tx, tl = torch.tensor(X, device=cuda), torch.tensor(lw, device=cuda)
+        sm = issm.ops.logweight_summary(tl)
+        shift = torch.full((d,), -8.0 if case == "far" else 0.7, dtype=torch.float64, device=cuda)
+        mean, cov = issm.ops.weighted_moments(tx, tl, sm, shift, precision=issm.native.PREC_BF16)
+        torch.cuda.synchronize()
+        issm.ops.check_tensor_core_errors(cuda)
+        em, ec, _ = orc.weighted_moments(X.astype(np.float64).reshape(-1), d, lw.astype(np.float64))
+        c = cov.cpu().numpy()
+        spread = float(np.trace(ec)) / d
+        assert np.max(np.abs(mean.cpu().numpy() - em)) < 2e-4 * np.sqrt(spread), case
+        assert np.max(np.abs(c - ec)) < 2e-4 * spread, case
+        assert np.linalg.eigvalsh(0.5 * (c + c.T)).min() > -1e-5 * spread, case
+
+
 @pytest.mark.parametrize("prec", ["tf32", "bf16"])
 def test_tc_amis_matches_native_form(issm, cuda, prec):
     """Same draws, FP32 SIMT vs tensor-core forms: log Z and the posterior
