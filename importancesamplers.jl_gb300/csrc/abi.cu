@@ -398,8 +398,9 @@ size_t issm_moments_workspace_bytes(int64_t n, int32_t d) {
 }
 
 int issm_weighted_moments_ws(const void *x, int32_t d, int64_t n, const void *logweights, int32_t dtype,
-                             const double *summary, const double *shift, double *mean, double *cov,
-                             int32_t precision, void *workspace, size_t workspace_bytes, issm_stream_t stream) {
+                             const double *summary, const double *shift, const void *prev_factor, double *mean,
+                             double *cov, int32_t precision, void *workspace, size_t workspace_bytes,
+                             issm_stream_t stream) {
     if (d < 1 || n < 1) return ISSM_E_SIZE;
     if (d > 64) return ISSM_E_UNSUPPORTED;
     if (!x || !logweights || !summary || !shift || !mean || !cov || !workspace) return ISSM_E_NULL;
@@ -411,8 +412,8 @@ int issm_weighted_moments_ws(const void *x, int32_t d, int64_t n, const void *lo
     if (precision != ISSM_PREC_TF32 && precision != ISSM_PREC_BF16) return ISSM_E_KIND;
     if (dtype != ISSM_F32) return ISSM_E_UNSUPPORTED;
     int *err = (int *)((char *)workspace + workspace_bytes - 64);
-    return moments_tc(x, d, n, logweights, summary, shift, mean, cov, precision, workspace, workspace_bytes - 64,
-                      err, (cudaStream_t)stream);
+    return moments_tc(x, d, n, logweights, summary, shift, (const float *)prev_factor, mean, cov, precision, workspace,
+                      workspace_bytes - 64, err, (cudaStream_t)stream);
 }
 
 int issm_weighted_moments(const void *x, int32_t d, int64_t n, const void *logweights, int32_t dtype,

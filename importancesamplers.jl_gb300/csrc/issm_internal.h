@@ -81,6 +81,7 @@ int tc_mixture(const issm_bank *bk, const issm_denominator *den, int mode, int f
 // tensor-core weighted moments (moments_tc.cu)
 size_t moments_tc_workspace_bytes(int64_t n);
 int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *summary, const double *shift,
+               const float *prev_factor,
                double *mean, double *cov, int precision, void *ws, size_t ws_bytes, int *error, cudaStream_t stream);
 
 // tensor-core self-test (tc_selftest.cu)

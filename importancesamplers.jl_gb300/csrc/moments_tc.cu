@@ -6,13 +6,20 @@
 // (c = previous proposal mean), row 64 holds sqrt(w), with the samples along
 // K; A A^T then holds S2 = sum w z z^T (rows/cols 0..63), S1 = sum w z
 // (row 64) and S0 = sum w (D[64][64]). A is split A = Ah + Al in bf16 and
-// A A^T ~ Ah Ah^T + X + X^T with X = Al Ah^T, so two accumulators in tensor
-// memory (H += Ah Ah^T + Al Al^T, X += Al Ah^T) give the four products with
-// three MMAs per K slice; the transpose of X is added when the sums are
-// finished. With Al Al^T included, S = (Ah + Al)(Ah + Al)^T is the Gram matrix
-// of the split operand, positive semidefinite up to FP32 accumulation, so the
-// covariance of a low-ESS sample stays semidefinite (the regularising ridge
-// then keeps the fit positive definite).
+// two accumulators in tensor memory, H += Ah Ah^T + Al Al^T and X += Al Ah^T,
+// with X^T added when the sums are finished, give S = (Ah + Al)(Ah + Al)^T:
+// the Gram matrix of the split operand (about 16 significant bits per
+// element), so the covariance (its Schur complement) is positive semidefinite
+// up to FP32 accumulation however few samples carry the weight, and the
+// regularising ridge keeps the fit positive definite. The third MMA per K
+// slice costs nothing measurable: the pass is bound by HBM.
+//
+// When the new mean lies far from c relative to the spread, S2/S0 and the
+// mean's outer product nearly cancel. A second pass centred at the first
+// pass's mean runs when the first pass's cancellation error could matter
+// against the variance or the fit's ridge (see the reduce kernel); its
+// kernels are always launched (graph replays see a fixed sequence) and
+// return at once when the flag is clear.
 //
 // A is stored MN-major: each sample's 8-coordinate groups are 16-byte chunks,
 // so a thread converts its own sample row straight from the staged tile. Warp
@@ -268,60 +275,107 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
     if (warp == 0) tc::tmem_dealloc(tbase, 256);
 }
 
-// Partials are [block][2][65][80] FP32 (H, X); stage 1 sums them over blocks
-// (32 entries x 8 block-strided lanes per CTA, coalesced), stage 2 forms
-// S = H + X + X^T and from it the mean and covariance.
-__global__ void moments_tc_reduce_kernel(const float *__restrict__ partial, int blocks, double *__restrict__ sums,
-                                         const int *__restrict__ gate) {
+// Partials are [block][2][65][80] FP32 (H, X). Every CTA sums 32 entries over
+// the blocks (32 block-strided lanes per entry, coalesced); the last CTA to
+// finish (a device-scope counter, reset by that CTA) forms S = H + X + X^T and
+// from it mean = c + S1/S0 and cov = S2/S0 - (S1/S0)(S1/S0)^T in FP64, with c
+// the FP32 value the pass subtracted. `center` and `mean` may be the same
+// array: each entry is read before it is written. With `refine` given, the
+// last CTA sets it when, on some diagonal, the pass's cancellation error
+// (2^-16 of the second moment s2 about c) exceeds 2^-8 of the variance v plus
+// 2^-4 of R = sqrt(eps(Float32)) tr(L L^T) / d for the previous factor L, the
+// scale of the ridge the fit adds (R = 0 without L): s2 > 256 v + 4096 R.
+// Low-ESS rounds whose variance is mostly ridge then refine only when the
+// mean moved by more than about one previous scale.
+constexpr int kMtReduceThreads = 1024;  // 32 entries x 32 block-strided lanes per CTA
+
+// FP64 work here runs on one SM's FP64 pipe (a warp-instruction holds it for
+// about 64 cycles on this GPU whatever the active lanes), so the kernel keeps
+// FP64 to the Schur complement itself: lanes combine in compensated FP32, the
+// ridge scale is FP32, 1/S0 is formed once, and only the lower triangle of the
+// covariance is computed (four FP64 operations per element).
+__global__ void __launch_bounds__(kMtReduceThreads) moments_tc_reduce_kernel(
+    const float *__restrict__ partial, int blocks, double *sums, int d, const double *center, double *mean,
+    double *__restrict__ cov, const int *__restrict__ gate, int *refine, const float *__restrict__ prev,
+    unsigned *counter) {
     if (gate != nullptr && *gate == 0) return;
-    __shared__ double acc_s[8][33];
+    __shared__ float acc_s[32][33], cmp_s[32][33];
+    __shared__ double s_m[65];  // S1 / S0 (the mean about c)
+    __shared__ double s_inv;
+    __shared__ float s_r[32];
+    __shared__ int last;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int e = blockIdx.x * 32 + tx;
-    // compensated FP32 over this lane's blocks (no serial FP64 chain), FP64 across lanes
+    // compensated FP32 over this lane's blocks, then over the 32 lanes
     float s = 0.f, cmp = 0.f;
     if (e < kMtPartial)
-        for (int b = ty; b < blocks; b += 8) {
+        for (int b = ty; b < blocks; b += 32) {
             const float y = partial[(size_t)b * kMtPartial + e] - cmp;
             const float t = s + y;
             cmp = (t - s) - y;
             s = t;
         }
-    const double acc = (double)s - (double)cmp;
-    acc_s[ty][tx] = acc;
+    acc_s[ty][tx] = s;
+    cmp_s[ty][tx] = cmp;
     __syncthreads();
     if (ty == 0 && e < kMtPartial) {
-        double t = 0.0;
-        for (int r = 0; r < 8; ++r) t += acc_s[r][tx];
-        sums[e] = t;
+        float t = 0.f, c = 0.f;
+        for (int r = 0; r < 32; ++r) {
+            const float y = acc_s[r][tx] - (cmp_s[r][tx] + c);
+            const float u = t + y;
+            c = (u - t) - y;
+            t = u;
+        }
+        sums[e] = (double)t - (double)c;
     }
-}
-
-// mean = c + S1/S0, cov = S2/S0 - (S1/S0)(S1/S0)^T with S = H + X + X^T (c as
-// the FP32 value the pass subtracted; `center` and `mean` may be the same
-// array, each entry read before it is written). When
-// the new mean lies far from the centre c relative to the spread, S2/S0 and
-// the mean's outer product nearly cancel and the bf16-split sums lose their
-// accuracy: a diagonal variance below 2^-6 of its second moment about c (six
-// bits or more cancelled) sets *refine, and a second pass centred at the new
-// mean (gated on that flag) replaces the result.
-__global__ void moments_tc_finish_kernel(const double *__restrict__ sums, int d, const double *center,
-                                         double *mean, double *__restrict__ cov,
-                                         const int *__restrict__ gate, int *__restrict__ refine) {
-    if (gate != nullptr && *gate == 0) return;
-    const double *H = sums, *X = sums + 65 * kMtCols;
-    auto S = [&](int r, int c) { return H[r * kMtCols + c] + X[r * kMtCols + c] + X[c * kMtCols + r]; };
-    const double inv = 1.0 / S(64, 64);
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < d * d; e += gridDim.x * blockDim.x) {
-        const int r = e % d, c = e / d;
-        const double mr = S(64, r) * inv, mc = S(64, c) * inv;
-        const double s2 = S(r, c) * inv, v = s2 - mr * mc;
-        cov[e] = v;
-        if (refine != nullptr && r == c && !(v > s2 * 0.015625)) atomicExch(refine, 1);
-    }
-    // the mean last: the refinement pass reads this call's mean as its centre
+    __threadfence();
     __syncthreads();
-    if (blockIdx.x == 0)
-        for (int j = threadIdx.x; j < d; j += blockDim.x) mean[j] = (double)(float)center[j] + S(64, j) * inv;
+    if (threadIdx.x == 0) last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const double *H = sums, *X = sums + 65 * kMtCols;
+    auto S = [&](int r, int c) {
+        return __ldcg(H + r * kMtCols + c) + __ldcg(X + r * kMtCols + c) + __ldcg(X + c * kMtCols + r);
+    };
+    if (threadIdx.x == 0) s_inv = 1.0 / S(64, 64);
+    // R = sqrt(eps(Float32)) tr(L L^T) / d of the previous factor (0 without one), in FP32
+    float rr = 0.f;
+    if (refine != nullptr && prev != nullptr)
+        for (int q = threadIdx.x; q < d * d; q += blockDim.x) rr = fmaf(prev[q], prev[q], rr);
+    for (int off = 16; off > 0; off >>= 1) rr += __shfl_xor_sync(0xffffffffu, rr, off);
+    if (tx == 0) s_r[ty] = rr;
+    __syncthreads();
+    if (threadIdx.x < 65) s_m[threadIdx.x] = S(64, threadIdx.x) * s_inv;
+    __syncthreads();
+    const double inv = s_inv;
+    // lower triangle, row-major: q -> (r, c), c <= r
+    const int tri = d * (d + 1) / 2;
+    for (int q = threadIdx.x; q < tri; q += blockDim.x) {
+        int r = (int)((sqrtf(8.f * (float)q + 1.f) - 1.f) * 0.5f);
+        if ((r + 1) * (r + 2) / 2 <= q) ++r;
+        if (r * (r + 1) / 2 > q) --r;
+        const int c = q - r * (r + 1) / 2;
+        const double v = fma(S(r, c), inv, -s_m[r] * s_m[c]);
+        cov[r + (size_t)c * d] = v;
+        cov[c + (size_t)r * d] = v;
+    }
+    int flag = 0;
+    if (refine != nullptr && threadIdx.x < d) {
+        float ridge = 0.f;
+        for (int w = 0; w < 32; ++w) ridge += s_r[w];
+        ridge *= 3.4526698e-4f / (float)d;  // sqrt(FLT_EPSILON)
+        const int r = threadIdx.x;
+        const double s2 = S(r, r) * inv, v = s2 - s_m[r] * s_m[r];
+        // the pass's error (2^-16 of s2) above 2^-8 of v plus 2^-4 of the ridge scale
+        flag = !(s2 <= 256.0 * v + 4096.0 * (double)ridge);
+    }
+    flag = __syncthreads_or(flag);  // also orders the reads of `center` below after every thread's work above
+    for (int j = threadIdx.x; j < d; j += blockDim.x) mean[j] = (double)(float)center[j] + s_m[j];
+    if (threadIdx.x == 0) {
+        if (refine != nullptr) *refine = flag;
+        *counter = 0u;
+    }
 }
 
 static int moments_tc_blocks(int64_t n) {
@@ -335,7 +389,8 @@ size_t moments_tc_workspace_bytes(int64_t n) {
 }
 
 int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *summary, const double *shift,
-               double *mean, double *cov, int precision, void *ws, size_t ws_bytes, int *error, cudaStream_t stream) {
+               const float *prev_factor, double *mean, double *cov, int precision, void *ws, size_t ws_bytes,
+               int *error, cudaStream_t stream) {
     (void)precision;  // both tensor-core forms use the bf16 split contraction
     if (d > 64) return ISSM_E_UNSUPPORTED;
     if (ws_bytes < moments_tc_workspace_bytes(n)) return ISSM_E_WORKSPACE;
@@ -345,20 +400,22 @@ int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *su
     if (e) return e;
     double *sums = reinterpret_cast<double *>(partial + (size_t)kSMs * kMtPartial);
     int *refine = reinterpret_cast<int *>(sums + kMtPartial);
-    cudaError_t ce = cudaMemsetAsync(refine, 0, sizeof(int), stream);
-    if (ce != cudaSuccess) return (int)ce;
+    unsigned *counter = reinterpret_cast<unsigned *>(error + 1);  // zero with the workspace; reset by each use
+    const int rblocks = (kMtPartial + 31) / 32;
     // pass 1 about `shift`
-    { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw, summary,
-                                                                shift, partial, error, nullptr); note_launch(); }
-    { moments_tc_reduce_kernel<<<(kMtPartial + 31) / 32, 256, 0, stream>>>(partial, blocks, sums, nullptr);
+    { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw,
+                                                                       summary, shift, partial, error, nullptr);
       note_launch(); }
-    { moments_tc_finish_kernel<<<1, 256, 0, stream>>>(sums, d, shift, mean, cov, nullptr, refine); note_launch(); }
-    // pass 2 about the new mean, only when pass 1 cancelled too many bits (kernels exit on the flag)
-    { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw, summary,
-                                                                mean, partial, error, refine); note_launch(); }
-    { moments_tc_reduce_kernel<<<(kMtPartial + 31) / 32, 256, 0, stream>>>(partial, blocks, sums, refine);
+    { moments_tc_reduce_kernel<<<rblocks, kMtReduceThreads, 0, stream>>>(partial, blocks, sums, d, shift, mean, cov,
+                                                                         nullptr, refine, prev_factor, counter);
       note_launch(); }
-    { moments_tc_finish_kernel<<<1, 256, 0, stream>>>(sums, d, mean, mean, cov, refine, nullptr); note_launch(); }
+    // pass 2 about the new mean (kernels return at once unless pass 1 set `refine`)
+    { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw,
+                                                                      summary, mean, partial, error, refine);
+      note_launch(); }
+    { moments_tc_reduce_kernel<<<rblocks, kMtReduceThreads, 0, stream>>>(partial, blocks, sums, d, mean, mean, cov,
+                                                                         refine, nullptr, nullptr, counter);
+      note_launch(); }
     return (int)cudaGetLastError();
 }
 

@@ -105,7 +105,7 @@ SIGNATURES = [
     ("issm_mixture_logdensity_ws", C.c_int, [_bank, _den, _p, _i64, _p, _i32, _p, _p, _p, _i64, _i32, _p, _sz,
                                              _p]),
     ("issm_amis_append_ws", C.c_int, [_bank, _i32, _p, _p, _i64, _p, _p, _i32, _p, _sz, _p]),
-    ("issm_weighted_moments_ws", C.c_int, [_p, _i32, _i64, _p, _i32, _p, _p, _p, _p, _i32, _p, _sz, _p]),
+    ("issm_weighted_moments_ws", C.c_int, [_p, _i32, _i64, _p, _i32, _p, _p, _p, _p, _p, _i32, _p, _sz, _p]),
 ]
 
 _lib = None

@@ -243,7 +243,8 @@ def local_resample(logweights, counts, uniforms, samples=None, ancestors=None, d
     return anc, destination
 
 
-def weighted_moments(x, logweights, summary, shift, mean=None, cov=None, precision=native.PREC_NATIVE):
+def weighted_moments(x, logweights, summary, shift, mean=None, cov=None, precision=native.PREC_NATIVE,
+                     prev_factor=None):
     n, d = x.shape
     dev = x.device
     mean = torch.empty(d, dtype=torch.float64, device=dev) if mean is None else mean
@@ -251,7 +252,8 @@ def weighted_moments(x, logweights, summary, shift, mean=None, cov=None, precisi
     nb = native.lib().issm_moments_workspace_bytes(n, d)
     ws = native.workspace(nb, dev, "moments", zero=True)
     native.call("issm_weighted_moments_ws", native.ptr(x), d, n, native.ptr(logweights), _dt(x),
-                native.ptr(summary), native.ptr(shift), native.ptr(mean), native.ptr(cov), int(precision),
+                native.ptr(summary), native.ptr(shift), native.ptr(prev_factor), native.ptr(mean), native.ptr(cov),
+                int(precision),
                 native.ptr(ws), ws.numel(), _s())
     return mean, cov
 

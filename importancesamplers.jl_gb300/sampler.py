@@ -377,7 +377,9 @@ def _moment_body(s, is_npmc):
                 x_fit = s.samples[:n_tot]
         with _Span(s, "moments", 2 * x_fit.shape[0] * (d + 1) * es):
             s.shift.copy_(h.locations[t])
-            ops.weighted_moments(x_fit, lw_fit, fit_summary, s.shift, s.mean, s.cov, precision=s.precision)
+            prev = h.scales[t] if h.scales[t].dim() == 2 and h.scales.dtype == torch.float32 else None
+            ops.weighted_moments(x_fit, lw_fit, fit_summary, s.shift, s.mean, s.cov, precision=s.precision,
+                                 prev_factor=prev)
         last = t + 1 == s.rounds
         out_loc = s.cand_loc if last else h.locations[t + 1]
         out_fac = s.cand_factor if last else h.scales[t + 1]

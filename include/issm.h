@@ -361,14 +361,23 @@ int issm_weighted_moments(const void *x, int32_t d, int64_t n,
                           double *mean, double *cov, void *workspace,
                           size_t workspace_bytes, issm_stream_t stream);
 /* As issm_weighted_moments with a precision: ISSM_PREC_TF32 / ISSM_PREC_BF16
- * run one tensor-core pass over FP32 samples about `shift`, accumulating
+ * run a tensor-core pass over FP32 samples about `shift`, accumulating
  * sum w z z^T, sum w z and sum w in FP32 tensor memory and finishing in FP64
- * (d <= 64); NATIVE runs the two-pass SIMT kernels. workspace_bytes >=
+ * (d <= 64; the split products form the Gram matrix of the bf16 hi/lo
+ * operand, so the covariance is semidefinite), and a second pass centred at
+ * the first pass's mean when the first pass's cancellation error
+ * (2^-16 of a diagonal second moment about `shift`) exceeds 2^-8 of that
+ * variance plus 2^-4 of R = sqrt(eps(Float32)) tr(L L^T) / d, L =
+ * `prev_factor` (the previous proposal's d x d factor in `dtype`, column-major;
+ * NULL takes R = 0). NATIVE runs the two-pass SIMT kernels and ignores
+ * `prev_factor`. workspace_bytes >=
  * issm_moments_workspace_bytes(n, d); its last 64 bytes hold the sticky
- * tensor-core timeout word (zero the workspace once when it is created). */
+ * tensor-core timeout word and a completion counter (zero the workspace once
+ * when it is created; every call leaves the counter at zero). */
 int issm_weighted_moments_ws(const void *x, int32_t d, int64_t n,
                              const void *logweights, int32_t dtype,
                              const double *summary, const double *shift,
+                             const void *prev_factor,
                              double *mean, double *cov, int32_t precision,
                              void *workspace, size_t workspace_bytes,
                              issm_stream_t stream);
