@@ -163,6 +163,21 @@ int issm_draw(const issm_bank *bank, const int32_t *slots, int32_t fixed_slot, c
                      radial_uniform_stride, n, samples, failures, index_base, (cudaStream_t)stream);
 }
 
+int issm_draw_philox(const issm_bank *bank, int32_t fixed_slot, uint64_t seed, const uint64_t *counter,
+                     uint64_t offset, const void *radial_normals, int32_t radial_normal_stride,
+                     const void *radial_uniforms, int32_t radial_uniform_stride, int64_t n, void *samples,
+                     uint64_t *failures, int64_t index_base, issm_stream_t stream) {
+    ISSM_TRY(check_bank(bank));
+    if (n < 0) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!samples) return ISSM_E_NULL;
+    if (fixed_slot < 0 || fixed_slot >= bank->count) return ISSM_E_SIZE;
+    if (bank->family == ISSM_STUDENT_T && !radial_normals) return ISSM_E_NULL;
+    return simt_draw_fused(bank, fixed_slot, seed, counter, offset, radial_normals, radial_normal_stride,
+                           radial_uniforms, radial_uniform_stride, n, samples, failures, index_base,
+                           (cudaStream_t)stream);
+}
+
 int issm_mixture_logdensity(const issm_bank *bank, const issm_denominator *den, const void *x, int64_t n,
                             const int32_t *slots, int32_t fixed_slot, void *out_logden, void *out_generating,
                             uint64_t *failures, int64_t index_base, int32_t precision, issm_stream_t stream) {

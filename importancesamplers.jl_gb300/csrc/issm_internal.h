@@ -20,6 +20,9 @@ int simt_round(const issm_bank *b, const issm_denominator *den, const int32_t *s
 int simt_draw(const issm_bank *b, const int32_t *slots, int32_t fixed_slot, const void *normals,
               const void *rn, int rn_stride, const void *ru, int ru_stride, int64_t n, void *samples,
               uint64_t *failures, int64_t index_base, cudaStream_t stream);
+int simt_draw_fused(const issm_bank *b, int32_t fixed_slot, uint64_t seed, const uint64_t *counter,
+                    uint64_t offset, const void *rn, int rn_stride, const void *ru, int ru_stride, int64_t n,
+                    void *samples, uint64_t *failures, int64_t index_base, cudaStream_t stream);
 int simt_append(const issm_bank *b, int slot, const void *logcounts, const void *x, int64_t n, void *lognum,
                 uint64_t *failures, cudaStream_t stream);
 

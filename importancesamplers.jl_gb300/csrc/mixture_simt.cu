@@ -14,6 +14,7 @@
 // reference's exponent-extended solves (src/student_t_range.jl:82-153).
 #include "issm_device.cuh"
 #include "issm_internal.h"
+#include "rng.cuh"
 #include "tcgen05.cuh"
 
 namespace issm {
@@ -49,6 +50,11 @@ template <typename T> struct MixParams {
     int fixed_slot;
     // draw inputs (ROUND)
     const T *normals, *rnormals, *runiforms;
+    // fused normals (fixed-slot factor draws): element e of row i is element
+    // noffset (+ *nbase) + i d + e of the (nseed) normal stream
+    int fused;
+    uint64_t nseed, noffset;
+    const uint64_t *nbase;
     int rn_stride, ru_stride;
     T *samples_out;
     // outputs
@@ -543,59 +549,129 @@ __global__ void __launch_bounds__(128) mixture_simt_kernel(MixParams<T> p) {
 }
 
 // Fixed-slot draws from one factor component, x = mu + L (m z) with the
-// reference's summation order (mu first, then q = 0..r): the factor is staged
-// once per CTA in its own column-major order (column q holds L[., q], so the
-// entries of 4 consecutive rows are one 16-byte load), tiles of 128 normal
-// rows are staged through padded shared memory with coalesced loads, each
-// thread holds its row of m z in registers and forms 4 rows of x at a time
-// (4 independent FMA chains), writing them back over the staged tile, which
-// is then stored coalesced.
+// reference's summation order (mu first, then q = 0..r). A CTA of 256 threads
+// takes a tile of 64 rows:
+//  * the factor is staged once per CTA, column-major (column q holds L[., q],
+//    so 4 consecutive rows of a column are one 16-byte broadcast load), with
+//    its upper triangle zeroed;
+//  * the tile's normals are staged transposed, zT[q][row], from coalesced
+//    loads or, with fused normals, generated there from the counter-based
+//    stream (the tile's elements are contiguous in the stream, so the threads
+//    take its Philox blocks in turn and no normal touches HBM);
+//  * four threads share a row and split its output coordinates where the
+//    triangular work quarters; each forms 4 coordinates at a time as
+//    independent FMA chains over q = 0..r0+3 (the zero upper triangle makes
+//    the extra terms exact no-ops), reading z[q] of 32 consecutive rows from
+//    32 banks, so the loops stay compact (a fully unrolled triangle overflows
+//    the instruction cache);
+//  * x goes to a row-major staging tile and is stored coalesced.
+constexpr int kDrawRows = 64;     // rows per tile
+constexpr int kDrawParts = 4;     // threads per row
+template <int D> struct DrawSplit {
+    // first output coordinate of part i: 4 * ceil(D sqrt(i / 4) / 4), the triangle's quarters
+    static constexpr int at(int i) {
+        return i == 0 ? 0 : i >= 4 ? D : D == 64 ? (i == 1 ? 32 : i == 2 ? 44 : 56)
+                                       : D == 32 ? (i == 1 ? 16 : i == 2 ? 24 : 28)
+                                       : D == 16 ? (i == 1 ? 8 : i == 2 ? 12 : 16)
+                                                 : D;
+    }
+};
+
 template <typename T, int D>
-__global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
-    constexpr int LC = D + 4;  // column stride of the staged factor (16-byte aligned columns)
-    constexpr int LZ = D + 4;  // row stride of the staged tile
+__global__ void __launch_bounds__(kDrawRows * kDrawParts) draw_fixed_kernel(MixParams<T> p) {
+    constexpr int LC = D + 4;          // column stride of the staged factor (16-byte aligned columns)
+    constexpr int LR = kDrawRows + 4;  // row stride of zT (per coordinate)
+    constexpr int LX = D + 4;          // row stride of the x tile
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *Lc = reinterpret_cast<T *>(smem_raw);  // D columns of LC
-    T *mus = Lc + D * LC;
-    T *zt = mus + D;                           // 128 x LZ
+    T *mus = Lc + D * LC;                      // D
+    T *zT = mus + D;                           // D x LR
+    T *xs = zT + D * LR;                       // kDrawRows x LX
+    __shared__ T s_mult[kDrawRows];
+    __shared__ int s_bad[kDrawRows];
     const int d = p.d, k = p.fixed_slot, tid = threadIdx.x;
+    const int row = tid % kDrawRows, part = tid / kDrawRows;  // warp-uniform parts
     const T *Lk = p.scales + (size_t)k * d * d;
-    for (int e = tid; e < D * LC; e += blockDim.x) {
-        const int q = e / LC, r = e - q * LC;
-        Lc[e] = (q < d && r < d) ? Lk[(size_t)q * d + r] : T(0);
+    // rows of whole 16-byte vectors, both buffers 16-byte aligned
+    const bool vec = (d * sizeof(T)) % 16 == 0 && (p.fused || (reinterpret_cast<uintptr_t>(p.normals) & 15) == 0) &&
+                     (reinterpret_cast<uintptr_t>(p.samples_out) & 15) == 0;
+    if (d == D && (reinterpret_cast<uintptr_t>(Lk) & 15) == 0) {
+        // every column in flight at once (16-byte asynchronous copies; the padding is never read)
+        constexpr int V = 16 / sizeof(T), CV = D / V;
+        for (int e = tid; e < D * CV; e += blockDim.x) {
+            const int q = e / CV, c = e - q * CV;
+            tc::cp_async16(Lc + q * LC + c * V, Lk + (size_t)q * D + c * V);
+        }
+        tc::cp_async_commit();
+        tc::cp_async_wait_all();
+        __syncthreads();
+        for (int e = tid; e < D * D; e += blockDim.x) {
+            const int q = e / D, r = e - q * D;
+            if (r < q) Lc[q * LC + r] = T(0);
+        }
+    } else {
+        for (int e = tid; e < D * LC; e += blockDim.x) {
+            const int q = e / LC, r = e - q * LC;
+            Lc[e] = (q < d && r < d && r >= q) ? Lk[(size_t)q * d + r] : T(0);
+        }
     }
     for (int r = tid; r < D; r += blockDim.x) mus[r] = r < d ? p.loc[(size_t)k * d + r] : T(0);
     const T dof = p.family == ISSM_STUDENT_T ? p.dofs[k] : T(0);
-    // rows of whole 16-byte vectors, both buffers 16-byte aligned
-    const bool vec = (d * sizeof(T)) % 16 == 0 && (reinterpret_cast<uintptr_t>(p.normals) & 15) == 0 &&
-                     (reinterpret_cast<uintptr_t>(p.samples_out) & 15) == 0;
+    const uint64_t noff = p.fused ? p.noffset + (p.nbase ? *p.nbase : 0ull) : 0ull;
+    // coordinates d..D-1 of z stay zero
+    for (int e = tid; e < (D - d) * LR; e += blockDim.x) zT[d * LR + e] = T(0);
     __syncthreads();
-    const int64_t ntiles = (p.n + 127) / 128;
+    const int lo = DrawSplit<D>::at(part), hi = DrawSplit<D>::at(part + 1);
+    const int64_t ntiles = (p.n + kDrawRows - 1) / kDrawRows;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int64_t row0 = tile * 128;
-        const int rows = (int)min((int64_t)128, p.n - row0);
-        const T *nz = p.normals + row0 * d;
-        if (vec) {
-            // 16-byte asynchronous copies, all of the tile in flight at once
-            constexpr int V = 16 / sizeof(T);
-            const int dv = d / V;
-            for (int e = tid; e < rows * dv; e += blockDim.x) {
-                const int r = e / dv, c = e - r * dv;
-                tc::cp_async16(zt + r * LZ + c * V, nz + (size_t)e * V);
+        const int64_t row0 = tile * kDrawRows;
+        const int rows = (int)min((int64_t)kDrawRows, p.n - row0);
+        if (p.fused) {
+            using NB = NormalBlock<T>;
+            const uint64_t first = noff + (uint64_t)row0 * d;
+            const int count = rows * d;
+            const uint64_t b0 = first >> NB::kShift;
+            if (d == D && (first & (NB::kPer - 1)) == 0) {
+                // every Philox block is kPer consecutive coordinates of one row;
+                // consecutive lanes take consecutive rows (conflict-free stores into zT)
+                constexpr int BPR = D / NB::kPer;
+                for (int j = tid; j < kDrawRows * BPR; j += blockDim.x) {
+                    const int r = j % kDrawRows, cb = j / kDrawRows;
+                    if (r >= rows) continue;
+                    T v[NB::kPer];
+                    NB::eval(b0 + (uint64_t)(r * BPR + cb), p.nseed, v);
+#pragma unroll
+                    for (int l = 0; l < NB::kPer; ++l) zT[(cb * NB::kPer + l) * LR + r] = v[l];
+                }
+            } else {
+                const int nb = (int)(((first + (uint64_t)count - 1) >> NB::kShift) - b0 + 1);
+                for (int j = tid; j < nb; j += blockDim.x) {
+                    const uint64_t blk = b0 + (uint64_t)j;
+                    T v[NB::kPer];
+                    NB::eval(blk, p.nseed, v);
+                    const int q0 = (int)(int64_t)((blk << NB::kShift) - first);  // negative in a split first block
+                    int r = q0 >= 0 ? q0 / d : -1;
+                    int c = q0 - r * d;
+#pragma unroll
+                    for (int l = 0; l < NB::kPer; ++l) {
+                        if (c >= d) { c -= d; ++r; }
+                        if (q0 + l >= 0 && q0 + l < count) zT[c * LR + r] = v[l];
+                        ++c;
+                    }
+                }
             }
-            tc::cp_async_commit();
-            tc::cp_async_wait<0>();
         } else {
+            const T *nz = p.normals + row0 * d;
             for (int e = tid; e < rows * d; e += blockDim.x) {
                 const int r = e / d, c = e - r * d;
-                zt[r * LZ + c] = nz[e];
+                zT[c * LR + r] = nz[e];
             }
         }
-        __syncthreads();
-        if (tid < rows) {
-            const int64_t i = row0 + tid;
+        // the radial multiplier of each row (Student-t), once per row
+        if (part == 0 && row < rows) {
             T m = T(1);
             if (p.family == ISSM_STUDENT_T) {
+                const int64_t i = row0 + row;
                 uint16_t rr;
                 m = radial_multiplier(dof, p.rnormals + (size_t)i * p.rn_stride,
                                       p.runiforms ? p.runiforms + (size_t)i * p.ru_stride : nullptr,
@@ -605,43 +681,52 @@ __global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
                     m = qnan<T>();
                 }
             }
-            T *zrow = zt + tid * LZ;
-            T z[D];
-#pragma unroll
-            for (int q = 0; q < D; ++q) z[q] = q < d ? zrow[q] * m : T(0);
-            bool valid = true;
-#pragma unroll
-            for (int r0 = 0; r0 < D; r0 += 4) {
-                T v0 = mus[r0], v1 = mus[r0 + 1], v2 = mus[r0 + 2], v3 = mus[r0 + 3];
-#pragma unroll
-                for (int q = 0; q < r0 + 4; ++q) {
-                    const T *col = Lc + q * LC + r0;
-                    const T l0 = col[0], l1 = col[1], l2 = col[2], l3 = col[3];
-                    if (q <= r0) v0 += l0 * z[q];
-                    if (q <= r0 + 1) v1 += l1 * z[q];
-                    if (q <= r0 + 2) v2 += l2 * z[q];
-                    v3 += l3 * z[q];
-                }
-                if (r0 < d) { zrow[r0] = v0; valid &= (bool)isfinite(v0); }
-                if (r0 + 1 < d) { zrow[r0 + 1] = v1; valid &= (bool)isfinite(v1); }
-                if (r0 + 2 < d) { zrow[r0 + 2] = v2; valid &= (bool)isfinite(v2); }
-                if (r0 + 3 < d) { zrow[r0 + 3] = v3; valid &= (bool)isfinite(v3); }
-            }
-            if (!valid) record_failure(p.failures, p.index_base + i + 1, 0, ISSM_REASON_GENERATED_NONFINITE);
+            s_mult[row] = m;
+            s_bad[row] = 0;
         }
         __syncthreads();
+        if (row < rows) {
+            const T m = s_mult[row];
+            const bool scaled = p.family == ISSM_STUDENT_T;
+            bool valid = true;
+            for (int r0 = lo; r0 < hi; r0 += 4) {
+                T v0 = mus[r0], v1 = mus[r0 + 1], v2 = mus[r0 + 2], v3 = mus[r0 + 3];
+                for (int q0 = 0; q0 <= r0; q0 += 4) {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int q = q0 + u;
+                        const T z = scaled ? zT[q * LR + row] * m : zT[q * LR + row];
+                        const T *col = Lc + q * LC + r0;
+                        v0 += col[0] * z;
+                        v1 += col[1] * z;
+                        v2 += col[2] * z;
+                        v3 += col[3] * z;
+                    }
+                }
+                T *xr = xs + row * LX + r0;
+                xr[0] = v0; xr[1] = v1; xr[2] = v2; xr[3] = v3;
+                if (r0 < d) valid &= (bool)isfinite(v0);
+                if (r0 + 1 < d) valid &= (bool)isfinite(v1);
+                if (r0 + 2 < d) valid &= (bool)isfinite(v2);
+                if (r0 + 3 < d) valid &= (bool)isfinite(v3);
+            }
+            if (!valid) s_bad[row] = 1;
+        }
+        __syncthreads();
+        if (part == 0 && row < rows && s_bad[row])
+            record_failure(p.failures, p.index_base + row0 + row + 1, 0, ISSM_REASON_GENERATED_NONFINITE);
         T *out = p.samples_out + row0 * d;
         if (vec) {
             constexpr int V = 16 / sizeof(T);
             const int dv = d / V;
             for (int e = tid; e < rows * dv; e += blockDim.x) {
                 const int r = e / dv, c = e - r * dv;
-                *reinterpret_cast<uint4 *>(out + (size_t)e * V) = *reinterpret_cast<const uint4 *>(zt + r * LZ + c * V);
+                *reinterpret_cast<uint4 *>(out + (size_t)e * V) = *reinterpret_cast<const uint4 *>(xs + r * LX + c * V);
             }
         } else {
             for (int e = tid; e < rows * d; e += blockDim.x) {
                 const int r = e / d, c = e - r * d;
-                out[e] = zt[r * LZ + c];
+                out[e] = xs[r * LX + c];
             }
         }
         __syncthreads();
@@ -651,16 +736,17 @@ __global__ void __launch_bounds__(128) draw_fixed_kernel(MixParams<T> p) {
 template <typename T, int D, bool FACTOR>
 static int launch_simt(MixParams<T> p, cudaStream_t stream) {
     if (FACTOR && p.mode == kModeDraw && p.slots == nullptr && p.samples_out != nullptr) {
-        const size_t smem = sizeof(T) * ((size_t)D * (D + 4) + D + (size_t)128 * (D + 4));
+        const size_t smem = sizeof(T) * ((size_t)D * (D + 4) + D + (size_t)D * (kDrawRows + 4) +
+                                         (size_t)kDrawRows * (D + 4));
         auto kern = draw_fixed_kernel<T, D>;
         if (smem > 48 * 1024) {
             const int e = allow_dynamic_smem((const void *)kern);
             if (e) return e;
         }
-        const int64_t tiles = (p.n + 127) / 128;
-        const int blocks = (int)min(tiles, (int64_t)kSMs * 4);
+        const int64_t tiles = (p.n + kDrawRows - 1) / kDrawRows;
+        const int blocks = (int)min(tiles, (int64_t)kSMs * 64);
         if (blocks < 1) return 0;
-        { kern<<<blocks, 128, smem, stream>>>(p); note_launch(); }
+        { kern<<<blocks, kDrawRows * kDrawParts, smem, stream>>>(p); note_launch(); }
         return (int)cudaGetLastError();
     }
     using Ly = Layout<D, FACTOR>;
@@ -782,6 +868,32 @@ int simt_draw(const issm_bank *b, const int32_t *slots, int32_t fixed_slot, cons
     return simt_round_t<double>(b, nullptr, slots, fixed_slot, normals, rn, rn_stride, ru, ru_stride,
                                 nullptr, n, samples, nullptr, nullptr, nullptr, failures, index_base,
                                 kModeDraw, stream);
+}
+
+template <typename T>
+static int simt_draw_fused_t(const issm_bank *b, int fixed_slot, uint64_t seed, const uint64_t *counter,
+                             uint64_t offset, const void *rn, int rn_stride, const void *ru, int ru_stride,
+                             int64_t n, void *samples, uint64_t *failures, int64_t index_base,
+                             cudaStream_t stream) {
+    auto p = params_from<T>(b, nullptr);
+    p.n = n; p.slots = nullptr; p.fixed_slot = fixed_slot;
+    p.rnormals = (const T *)rn; p.rn_stride = rn_stride;
+    p.runiforms = (const T *)ru; p.ru_stride = ru_stride;
+    p.samples_out = (T *)samples;
+    p.failures = failures; p.index_base = index_base; p.mode = kModeDraw;
+    p.fused = 1; p.nseed = seed; p.nbase = counter; p.noffset = offset;
+    return dispatch_simt(p, stream);
+}
+
+int simt_draw_fused(const issm_bank *b, int32_t fixed_slot, uint64_t seed, const uint64_t *counter,
+                    uint64_t offset, const void *rn, int rn_stride, const void *ru, int ru_stride, int64_t n,
+                    void *samples, uint64_t *failures, int64_t index_base, cudaStream_t stream) {
+    if (b->scale_kind != ISSM_SCALE_FACTOR) return ISSM_E_UNSUPPORTED;
+    if (b->dtype == ISSM_F32)
+        return simt_draw_fused_t<float>(b, fixed_slot, seed, counter, offset, rn, rn_stride, ru, ru_stride, n,
+                                        samples, failures, index_base, stream);
+    return simt_draw_fused_t<double>(b, fixed_slot, seed, counter, offset, rn, rn_stride, ru, ru_stride, n,
+                                     samples, failures, index_base, stream);
 }
 
 template <typename T>

@@ -1,8 +1,9 @@
 // reduce.cu — log-weight reductions (HBM-bound, one read of the log weights).
 //
 // logweight_summary: single pass; each thread keeps an online (max, S, S2)
-// with S = sum exp(l - max) computed in the weight dtype and accumulated in
-// FP64; warps and blocks merge with the reference's rescaling rule
+// with S = sum exp(l - max) computed in the weight dtype (FP32 data: Kahan
+// FP32 per thread, then compensated FP32 pairs; FP64 data: FP64); warps and
+// blocks merge with the reference's rescaling rule
 // (_merge_logweight_moments, src/execution.jl:166-173); the last block to
 // finish merges the per-block partials, so one launch yields the final three
 // FP64 words with no host round trip.
@@ -71,7 +72,8 @@ template <typename T> __device__ Moments3 block_merge3(Moments3 v) {
 // Per-thread running (max, S, S2). FP64 data accumulates in FP64; FP32 data
 // accumulates in FP32 with Kahan compensation (error about 2 ulp of the
 // thread's sum however many terms it takes, and none of the slow FP64
-// additions per element), then every merge above the thread is FP64.
+// additions per element); its merges above the thread carry hi + lo FP32
+// pairs (summary_finish below).
 template <typename T> struct ThreadSums {
     T m = -num<T>::inf();
     double s = 0.0, s2 = 0.0;
@@ -123,9 +125,10 @@ template <> struct ThreadSums<float> {
 
 // Block merge of the threads' (max, S, S2), then the last block to finish
 // merges the per-block partials in the same launch and writes the FP64 words.
-template <typename T>
-__device__ void summary_finish(Moments3 thread_sums, double *out, Moments3 *partials, unsigned int *counter) {
-    Moments3 v = block_merge3<T>(thread_sums);
+// FP64 data: FP64 throughout.
+__device__ void summary_finish(const ThreadSums<double> &ts, double *out, Moments3 *partials,
+                               unsigned int *counter) {
+    Moments3 v = block_merge3<double>(ts.result());
     __shared__ bool last;
     if (threadIdx.x == 0) {
         partials[blockIdx.x] = v;
@@ -144,21 +147,124 @@ __device__ void summary_finish(Moments3 thread_sums, double *out, Moments3 *part
         if (bs == 0.0) continue;
         if (ps == 0.0 || bm > pm) {
             if (ps != 0.0) {
-                const double f = scale_factor<T>(pm, bm);
+                const double f = scale_factor<double>(pm, bm);
                 ps *= f;
                 ps2 *= f * f;
             }
             pm = bm;
         }
-        const double f = scale_factor<T>(bm, pm);
+        const double f = scale_factor<double>(bm, pm);
         ps += bs * f;
         ps2 += bs2 * (f * f);
     }
-    const Moments3 acc = block_merge3<T>(Moments3{pm, ps, ps2});
+    const Moments3 acc = block_merge3<double>(Moments3{pm, ps, ps2});
     if (threadIdx.x == 0) {
         out[0] = acc.s == 0.0 ? -INFINITY : acc.m;
         out[1] = acc.s;
         out[2] = acc.s2;
+        *counter = 0u;
+    }
+}
+
+// FP32 data: every merge in FP32 with the sums carried as unevaluated pairs
+// hi + lo (error-free two-sum; about 44 significant bits), because FP64
+// instructions hold a warp's FP64 pipe for about 64 cycles on this GPU and a
+// few dozen of them per thread would cost more than the pass's HBM traffic.
+// Only the last block's three output words are formed in FP64.
+struct Pair {
+    float h, l;
+};
+__device__ __forceinline__ Pair pair_add(Pair a, Pair b) {
+    const float s = a.h + b.h, bb = s - a.h;
+    const float e = ((a.h - (s - bb)) + (b.h - bb)) + (a.l + b.l);
+    const float h = s + e;
+    return Pair{h, e - (h - s)};
+}
+__device__ __forceinline__ Pair pair_scale(Pair a, float f) {
+    const float p = a.h * f;
+    const float l = fmaf(a.l, f, fmaf(a.h, f, -p));
+    const float h = p + l;
+    return Pair{h, l - (h - p)};
+}
+__device__ __forceinline__ Pair shfl_pair(Pair a, int off) {
+    return Pair{__shfl_xor_sync(0xffffffffu, a.h, off), __shfl_xor_sync(0xffffffffu, a.l, off)};
+}
+struct Partial3f {
+    float m;
+    Pair s, s2;
+};
+static_assert(sizeof(Partial3f) <= sizeof(Moments3), "FP32 partials reuse the FP64 partial slots");
+
+// block max of m over entries with s != 0, then sum s f, s2 f^2 with f = exp(m - M)
+__device__ Partial3f block_merge3f(float m, Pair s, Pair s2) {
+    __shared__ float red_m[32];
+    __shared__ Pair red_s[32], red_s2[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    const bool live = s.h != 0.f;
+    float wm = live ? m : -INFINITY;
+    for (int off = 16; off > 0; off >>= 1) wm = fmaxf(wm, __shfl_xor_sync(0xffffffffu, wm, off));
+    if (lane == 0) red_m[warp] = wm;
+    __syncthreads();
+    float M = -INFINITY;
+    for (int w = 0; w < nw; ++w) M = fmaxf(M, red_m[w]);
+    Pair a{0.f, 0.f}, b{0.f, 0.f};
+    if (live) {
+        const float f = expf(m - M);
+        a = pair_scale(s, f);
+        b = pair_scale(s2, f * f);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        a = pair_add(a, shfl_pair(a, off));
+        b = pair_add(b, shfl_pair(b, off));
+    }
+    if (lane == 0) {
+        red_s[warp] = a;
+        red_s2[warp] = b;
+    }
+    __syncthreads();
+    Pair ta{0.f, 0.f}, tb{0.f, 0.f};
+    for (int w = 0; w < nw; ++w) {
+        ta = pair_add(ta, red_s[w]);
+        tb = pair_add(tb, red_s2[w]);
+    }
+    __syncthreads();
+    return Partial3f{M, ta, tb};
+}
+
+__device__ void summary_finish(const ThreadSums<float> &ts, double *out, Moments3 *partials_d,
+                               unsigned int *counter) {
+    Partial3f *partials = reinterpret_cast<Partial3f *>(partials_d);
+    const Partial3f v = block_merge3f(ts.m, Pair{ts.s, -ts.cs}, Pair{ts.s2, -ts.cs2});
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = v;
+        __threadfence();
+        unsigned int done = atomicAdd(counter, 1u);
+        last = (done == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    // the last block: this thread's partials about their own maximum, then the block merge
+    const volatile float *pv = reinterpret_cast<const volatile float *>(partials);
+    constexpr int kW = sizeof(Partial3f) / sizeof(float);
+    float pm = -INFINITY;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+        if (pv[kW * b + 1] != 0.f) pm = fmaxf(pm, pv[kW * b]);
+    Pair ps{0.f, 0.f}, ps2{0.f, 0.f};
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+        const Pair bs{pv[kW * b + 1], pv[kW * b + 2]}, bs2{pv[kW * b + 3], pv[kW * b + 4]};
+        if (bs.h == 0.f) continue;
+        const float f = expf(pv[kW * b] - pm);
+        ps = pair_add(ps, pair_scale(bs, f));
+        ps2 = pair_add(ps2, pair_scale(bs2, f * f));
+    }
+    const Partial3f acc = block_merge3f(pm, ps, ps2);
+    if (threadIdx.x == 0) {
+        const double S = (double)acc.s.h + (double)acc.s.l;
+        out[0] = S == 0.0 ? -INFINITY : (double)acc.m;
+        out[1] = S;
+        out[2] = (double)acc.s2.h + (double)acc.s2.l;
         *counter = 0u;
     }
 }
@@ -184,7 +290,7 @@ __global__ void __launch_bounds__(256) summary_kernel(const T *__restrict__ lw, 
     } else {
         for (int64_t i = t0; i < n; i += stride) ts.add(lw[i]);
     }
-    summary_finish<T>(ts.result(), out, partials, counter);
+    summary_finish(ts, out, partials, counter);
 }
 
 // AMIS log weights of rounds 1..t and their summary in one pass
@@ -237,7 +343,7 @@ __global__ void __launch_bounds__(256) form_summary_kernel(const T *__restrict__
         if (round_ids && round_ids[i] == 0) continue;
         one(i, lt[i], lnum[i]);
     }
-    summary_finish<T>(ts.result(), out, partials, counter);
+    summary_finish(ts, out, partials, counter);
 }
 
 static int summary_blocks(int64_t n) {

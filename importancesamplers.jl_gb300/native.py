@@ -73,6 +73,7 @@ SIGNATURES = [
     ("issm_counter_advance", C.c_int, [_p, _u64, _p]),
     ("issm_static_assign", C.c_int, [_p, _i32, _p, _i64, _i32, _p, _i32, _p]),
     ("issm_draw", C.c_int, [_bank, _p, _i32, _p, _p, _i32, _p, _i32, _i64, _p, _p, _i64, _p]),
+    ("issm_draw_philox", C.c_int, [_bank, _i32, _u64, _p, _u64, _p, _i32, _p, _i32, _i64, _p, _p, _i64, _p]),
     ("issm_mixture_logdensity", C.c_int, [_bank, _den, _p, _i64, _p, _i32, _p, _p, _p, _i64, _i32, _p]),
     ("issm_mis_round", C.c_int, [_bank, _den, _p, _p, _p, _i32, _p, _i32, _p, _i64, _p, _p, _p, _p, _p,
                                  _i32, _p]),

@@ -79,6 +79,20 @@ def draw(bank, normals, n, slots=None, fixed_slot=0, radial_normals=None, rn_str
     return out
 
 
+def draw_philox(bank, n, seed, counter=None, offset=0, fixed_slot=0, radial_normals=None, rn_stride=0,
+                radial_uniforms=None, ru_stride=0, failures=None, index_base=0, out=None, bank_ref=None):
+    """draw() from a factor bank with the standard normals generated in the
+    kernel: element offset (+ counter[0]) + i d + e of the `seed` normal
+    stream (fill_normals_at) for row i, coordinate e. Bitwise equal to
+    fill_normals_at followed by draw()."""
+    out = torch.empty(int(n), bank.d, dtype=bank.dtype, device=bank.locations.device) if out is None else out
+    native.call("issm_draw_philox", bank_ref or bank.ref(), int(fixed_slot), int(seed) & (2 ** 64 - 1),
+                native.ptr(counter), int(offset), native.ptr(radial_normals), int(rn_stride),
+                native.ptr(radial_uniforms), int(ru_stride), int(n), native.ptr(out), native.ptr(failures),
+                int(index_base), _s())
+    return out
+
+
 def _tc_workspace(count, d, device):
     nb = native.lib().issm_tc_workspace_bytes(int(count), int(d))
     # the error word sits in the last 64 bytes of whatever buffer is passed: size it exactly

@@ -151,6 +151,17 @@ class PreparedSampler:
         self.offset += int(n) + 8
         return out
 
+    def normal_stream(self, n):
+        """(seed, device counter or None, offset) of the next n standard
+        normals, advanced as normals(n) would be; None when normals() has been
+        replaced on the instance (prefilled batches), so callers take the
+        buffer path."""
+        if "normals" in self.__dict__:
+            return None
+        out = (self.seed, self.counter, self.offset)
+        self.offset += int(n) + 8
+        return out
+
     def uniforms(self, n, dtype):
         if self.counter is not None:
             out = ops.fill_uniforms_at(n, dtype, self.device, self.seed, self.counter, self.offset)
@@ -343,12 +354,19 @@ def _moment_body(s, is_npmc):
         fail = s.round_failures[t]
         view = h.view(t + 1)
         es = h.scales.element_size()
-        with _Span(s, "draw", n_new * d * es * 2):
-            normals = s.normals(n_new * d, dt)
+        with _Span(s, "draw", n_new * d * es):
+            # standard normals generated inside the draw kernel (no normal buffer)
+            stream = s.normal_stream(n_new * d)
+            normals = s.normals(n_new * d, dt) if stream is None else None
             rn, ru = _radial_buffers(s, n_new, dt)
             x_new = s.samples[n_old:n_tot]
-            ops.draw(h, normals, n_new, fixed_slot=t, radial_normals=rn, rn_stride=s.rn_stride,
-                     radial_uniforms=ru, ru_stride=s.ru_stride, failures=fail, out=x_new, bank_ref=view)
+            if stream is None:
+                ops.draw(h, normals, n_new, fixed_slot=t, radial_normals=rn, rn_stride=s.rn_stride,
+                         radial_uniforms=ru, ru_stride=s.ru_stride, failures=fail, out=x_new, bank_ref=view)
+            else:
+                ops.draw_philox(h, n_new, stream[0], stream[1], stream[2], fixed_slot=t, radial_normals=rn,
+                                rn_stride=s.rn_stride, radial_uniforms=ru, ru_stride=s.ru_stride, failures=fail,
+                                out=x_new, bank_ref=view)
         with _Span(s, "target", n_new * (d + 1) * es):
             s.bound_target.evaluate(x_new, out=s.logtargets[n_old:n_tot], precision=s.precision)
             ops.check_target_values(s.logtargets[n_old:n_tot], s.round_ids[n_old:n_tot], fail)

@@ -173,6 +173,21 @@ int issm_draw(const issm_bank *bank, const int32_t *slots, int32_t fixed_slot,
               int32_t radial_uniform_stride, int64_t n, void *samples,
               uint64_t *failures, int64_t index_base, issm_stream_t stream);
 
+/* issm_draw from component `fixed_slot` of a factor bank with the standard
+ * normals generated in the kernel: row i, coordinate e takes element
+ * offset + (*counter if counter) + i d + e of the (seed) stream that
+ * issm_fill_normals_at writes, so the samples are bitwise those of
+ * issm_fill_normals_at followed by issm_draw, and no normal is stored.
+ * ISSM_E_UNSUPPORTED for scalar or spherical scales. No reference
+ * counterpart: the reference fills a normal buffer and then draws from it
+ * (_launch_prefilled_amis_factor_batch!, src/amis_execution.jl:162-194). */
+int issm_draw_philox(const issm_bank *bank, int32_t fixed_slot, uint64_t seed,
+                     const uint64_t *counter, uint64_t offset,
+                     const void *radial_normals, int32_t radial_normal_stride,
+                     const void *radial_uniforms, int32_t radial_uniform_stride,
+                     int64_t n, void *samples, uint64_t *failures,
+                     int64_t index_base, issm_stream_t stream);
+
 /* ---- balance-heuristic denominators ------------------------------------ */
 /* out_logden[i] = log sum_{k in terms(i)} exp(coef_k + log q_k(x_i)),
  * out_generating[i] = log q_{slots[i]}(x_i) (optional). Records

@@ -202,6 +202,35 @@ def test_mis_round_vs_oracle(issm, orc, cuda, dtype, family):
     assert int(fail[0].item()) == int(np.count_nonzero(rs))
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("d", [1, 3, 5, 16, 64])
+@pytest.mark.parametrize("family", ["gaussian", "student"])
+def test_draw_philox_matches_fill_then_draw(issm, orc, cuda, dtype, d, family):
+    """Normals generated inside the draw kernel give bitwise the samples of
+    fill_normals_at + draw, for stream offsets that split Philox blocks, with
+    and without a device counter, over several 128-row tiles and a ragged one."""
+    rng = np.random.default_rng(d)
+    _, db, _ = make_bank(issm, orc, rng, d, 3, family, "factor", dtype, cuda)
+    n, seed = 1000, 0xC0FFEE
+    rn_stride, ru_stride = (8, 8) if family == "student" else (0, 0)
+    T = lambda a: None if a is None else torch.tensor(a, device=cuda)  # noqa: E731
+    rn = T(rng.normal(size=n * 8).astype(dtype)) if family == "student" else None
+    ru = T(rng.random(size=n * 8).astype(dtype)) if family == "student" else None
+    for counter_value, offset in ((None, 0), (None, 3), (7, 5), (4096, 0)):
+        counter = None if counter_value is None else torch.tensor([counter_value], dtype=torch.int64, device=cuda)
+        f1, f2 = issm.ops.new_failures(cuda), issm.ops.new_failures(cuda)
+        if counter is None:
+            normals = issm.ops.fill_normals(n * d, tdt(dtype), cuda, seed=seed, offset=offset)
+        else:
+            normals = issm.ops.fill_normals_at(n * d, tdt(dtype), cuda, seed, counter, offset)
+        a = issm.ops.draw(db, normals, n, fixed_slot=1, radial_normals=rn, rn_stride=rn_stride,
+                          radial_uniforms=ru, ru_stride=ru_stride, failures=f1)
+        b = issm.ops.draw_philox(db, n, seed, counter, offset, fixed_slot=1, radial_normals=rn,
+                                 rn_stride=rn_stride, radial_uniforms=ru, ru_stride=ru_stride, failures=f2)
+        assert torch.equal(a, b), (counter_value, offset)
+        assert torch.equal(f1, f2)
+
+
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 def test_amis_append_and_form_vs_oracle(issm, orc, cuda, dtype, golden):
     c = golden["amis_retrospective_mixture"]
