@@ -56,6 +56,20 @@ class Target(C.Structure):
                 ("a", C.c_void_p), ("b", C.c_void_p), ("c", C.c_void_p), ("p0", C.c_double), ("p1", C.c_double)]
 
 
+class AmisRunDesc(C.Structure):
+    """issm_amis_run_desc (include/issm.h)."""
+    _fields_ = [("history", Bank), ("target", C.c_void_p), ("rounds", C.c_int32), ("precision", C.c_int32),
+                ("round_sizes", C.c_void_p), ("logconstant", C.c_double), ("seed", C.c_uint64),
+                ("normal_offset", C.c_uint64), ("counter", C.c_void_p), ("logcounts", C.c_void_p),
+                ("round_ids_init", C.c_void_p), ("initial_location", C.c_void_p), ("initial_factor", C.c_void_p),
+                ("initial_lognormalizer", C.c_void_p), ("samples", C.c_void_p), ("logtargets", C.c_void_p),
+                ("lognum", C.c_void_p), ("logweights", C.c_void_p), ("round_ids", C.c_void_p),
+                ("summaries", C.c_void_p), ("round_failures", C.c_void_p), ("mean", C.c_void_p),
+                ("cov", C.c_void_p), ("shift", C.c_void_p), ("cand_location", C.c_void_p),
+                ("cand_factor", C.c_void_p), ("cand_lognormalizer", C.c_void_p), ("workspace", C.c_void_p),
+                ("workspace_bytes", C.c_size_t)]
+
+
 TARGET_GAUSS_MIX, TARGET_STUDENT_T, TARGET_LINREG, TARGET_LOGISTIC, TARGET_STD_NORMAL, TARGET_QUADRATIC = range(6)
 
 # (name, restype, argtypes) for every entry point of include/issm.h
@@ -101,6 +115,8 @@ SIGNATURES = [
     ("issm_fit_factor_ex", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _p, _p, _p, _p, _p, _i64, _p]),
     ("issm_target_logdensity", C.c_int, [C.POINTER(Target), _p, _i64, _p, _p]),
     ("issm_tc_selftest", C.c_int, [_p, _p, _p, _i32, _i32, _i32, _p, _p]),
+    ("issm_amis_run_workspace_bytes", _sz, [_i32, _i64, _i32]),
+    ("issm_amis_run", C.c_int, [C.POINTER(AmisRunDesc), _p]),
     ("issm_tc_workspace_bytes", _sz, [_i32, _i32]),
     ("issm_invert_factors", C.c_int, [_bank, _i32, _i32, _p, _p]),
     ("issm_mixture_logdensity_ws", C.c_int, [_bank, _den, _p, _i64, _p, _i32, _p, _p, _p, _i64, _i32, _p, _sz,

@@ -8,6 +8,7 @@ where the per-round summaries and failure words are read back in one copy.
 The reference instead synchronises after nearly every launch
 (src/mis_execution.jl:840) and reads scalars every round.
 """
+import ctypes
 import math
 from fractions import Fraction
 
@@ -18,7 +19,7 @@ from . import native, ops
 from .bank import DeviceHistory, pack
 from .methods import (AMIS, NPMC, DeterministicMixturePMC, GlobalResampling, ImportanceSampling, LocalResampling,
                       PartialDeterministicMixture, RandomMixture, StandardMIS)
-from .proposals import STUDENT_T
+from .proposals import GAUSSIAN, STUDENT_T
 from .results import (AMISRoundError, DMPMCRoundError, NPMCRoundError, SamplerExecutionError, WeightedSamples,
                       phase_of)
 
@@ -301,8 +302,10 @@ def _prepare_moment(s):
     dofs = None if p.family != STUDENT_T else [float(p.dof)]
     s.rn_stride, s.ru_stride = _radial_strides(dofs)
     s.bound_target = s.target.bind(s.device, dt)
+    # output_size given: no device-to-host read of the total
     s.round_ids_init = torch.repeat_interleave(torch.arange(1, s.rounds + 1, device=dev),
-                                               torch.tensor(s.schedule, device=dev)).contiguous()
+                                               torch.tensor(s.schedule, device=dev),
+                                               output_size=total).contiguous()
     s.round_ids = s.round_ids_init.clone()
 
 
@@ -411,11 +414,92 @@ def _moment_body(s, is_npmc):
     ops.counter_advance(s.counter, s.offset)
 
 
+def native_body_eligible(s):
+    """issm_amis_run covers AMIS with a Gaussian factor history, a native
+    target, generated normals and no per-span profiling."""
+    from .targets import _Bound
+
+    h = getattr(s, "history", None)
+    return (isinstance(s.algorithm, AMIS) and h is not None and h.family == GAUSSIAN and h.d <= 64
+            and h.scale_kind == native.SCALE_FACTOR and isinstance(s.bound_target, _Bound) and s.profile is None
+            and "normals" not in s.__dict__ and "uniforms" not in s.__dict__
+            and (s.precision == native.PREC_NATIVE or h.dtype == torch.float32))
+
+
+def _native_body(s):
+    """Every launch of one AMIS run through one issm_amis_run call: the same
+    library calls as _moment_body, issued from native code."""
+    h = s.history
+    if s.precision != native.PREC_NATIVE:
+        h.attach_inverse_factors(0, 0)  # allocate; the run inverts slot 0 itself
+    d, total = h.d, int(s.offsets[-1])
+    nb = native.lib().issm_amis_run_workspace_bytes(d, total, s.rounds)
+    ws = native.workspace(nb, s.device, "run", zero=True)
+    s.run_workspace = ws
+    sizes = (ctypes.c_int64 * s.rounds)(*[int(v) for v in s.schedule])
+    bank = h.view(h.count)._obj
+    loc0, fac0, ln0 = s.committed
+    desc = native.AmisRunDesc(bank, ctypes.cast(ctypes.byref(s.bound_target.struct), ctypes.c_void_p), s.rounds,
+                              int(s.precision), ctypes.cast(sizes, ctypes.c_void_p), float(h.logconstant), s.seed, 0,
+                              native.ptr(s.counter), native.ptr(s.logcounts), native.ptr(s.round_ids_init),
+                              native.ptr(loc0), native.ptr(fac0), native.ptr(ln0), native.ptr(s.samples),
+                              native.ptr(s.logtargets), native.ptr(s.lognum), native.ptr(s.logweights),
+                              native.ptr(s.round_ids), native.ptr(s.summaries), native.ptr(s.round_failures),
+                              native.ptr(s.mean), native.ptr(s.cov), native.ptr(s.shift), native.ptr(s.cand_loc),
+                              native.ptr(s.cand_factor), native.ptr(s.cand_lognorm), native.ptr(ws), ws.numel())
+    native.call("issm_amis_run", ctypes.byref(desc), native.stream_ptr())
+    s.offset = sum(int(v) * d + 8 for v in s.schedule)
+
+
+def _run_workspace_errors(s):
+    """The sticky timeout words of the tensor-core and moments regions of the
+    run workspace (issm_amis_run_desc layout)."""
+    ws = getattr(s, "run_workspace", None)
+    if ws is None:
+        return
+    lib = native.lib()
+    d, total = s.history.d, int(s.offsets[-1])
+    up = lambda v: (int(v) + 255) // 256 * 256  # noqa: E731
+    tc_end = up(lib.issm_tc_workspace_bytes(s.rounds, d))
+    mom_end = tc_end + up(lib.issm_moments_workspace_bytes(total, d))
+    for end in (tc_end, mom_end):
+        if int(ws[end - 64:end - 60].view(torch.int32).item()) != 0:
+            raise RuntimeError("a tensor-core kernel timed out waiting for MMA completion")
+
+
+def _finish_moment_summary(s):
+    """The serving form of _finish_moment for AMIS: one packed device-to-host
+    read of the failure records, the per-round summaries and the posterior
+    mean (the last round's FP64 moment pass runs over every retained sample
+    with the final weights, so its mean is the weighted posterior mean);
+    raises on the first failed round; returns (posterior mean, log Z, ESS)
+    of the final round. The samples stay on the device, uncopied."""
+    packed = torch.cat([s.round_failures.view(torch.float64).reshape(-1), s.summaries.reshape(-1), s.mean]).cpu()
+    words = packed[:3 * s.rounds].view(torch.int64).numpy().reshape(s.rounds, 3)
+    summaries = packed[3 * s.rounds:6 * s.rounds].numpy().reshape(s.rounds, 3)
+    if s.precision != native.PREC_NATIVE:
+        if getattr(s, "run_workspace", None) is not None:
+            _run_workspace_errors(s)
+        else:
+            ops.check_tensor_core_errors(s.device)
+    for t in range(s.rounds):
+        if words[t][0] != 0:
+            _raise_failures(words[t], AMISRoundError, t + 1)
+    m, sm, s2 = summaries[-1]
+    n = int(s.offsets[-1])
+    ess = 0.0 if sm == 0 else sm * sm / s2
+    logz = -np.inf if sm == 0 else m + np.log(sm) - np.log(n)
+    return packed[6 * s.rounds:].numpy().copy(), float(logz), float(ess)
+
+
 def _finish_moment(s, is_npmc):
     words = s.round_failures.cpu().numpy()
     summaries = s.summaries.cpu().numpy()
     if s.precision != native.PREC_NATIVE:
-        ops.check_tensor_core_errors(s.device)
+        if getattr(s, "run_workspace", None) is not None:
+            _run_workspace_errors(s)
+        else:
+            ops.check_tensor_core_errors(s.device)
     err = NPMCRoundError if is_npmc else AMISRoundError
     for t in range(s.rounds):
         if words[t][0] != 0:
@@ -530,7 +614,7 @@ def _run_dmpmc(s):
     logz = np.array([sm[0] + np.log(sm[1]) - np.log(s.schedule[r]) for r, sm in enumerate(summaries)])
     s.committed_locations = db.locations.clone()
     round_ids = torch.repeat_interleave(torch.arange(1, s.rounds + 1, device=s.device),
-                                        torch.tensor(s.schedule, device=s.device))
+                                        torch.tensor(s.schedule, device=s.device), output_size=int(sum(s.schedule)))
     return WeightedSamples(s.samples.clone(), s.logweights.clone(),
                            provenance={"round": round_ids, "proposal_id": s.proposal_ids.clone()},
                            diagnostics={"method": "deterministic_mixture_pmc", "rounds": s.rounds,

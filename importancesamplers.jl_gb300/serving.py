@@ -6,15 +6,15 @@ arrived, a stream slot is free and its device footprint fits the memory
 budget. Each admitted run gets its own CUDA stream and its own scratch
 buffers (a workspace scope). All of its kernels (draws, target, retrospective
 denominators, weights, summaries, moments, FP64 fits) are queued on that stream
-without a host synchronisation, so the device overlaps runs of different
-dimension and budget. The loop polls the runs' completion events, reads back
+without a host synchronisation, by one native call (issm_amis_run) for
+Gaussian factor proposals with a native target, so the device overlaps runs of
+different dimension and budget and the host's cost per run stays small. The loop polls the runs' completion events, reads back
 each finished run's summaries and posterior mean, frees its buffers and
 admits the next. A run's results depend only on its own inputs and seed: the
 same run alone or in the mix gives bitwise the same numbers.
 
 Not done here: merging the kernels of many small runs into one launch (every
-run issues its own launches; with many tiny runs the host's launch rate
-bounds throughput).
+run issues its own launches, from native code).
 """
 import heapq
 import itertools
@@ -25,8 +25,8 @@ import torch
 
 from . import native
 from .methods import AMIS
-from .results import mean as weighted_mean
-from .sampler import SamplerBusyError, _finish_moment, _moment_body, prepare_sampler
+from .sampler import (SamplerBusyError, _finish_moment_summary, _moment_body, _native_body, native_body_eligible,
+                      prepare_sampler)
 
 
 class ServeRequest:
@@ -97,7 +97,10 @@ class ServeLoop:
             if s.busy:
                 raise SamplerBusyError("prepared sampler is already running")
             s.busy = True
-            _moment_body(s, False)
+            if native_body_eligible(s):
+                _native_body(s)  # every launch of the run in one native call
+            else:
+                _moment_body(s, False)
             event = torch.cuda.Event()
             event.record(stream)
         s.scope = scope
@@ -107,13 +110,10 @@ class ServeLoop:
         s = run.sampler
         with torch.cuda.stream(run.stream), native.workspace_scope(s.scope):
             try:
-                res = _finish_moment(s, False)
-                pm = weighted_mean(res).cpu().numpy()
+                pm, logz, ess = _finish_moment_summary(s)
             finally:
                 s.busy = False
         native.release_scope(s.scope)
-        logz = float(res.diagnostics["round_lognormalizers"][-1])
-        ess = float(res.diagnostics["round_ess"][-1])
         return ServeResult(run.request, pm, logz, ess, run.start, now)
 
     def run(self, requests, clock=time.perf_counter):

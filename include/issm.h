@@ -443,6 +443,48 @@ typedef struct issm_target {
 int issm_target_logdensity(const issm_target *target, const void *x, int64_t n,
                            void *out, issm_stream_t stream);
 
+/* ---- one AMIS run in one call --------------------------------------------
+ * Every launch of an AMIS run with a Gaussian factor proposal (draws with
+ * in-kernel normals, target, retrospective append, prefix mixture, weights
+ * and per-round summary, moments, FP64 fit), stream-ordered with no host
+ * synchronisation: the same library calls, in the same order, as the host
+ * round loop, so the results are bitwise those of issuing them one by one.
+ * Replaces the round loop over _launch_prefilled_amis_round!
+ * (src/amis_execution.jl:261-357) and _fit_moment_proposal!
+ * (src/adaptive_gaussian_execution.jl:348-425).
+ * history: `rounds` (or more) slots; slot 0 is overwritten with the initial
+ * proposal, slot t + 1 receives round t's fit; inverse_factors is required
+ * for the tensor-core precisions. Sample t of round r takes normal stream
+ * elements from normal_offset (+ *counter); *counter advances by the run's
+ * total at the end. The workspace (issm_amis_run_workspace_bytes) is zeroed
+ * once when created; it holds, in order, the tensor-core scratch
+ * (issm_tc_workspace_bytes(rounds, d), rounded up to 256 bytes), the moments
+ * scratch (issm_moments_workspace_bytes(total, d), rounded up) and the
+ * reduction scratch; the first two end in their sticky timeout words.
+ * ISSM_E_UNSUPPORTED for Student-t or non-factor histories. */
+typedef struct issm_amis_run_desc {
+    issm_bank history;
+    const issm_target *target;
+    int32_t rounds, precision;
+    const int64_t *round_sizes;      /* host, rounds entries */
+    double logconstant;              /* radial log constant of the family (0 for Gaussian) */
+    uint64_t seed, normal_offset;
+    uint64_t *counter;               /* device normal-stream base, or NULL */
+    const void *logcounts;           /* device, log(round_sizes) in the history dtype */
+    const int64_t *round_ids_init;   /* device, round id (1-based) of each sample */
+    const void *initial_location, *initial_factor, *initial_lognormalizer;
+    void *samples, *logtargets, *lognum, *logweights;  /* total (x d) entries */
+    int64_t *round_ids;
+    double *summaries;               /* rounds x 3: (max, S, S2) of each round's weights */
+    int64_t *round_failures;         /* rounds x 3 failure records */
+    double *mean, *cov, *shift;      /* FP64 scratch: d, d x d, d */
+    void *cand_location, *cand_factor, *cand_lognormalizer;  /* the last round's fit */
+    void *workspace;
+    size_t workspace_bytes;
+} issm_amis_run_desc;
+size_t issm_amis_run_workspace_bytes(int32_t d, int64_t total, int32_t rounds);
+int issm_amis_run(const issm_amis_run_desc *run, issm_stream_t stream);
+
 /* ---- tensor-core self-test ------------------------------------------------
  * No counterpart in the reference: a one-CTA tcgen05 GEMM
  * C[128 x n] = A[128 x k] B[n x k]^T (row-major FP32 in and out; inputs rounded

@@ -3,6 +3,7 @@ posteriors of uneven dimension and budget): every run gives bitwise the same
 result alone and in the mix, and matches the conjugate analytic posterior."""
 import numpy as np
 import pytest
+import torch
 
 pytestmark = pytest.mark.gpu
 
@@ -88,3 +89,37 @@ def test_tc_amis_far_start_completes(issm, cuda, d, n_obs, budget):
     res = issm.importance_sample_(s)
     issm.ops.check_tensor_core_errors(cuda)
     assert np.isfinite(float(res.diagnostics["round_lognormalizers"][-1]))
+
+
+@pytest.mark.parametrize("precision", ["native", "bf16"])
+@pytest.mark.parametrize("d", [5, 33, 64])
+def test_native_run_matches_host_round_loop(issm, cuda, precision, d):
+    """issm_amis_run issues the same library calls as the host round loop:
+    samples, log weights, summaries and the final proposal are bitwise equal."""
+    rng = np.random.default_rng(d)
+    X = rng.normal(size=(200, d))
+    y = X @ rng.normal(size=d) + 0.5 * rng.normal(size=200)
+    target = issm.LinearRegressionTarget(X, y, sigma=0.5, prior_var=1.0)
+    mean, _ = target.analytic()
+    L = np.linalg.cholesky(np.linalg.inv(X.T @ X / 0.25 + np.eye(d)))
+    p = issm.FactorGaussian((mean + 0.1 * L @ rng.normal(size=d)).astype(np.float32), (1.2 * L).astype(np.float32))
+    prec = issm.native.PREC_NATIVE if precision == "native" else issm.native.PREC_BF16
+    out = []
+    for native_run in (False, True):
+        s = issm.prepare_sampler(77, target, issm.AMIS(p, rounds=4, round_size=[3000, 2000, 2500, 1999]),
+                                 device=cuda, precision=prec, graphs=False)
+        assert issm.sampler.native_body_eligible(s)
+        s.busy = True
+        if native_run:
+            issm.sampler._native_body(s)
+        else:
+            issm.sampler._moment_body(s, False)
+        res = issm.sampler._finish_moment(s, False)
+        s.busy = False
+        out.append((res.samples.cpu(), res.logweights.cpu(), s.summaries.cpu(), s.committed[0].cpu(),
+                    s.committed[1].cpu(), s.offset))
+    for a, b in zip(*out):
+        if isinstance(a, torch.Tensor):
+            assert torch.equal(a, b)
+        else:
+            assert a == b
