@@ -396,7 +396,10 @@ def _moment_body(s, is_npmc):
                                                     round_ids=s.round_ids[:n_tot], failures=fail)
                 lw_fit = s.logweights[:n_tot]
                 x_fit = s.samples[:n_tot]
-        with _Span(s, "moments", 2 * x_fit.shape[0] * (d + 1) * es):
+        # algorithmic bytes: one read of the samples and weights (tensor-core
+        # form), two (the native two-pass form)
+        passes = 1 if s.precision != native.PREC_NATIVE else 2
+        with _Span(s, "moments", passes * x_fit.shape[0] * (d + 1) * es):
             s.shift.copy_(h.locations[t])
             prev = h.scales[t] if h.scales[t].dim() == 2 and h.scales.dtype == torch.float32 else None
             ops.weighted_moments(x_fit, lw_fit, fit_summary, s.shift, s.mean, s.cov, precision=s.precision,
