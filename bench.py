@@ -236,9 +236,11 @@ def run_gb300(args):
         head = measure(step, args.steps, warmup)
 
     # per-kernel profile of one extra run: a spin kernel first lets the host
-    # queue the whole run, so every span's events time only its kernels
+    # queue the whole run (about 600 launches and 600 events from Python), so
+    # every span's events time only its kernels; the spin must outlast the
+    # queueing or the later spans include host gaps
     sampler.profile = []
-    torch.cuda._sleep(int(5e7))
+    torch.cuda._sleep(int(4e8))
     step()
     torch.cuda.synchronize()
     groups = {}

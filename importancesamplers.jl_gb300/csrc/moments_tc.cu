@@ -7,7 +7,8 @@
 // K; A A^T then holds S2 = sum w z z^T (rows/cols 0..63), S1 = sum w z
 // (row 64) and S0 = sum w (D[64][64]). A is split A = Ah + Al in bf16 and
 // two accumulators in tensor memory, H += Ah Ah^T + Al Al^T and X += Al Ah^T,
-// with X^T added when the sums are finished, give S = (Ah + Al)(Ah + Al)^T:
+// give S = H + X + X^T = (Ah + Al)(Ah + Al)^T (each CTA stores P = H / 2 + X,
+// and S = P + P^T since H is symmetric):
 // the Gram matrix of the split operand (about 16 significant bits per
 // element), so the covariance (its Schur complement) is positive semidefinite
 // up to FP32 accumulation however few samples carry the weight, and the
@@ -22,12 +23,12 @@
 // return at once when the flag is clear.
 //
 // A is stored MN-major: each sample's 8-coordinate groups are 16-byte chunks,
-// so a thread converts its own sample row straight from the staged tile. Warp
+// so two threads convert a sample row straight from the staged tile. Warp
 // roles: warp 0 issues the MMAs; warps 1..8 stage tiles with cp.async into a
 // three-deep ring of padded stages and build A (double-buffered), handing
 // buffers over through mbarriers. Per-CTA partials are summed across CTAs
-// (compensated FP32, FP64 across lanes) and mean = c + S1/S0,
-// cov = S2/S0 - (S1/S0)(S1/S0)^T in FP64.
+// (compensated FP32) and mean = c + S1/S0, cov = S2/S0 - (S1/S0)(S1/S0)^T
+// in FP64.
 #include "issm_device.cuh"
 #include "issm_internal.h"
 #include "tcgen05.cuh"
@@ -38,6 +39,9 @@ constexpr int kMtConvWarps = 8;
 constexpr int kMtConvThreads = 32 * kMtConvWarps;
 constexpr int kMtThreads = 32 * (1 + kMtConvWarps);
 constexpr int kMtTile = 128;   // samples per tile = MMA K extent per tile
+constexpr int kMtTPR = kMtConvThreads / kMtTile;  // converter threads per sample row
+constexpr int kMtGPT = 8 / kMtTPR;                // coordinate groups (of 8) per converter thread
+constexpr int kMtCtasPerSm = 1;  // CTAs per SM (two 64-sample pipelines measured the same)
 constexpr int kMtCols = 80;    // MMA N (64 coordinates + sqrt(w) + padding)
 constexpr int kMtStages = 3;   // staged sample tiles in flight
 constexpr int kMtRS = 68;      // padded row of a staged tile (floats)
@@ -50,9 +54,9 @@ constexpr int kMtGroups = 9;
 constexpr int kMtPart = kMtGroups * kMtTile * 16;
 constexpr size_t kMtSmem = (size_t)2 * 2 * kMtPart + (size_t)kMtStages * kMtRawBytes + 256;
 static_assert((size_t)3 * kMtPart + (size_t)16 * kMtTile * 16 <= kMtSmem, "M = 128 reads stay inside the CTA's shared memory");
-constexpr int kMtPartial = 2 * 65 * kMtCols;  // H and X sums of one CTA
+constexpr int kMtPartial = 65 * kMtCols;  // P = H / 2 + X of one CTA (S = P + P^T: H is symmetric)
 
-__global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *__restrict__ x, int d, int64_t n,
+__global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(const float *__restrict__ x, int d, int64_t n,
                                                                     const float *__restrict__ lw,
                                                                     const double *__restrict__ summary,
                                                                     const double *__restrict__ center,
@@ -161,7 +165,7 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
             tc::cp_async_commit();
         };
         for (int s = 0; s < kMtStages; ++s) issue_raw(s);
-        const int k = ctid & (kMtTile - 1), half = ctid >> 7;
+        const int k = ctid % kMtTile, part = ctid / kMtTile;
         for (int it = 0; it < my_tiles; ++it) {
             const int buf = it & 1;
             tc::cp_async_wait<kMtStages - 1>();
@@ -181,8 +185,8 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
                 const float sw = l == -INFINITY ? 0.f : expf(0.5f * (l - m)) * inv_sqrt_s;
                 const bool full = active && d == 64;
 #pragma unroll
-                for (int gg = 0; gg < 4; ++gg) {
-                    const int g = half * 4 + gg, c = g * 8;
+                for (int gg = 0; gg < kMtGPT; ++gg) {
+                    const int g = part * kMtGPT + gg, c = g * 8;
                     float v[8];
                     const float4 c0 = *reinterpret_cast<const float4 *>(s_c + c),
                                  c1 = *reinterpret_cast<const float4 *>(s_c + c + 4);
@@ -222,7 +226,7 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
                     *reinterpret_cast<uint4 *>(ah + (size_t)g * kMtTile * 16 + k * 16) = hi;
                     *reinterpret_cast<uint4 *>(al + (size_t)g * kMtTile * 16 + k * 16) = lo;
                 }
-                if (half == 1) {
+                if (part == kMtTPR - 1) {
                     // row group 8: sqrt(w) in row 64
                     const uint32_t h = tc::pack_bf16x2(sw, 0.f);
                     const uint32_t lo = tc::pack_bf16x2(sw - __uint_as_float(h << 16), 0.f);
@@ -255,18 +259,16 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
     if (!abort_flag && warp >= 1 && warp <= 4) {
         const int q = warp & 3, row = 32 * q + lane;
 #pragma unroll
-        for (int acc = 0; acc < 2; ++acc) {
-#pragma unroll
-            for (int c0 = 0; c0 < kMtCols; c0 += 16) {
-                float v[16];
-                if (my_tiles > 0) {
-                    tc::tmem_ld16(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(acc * 128 + c0), v);
-                } else {
-                    for (int j = 0; j < 16; ++j) v[j] = 0.f;
-                }
-                if (row <= 64) {
-                    for (int j = 0; j < 16; ++j) out[acc * 65 * kMtCols + row * kMtCols + c0 + j] = v[j];
-                }
+        for (int c0 = 0; c0 < kMtCols; c0 += 16) {
+            float h[16], xv[16];
+            if (my_tiles > 0) {
+                tc::tmem_ld16(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, h);
+                tc::tmem_ld16(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(128 + c0), xv);
+            } else {
+                for (int j = 0; j < 16; ++j) h[j] = xv[j] = 0.f;
+            }
+            if (row <= 64) {
+                for (int j = 0; j < 16; ++j) out[row * kMtCols + c0 + j] = fmaf(0.5f, h[j], xv[j]);
             }
         }
     }
@@ -275,9 +277,9 @@ __global__ void __launch_bounds__(kMtThreads, 1) moments_tc_kernel(const float *
     if (warp == 0) tc::tmem_dealloc(tbase, 256);
 }
 
-// Partials are [block][2][65][80] FP32 (H, X). Every CTA sums 32 entries over
-// the blocks (32 block-strided lanes per entry, coalesced); the last CTA to
-// finish (a device-scope counter, reset by that CTA) forms S = H + X + X^T and
+// Partials are [block][65][80] FP32 (P = H / 2 + X). Every CTA sums 32 entries
+// over the blocks (32 block-strided lanes per entry, coalesced); the last CTA
+// to finish (a device-scope counter, reset by that CTA) forms S = P + P^T and
 // from it mean = c + S1/S0 and cov = S2/S0 - (S1/S0)(S1/S0)^T in FP64, with c
 // the FP32 value the pass subtracted. `center` and `mean` may be the same
 // array: each entry is read before it is written. With `refine` given, the
@@ -334,10 +336,7 @@ __global__ void __launch_bounds__(kMtReduceThreads) moments_tc_reduce_kernel(
     __syncthreads();
     if (!last) return;
     __threadfence();
-    const double *H = sums, *X = sums + 65 * kMtCols;
-    auto S = [&](int r, int c) {
-        return __ldcg(H + r * kMtCols + c) + __ldcg(X + r * kMtCols + c) + __ldcg(X + c * kMtCols + r);
-    };
+    auto S = [&](int r, int c) { return __ldcg(sums + r * kMtCols + c) + __ldcg(sums + c * kMtCols + r); };
     if (threadIdx.x == 0) s_inv = 1.0 / S(64, 64);
     // R = sqrt(eps(Float32)) tr(L L^T) / d of the previous factor (0 without one), in FP32
     float rr = 0.f;
@@ -378,14 +377,16 @@ __global__ void __launch_bounds__(kMtReduceThreads) moments_tc_reduce_kernel(
     }
 }
 
+constexpr int kMtMaxBlocks = kSMs * kMtCtasPerSm;
+
 static int moments_tc_blocks(int64_t n) {
     const int64_t t = (n + kMtTile - 1) / kMtTile;
-    return (int)(t < kSMs ? (t < 1 ? 1 : t) : kSMs);
+    return (int)(t < kMtMaxBlocks ? (t < 1 ? 1 : t) : kMtMaxBlocks);
 }
 
 size_t moments_tc_workspace_bytes(int64_t n) {
     (void)n;
-    return sizeof(float) * (size_t)kSMs * kMtPartial + sizeof(double) * kMtPartial + 256;
+    return sizeof(float) * (size_t)kMtMaxBlocks * kMtPartial + sizeof(double) * kMtPartial + 256;
 }
 
 int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *summary, const double *shift,
@@ -398,7 +399,7 @@ int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *su
     float *partial = (float *)ws;
     const int e = allow_dynamic_smem((const void *)moments_tc_kernel);
     if (e) return e;
-    double *sums = reinterpret_cast<double *>(partial + (size_t)kSMs * kMtPartial);
+    double *sums = reinterpret_cast<double *>(partial + (size_t)kMtMaxBlocks * kMtPartial);
     int *refine = reinterpret_cast<int *>(sums + kMtPartial);
     unsigned *counter = reinterpret_cast<unsigned *>(error + 1);  // zero with the workspace; reset by each use
     const int rblocks = (kMtPartial + 31) / 32;
