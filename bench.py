@@ -255,6 +255,25 @@ def run_gb300(args):
     hbm, tflops, src = read_peaks()
     achieved = (nbytes / cnt) / ((tms / cnt) / 1e3) / 1e9
     share = {k: round(v[0] / sum(x[0] for x in groups.values()), 4) for k, v in groups.items()}
+    # every span against its own bound: HBM spans by their algorithmic bytes,
+    # the prefix mixture (tensor-bound) by its MMA flops
+    dp = 16 if D <= 16 else 32 if D <= 32 else 64
+    split = 3 if args.precision == "bf16" else 1
+    mma_flops = sum((t + 1) * round_size for t in range(rounds)) * 2 * dp * (dp + 16) * split
+    kernels = {}
+    for k, (ms, c, nb) in groups.items():
+        if k == "mixture_new" and args.precision != "fp32":
+            # the measured bf16 GEMM rate; tf32 MMAs run at half the bf16 rate
+            peak = tflops if args.precision == "bf16" else tflops / 2
+            ach = mma_flops / (ms / 1e3) / 1e12
+            kernels[k] = {"bound": "tensor", "achieved": round(ach, 1), "peak": round(peak, 1), "unit": "TFLOP/s",
+                          "frac": round(ach / peak, 4), "ms_per_run": round(ms, 3)}
+        elif k in ("draw", "target", "amis_append", "form_summary", "moments"):
+            ach = nb / (ms / 1e3) / 1e9
+            kernels[k] = {"bound": "hbm", "achieved": round(ach, 1), "peak": round(hbm, 1), "unit": "GB/s",
+                          "frac": round(ach / hbm, 4), "ms_per_run": round(ms, 3)}
+        else:
+            kernels[k] = {"bound": "fp64 latency (one CTA per fit)", "ms_per_run": round(ms, 3)}
     traffic = None
     if dominant in TRAFFIC_PER_SAMPLE:
         samples = sum(SPAN_SAMPLES[dominant](t, round_size) for t in range(rounds) if dominant != "amis_append" or t > 0)
@@ -321,7 +340,7 @@ def run_gb300(args):
                       "abs_logz_diff_vs_headline": abs(v["logz"] - head["logz"])} for k, v in forms.items()},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "peak_source": f"{src} hbm_gbs", "traffic": traffic,
-                     "kernel_share": share},
+                     "kernel_share": share, "kernels": kernels},
         "cpu_baseline": {"value": cpu_value, "unit": "weighted samples/s", "cores": cores, "kind": "port",
                          "sample": f"40 rounds x {CPU_ROUND_SIZE} samples (d=64), FP64 oracle AMIS"},
         "e2e": {"value": total * world / (e2e_ms / 1e3), "unit": "weighted samples/s", "h2d_bytes_per_step": h2d,
