@@ -400,16 +400,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
                 chunk_range(ch, k0, cnt);
                 const uint32_t lane_base = tbase + ((uint32_t)(32 * qd) << 16) + (uint32_t)((j & 1) * NW);
                 for (int kk = 0; kk < cnt; ++kk) {
+                    // a component's DP columns in one round trip (all loads, then one wait)
+                    float v[DP];
+                    if constexpr (DP == 64) tc::tmem_ld64(lane_base + (uint32_t)(kk * DP), v);
+                    else if constexpr (DP == 32) tc::tmem_ld32(lane_base + (uint32_t)(kk * DP), v);
+                    else tc::tmem_ld16(lane_base + (uint32_t)(kk * DP), v);
                     float r2a = 0.f, r2b = 0.f;
 #pragma unroll
-                    for (int c0 = 0; c0 < DP; c0 += 16) {
-                        float v[16];
-                        tc::tmem_ld16(lane_base + (uint32_t)(kk * DP + c0), v);
-#pragma unroll
-                        for (int q = 0; q < 16; q += 2) {
-                            r2a = fmaf(v[q], v[q], r2a);
-                            r2b = fmaf(v[q + 1], v[q + 1], r2b);
-                        }
+                    for (int q = 0; q < DP; q += 2) {
+                        r2a = fmaf(v[q], v[q], r2a);
+                        r2b = fmaf(v[q + 1], v[q + 1], r2b);
                     }
                     const float r2 = r2a + r2b;
                     const int k = k0 + kk;
