@@ -180,9 +180,14 @@ class DeviceHistory(DeviceBank):
         loc = torch.zeros(rounds, d, dtype=tdt, device=device)
         sc = torch.zeros(rounds, d, d, dtype=tdt, device=device)
         lnorm = torch.zeros(rounds, dtype=tdt, device=device)
-        loc[0] = torch.tensor(proposal.location, device=device)
-        sc[0] = torch.tensor(np.ascontiguousarray(proposal.factor_matrix().T), device=device)
-        lnorm[0] = float(proposal.lognormalizer)
+        # slot 0 in one host-to-device copy
+        host = np.concatenate([np.asarray(proposal.location, dtype=dt).reshape(-1),
+                               np.ascontiguousarray(proposal.factor_matrix().T, dtype=dt).reshape(-1),
+                               np.asarray([proposal.lognormalizer], dtype=dt)])
+        first = torch.from_numpy(host).to(device)
+        loc[0].copy_(first[:d])
+        sc[0].copy_(first[d:d + d * d].view(d, d))
+        lnorm[0:1].copy_(first[d + d * d:])
         dofs = rr = None
         fam = native.GAUSSIAN
         if proposal.family == STUDENT_T:

@@ -281,7 +281,11 @@ def _prepare_moment(s):
     s.schedule = list(alg.round_size)
     s.offsets = np.concatenate([[0], np.cumsum(s.schedule)])
     s.history = DeviceHistory.allocate(p, s.rounds, s.device)
-    s.logcounts = torch.tensor(np.log(np.array(s.schedule, dtype=np.float64)), dtype=s.dtype, device=s.device)
+    uniform = len(set(s.schedule)) == 1
+    if uniform:  # no host-to-device copy (a blocking copy synchronises the stream)
+        s.logcounts = torch.full((s.rounds,), math.log(s.schedule[0]), dtype=s.dtype, device=s.device)
+    else:
+        s.logcounts = torch.tensor(np.log(np.array(s.schedule, dtype=np.float64)), dtype=s.dtype, device=s.device)
     total = int(s.offsets[-1])
     d = p.dimension
     dev, dt = s.device, s.dtype
@@ -289,24 +293,35 @@ def _prepare_moment(s):
     s.logtargets = torch.empty(total, dtype=dt, device=dev)
     s.lognum = torch.empty(total, dtype=dt, device=dev)
     s.logweights = torch.empty(total, dtype=dt, device=dev)
-    s.summaries = torch.zeros(s.rounds, 3, dtype=torch.float64, device=dev)
-    s.round_failures = torch.zeros(s.rounds, 3, dtype=torch.int64, device=dev)
-    s.mean = torch.zeros(d, dtype=torch.float64, device=dev)
-    s.cov = torch.zeros(d, d, dtype=torch.float64, device=dev)
-    s.shift = torch.zeros(d, dtype=torch.float64, device=dev)
-    s.cand_loc = torch.zeros(d, dtype=dt, device=dev)
-    s.cand_factor = torch.zeros(d, d, dtype=dt, device=dev)
-    s.cand_lognorm = torch.zeros(1, dtype=dt, device=dev)
+    # the small per-run state in three zeroed blocks (each part 256-byte aligned)
+    s.summaries, s.mean, s.cov, s.shift = _carve(torch.float64, dev, (s.rounds, 3), (d,), (d, d), (d,))
+    s.round_failures, s.counter = _carve(torch.int64, dev, (s.rounds, 3), (1,))
+    s.cand_loc, s.cand_factor, s.cand_lognorm = _carve(dt, dev, (d,), (d, d), (1,))
     s.committed = (s.history.locations[0].clone(), s.history.scales[0].clone(), s.history.lognormalizers[0].clone())
-    s.counter = torch.zeros(1, dtype=torch.int64, device=dev)
     dofs = None if p.family != STUDENT_T else [float(p.dof)]
     s.rn_stride, s.ru_stride = _radial_strides(dofs)
     s.bound_target = s.target.bind(s.device, dt)
-    # output_size given: no device-to-host read of the total
-    s.round_ids_init = torch.repeat_interleave(torch.arange(1, s.rounds + 1, device=dev),
-                                               torch.tensor(s.schedule, device=dev),
-                                               output_size=total).contiguous()
+    if uniform:  # 1-based round of each sample, with no host-to-device copy
+        s.round_ids_init = torch.arange(total, device=dev) // s.schedule[0] + 1
+    else:
+        s.round_ids_init = torch.repeat_interleave(torch.arange(1, s.rounds + 1, device=dev),
+                                                   torch.tensor(s.schedule, device=dev),
+                                                   output_size=total).contiguous()
     s.round_ids = s.round_ids_init.clone()
+
+
+def _carve(dtype, device, *shapes):
+    """Zeroed tensors of the given shapes carved from one allocation, each
+    starting on a 256-byte boundary (vectorised kernels read them)."""
+    es = torch.empty((), dtype=dtype).element_size()
+    step = 256 // es
+    sizes = [int(np.prod(sh)) for sh in shapes]
+    starts, o = [], 0
+    for n in sizes:
+        starts.append(o)
+        o += (n + step - 1) // step * step
+    buf = torch.zeros(o, dtype=dtype, device=device)
+    return [buf[a:a + n].view(*sh) for a, n, sh in zip(starts, sizes, shapes)]
 
 
 def _graph_eligible(s):
