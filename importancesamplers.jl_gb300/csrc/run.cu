@@ -11,6 +11,7 @@
 // (_fit_moment_proposal!, src/adaptive_gaussian_execution.jl:348-425), for
 // every round.
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 
 #include "issm_device.cuh"
@@ -35,6 +36,9 @@ static size_t round_up(size_t v) { return (v + 255) & ~(size_t)255; }
 using namespace issm;
 
 extern "C" {
+
+size_t issm_amis_run_desc_bytes(void) { return sizeof(issm_amis_run_desc); }
+size_t issm_amis_run_desc_workspace_offset(void) { return offsetof(issm_amis_run_desc, workspace_bytes); }
 
 size_t issm_amis_run_workspace_bytes(int32_t d, int64_t total, int32_t rounds) {
     if (d < 1 || total < 1 || rounds < 1) return 0;

@@ -117,6 +117,8 @@ SIGNATURES = [
     ("issm_tc_selftest", C.c_int, [_p, _p, _p, _i32, _i32, _i32, _p, _p]),
     ("issm_amis_run_workspace_bytes", _sz, [_i32, _i64, _i32]),
     ("issm_amis_run", C.c_int, [C.POINTER(AmisRunDesc), _p]),
+    ("issm_amis_run_desc_bytes", _sz, []),
+    ("issm_amis_run_desc_workspace_offset", _sz, []),
     ("issm_tc_workspace_bytes", _sz, [_i32, _i32]),
     ("issm_invert_factors", C.c_int, [_bank, _i32, _i32, _p, _p]),
     ("issm_mixture_logdensity_ws", C.c_int, [_bank, _den, _p, _i64, _p, _i32, _p, _p, _p, _i64, _i32, _p, _sz,

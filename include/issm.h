@@ -484,6 +484,10 @@ typedef struct issm_amis_run_desc {
 } issm_amis_run_desc;
 size_t issm_amis_run_workspace_bytes(int32_t d, int64_t total, int32_t rounds);
 int issm_amis_run(const issm_amis_run_desc *run, issm_stream_t stream);
+/* sizeof(issm_amis_run_desc) and the offset of its last field, for bindings
+ * that mirror the struct (checked by the CPU tests). */
+size_t issm_amis_run_desc_bytes(void);
+size_t issm_amis_run_desc_workspace_offset(void);
 
 /* ---- tensor-core self-test ------------------------------------------------
  * No counterpart in the reference: a one-CTA tcgen05 GEMM

@@ -66,3 +66,16 @@ def test_argument_errors_need_no_gpu(issm):
     assert lib.issm_mixture_logdensity(ctypes.byref(b), ctypes.byref(den), 1, 1, None, 0, 1, None, None, 0, 0,
                                        None) == -1
     assert lib.issm_resample_systematic(1, 4, 0, 1.5, 4, 1, 1, 10 ** 6, None) == -2
+
+
+def test_run_descriptor_layout_matches_binding(issm):
+    """The ctypes mirror of issm_amis_run_desc has the C struct's size and
+    field offsets; a NULL descriptor is rejected before any launch."""
+    if not os.path.exists(issm.native.library_path()):
+        pytest.skip("libissm103.so not built")
+    lib = issm.native.load()
+    D = issm.native.AmisRunDesc
+    assert ctypes.sizeof(D) == lib.issm_amis_run_desc_bytes()
+    assert D.workspace_bytes.offset == lib.issm_amis_run_desc_workspace_offset()
+    assert lib.issm_amis_run(None, None) == -1
+    assert lib.issm_amis_run_workspace_bytes(0, 10, 4) == 0
