@@ -79,3 +79,16 @@ def test_run_descriptor_layout_matches_binding(issm):
     assert D.workspace_bytes.offset == lib.issm_amis_run_desc_workspace_offset()
     assert lib.issm_amis_run(None, None) == -1
     assert lib.issm_amis_run_workspace_bytes(0, 10, 4) == 0
+
+
+def test_draw_philox_argument_errors_need_no_gpu(issm):
+    if not os.path.exists(issm.native.library_path()):
+        pytest.skip("libissm103.so not built")
+    lib = issm.native.load()
+    b = issm.native.Bank(2, 1, 0, issm.native.SCALE_FACTOR, 0, 0, 1, 1, 1, None, None, None)
+    assert lib.issm_draw_philox(ctypes.byref(b), 0, 1, None, 0, None, 0, None, 0, 0, None, None, 0, None) == 0
+    assert lib.issm_draw_philox(ctypes.byref(b), 0, 1, None, 0, None, 0, None, 0, -1, 1, None, 0, None) == -2
+    assert lib.issm_draw_philox(ctypes.byref(b), 0, 1, None, 0, None, 0, None, 0, 4, None, None, 0, None) == -1
+    assert lib.issm_draw_philox(ctypes.byref(b), 1, 1, None, 0, None, 0, None, 0, 4, 1, None, 0, None) == -2
+    b.family = 1  # Student-t needs radial normals
+    assert lib.issm_draw_philox(ctypes.byref(b), 0, 1, None, 0, None, 0, None, 0, 4, 1, None, 0, None) == -1

@@ -123,3 +123,44 @@ def test_native_run_matches_host_round_loop(issm, cuda, precision, d):
             assert torch.equal(a, b)
         else:
             assert a == b
+
+
+def test_native_run_failure_matches_host_round_loop(issm, cuda):
+    """A target that returns NaN fails round 1 with the same error through
+    issm_amis_run as through the host round loop."""
+    d = 4
+    target = issm.QuadraticTarget(np.zeros(d), float("nan"))
+    p = issm.FactorGaussian(np.zeros(d, dtype=np.float32), np.eye(d, dtype=np.float32))
+    msgs = []
+    for native_run in (False, True):
+        s = issm.prepare_sampler(3, target, issm.AMIS(p, rounds=3, round_size=500), device=cuda, graphs=False)
+        assert issm.sampler.native_body_eligible(s)
+        s.busy = True
+        (issm.sampler._native_body if native_run else (lambda x: issm.sampler._moment_body(x, False)))(s)
+        with pytest.raises(issm.AMISRoundError) as e:
+            issm.sampler._finish_moment_summary(s)
+        s.busy = False
+        msgs.append(str(e.value))
+    assert msgs[0] == msgs[1] and "round 1" in msgs[0]
+
+
+def test_serving_falls_back_for_student_t_proposals(issm, cuda):
+    """Student-t proposal histories are not covered by issm_amis_run: the loop
+    issues those runs from the host round loop, with the same results as a
+    run alone."""
+    rng = np.random.default_rng(9)
+    d = 6
+    X = rng.normal(size=(80, d))
+    y = X @ rng.normal(size=d) + 0.5 * rng.normal(size=80)
+    target = issm.LinearRegressionTarget(X, y, sigma=0.5, prior_var=1.0)
+    mean, _ = target.analytic()
+    L = np.linalg.cholesky(np.linalg.inv(X.T @ X / 0.25 + np.eye(d)))
+    mk = lambda rid: issm.serving.ServeRequest(  # noqa: E731
+        rid, target, issm.FactorStudentT(np.float32(7.0), mean.astype(np.float32), (1.3 * L).astype(np.float32)),
+        rounds=3, round_size=2000, seed=40 + rid)
+    s = issm.prepare_sampler(0, target, issm.AMIS(mk(0).proposal, rounds=3, round_size=2000), device=cuda)
+    assert not issm.sampler.native_body_eligible(s)
+    alone = issm.serving.ServeLoop(cuda, max_inflight=1).run([mk(0)])[0]
+    mixed = {r.rid: r for r in issm.serving.ServeLoop(cuda, max_inflight=2).run([mk(0), mk(1)])}
+    assert np.array_equal(alone.posterior_mean, mixed[0].posterior_mean) and alone.logz == mixed[0].logz
+    assert np.all(np.isfinite(mixed[1].posterior_mean))
