@@ -141,7 +141,7 @@ constexpr int kFirstEpiWarp = 1 + kConvWarps;
 constexpr int kTcThreads = 32 * (1 + kConvWarps + kEpiWarps);
 constexpr int kBRing = 3;      // operand buffers in flight when a tile needs several chunks
 
-template <int KIND, int SPLIT, int DP>
+template <int KIND, int SPLIT, int DP, bool DIRECT>
 __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
     constexpr int PER = 16 / EB;              // elements per 16-byte K group
@@ -329,11 +329,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
         };
         for (int s = 0; s < S; ++s) issue_raw(s);
         const int row = ctid & (kTcTile - 1), half = ctid >> 7;
+        constexpr int HV = DP / 8;  // float4s of this thread's half row
         for (int it = 0; it < my_tiles; ++it) {
-            if (S == 1) tc::cp_async_wait<0>();
-            else if (S == 2) tc::cp_async_wait<1>();
-            else tc::cp_async_wait<2>();
-            tc::named_sync(1, kConvThreads);
+            const int64_t i = tile_of(it) * kTcTile + row;
+            const bool active = i < p.n;
+            // DIRECT (no staged tile): this thread's half row straight from
+            // global memory into registers, issued before the A-buffer wait so
+            // its latency overlaps the previous tile's MMAs
+            float4 gv[DIRECT ? HV : 1];
+            if constexpr (DIRECT) {
+#pragma unroll
+                for (int u = 0; u < HV; ++u) {
+                    const int c = half * (DP / 2) + 4 * u;
+                    if (active && vec && c + 3 < p.d) {
+                        gv[u] = *reinterpret_cast<const float4 *>(p.x + i * p.d + c);
+                    } else {
+                        const float *xr = p.x + i * p.d;
+                        gv[u] = make_float4(active && c < p.d ? xr[c] : 0.f, active && c + 1 < p.d ? xr[c + 1] : 0.f,
+                                            active && c + 2 < p.d ? xr[c + 2] : 0.f,
+                                            active && c + 3 < p.d ? xr[c + 3] : 0.f);
+                    }
+                }
+            } else {
+                if (S == 1) tc::cp_async_wait<0>();
+                else if (S == 2) tc::cp_async_wait<1>();
+                else tc::cp_async_wait<2>();
+                tc::named_sync(1, kConvThreads);
+            }
             bool ok = true;
             const int abuf = it % nbufA;
             if (it >= nbufA) {
@@ -341,10 +363,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
                 ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
             }
             if (ok) {
-                const float *raw = reinterpret_cast<const float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
+                const float *raw = S > 0 ? reinterpret_cast<const float *>(s_raw + (size_t)(it % S) * RAW_BYTES)
+                                         : nullptr;
                 unsigned char *a = s_a + (size_t)abuf * NPART * A_PART;
-                const int64_t i = tile_of(it) * kTcTile + row;
-                const bool active = i < p.n;
                 const bool full = active && p.d == DP;
 #pragma unroll
                 for (int qq = 0; qq < QH; ++qq) {
@@ -354,7 +375,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
                     for (int m = 0; m < PER; m += 4) {
                         const int c = q * PER + m;
                         const float4 cc = *reinterpret_cast<const float4 *>(s_c + c);
-                        if (full) {
+                        if constexpr (DIRECT) {
+                            // gv holds zeros beyond d and for inactive rows
+                            const float4 f = gv[(qq * PER + m) / 4];
+                            v[m] = (active && c < p.d) ? f.x - cc.x : 0.f;
+                            v[m + 1] = (active && c + 1 < p.d) ? f.y - cc.y : 0.f;
+                            v[m + 2] = (active && c + 2 < p.d) ? f.z - cc.z : 0.f;
+                            v[m + 3] = (active && c + 3 < p.d) ? f.w - cc.w : 0.f;
+                        } else if (full) {
                             const float4 f = *reinterpret_cast<const float4 *>(raw + row * RS + c);
                             v[m] = f.x - cc.x;
                             v[m + 1] = f.y - cc.y;
@@ -378,8 +406,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
             tc::fence_proxy_async();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&a_full[it % nbufA]);
-            tc::named_sync(1, kConvThreads);  // the stage is consumed: refill it
-            issue_raw(it + S);
+            if (!DIRECT) {
+                tc::named_sync(1, kConvThreads);  // the stage is consumed: refill it
+                issue_raw(it + S);
+            }
         }
         tc::cp_async_wait_all();
     } else {
@@ -529,8 +559,8 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     static_assert(NPART * B_COMP <= (size_t)DP * (4 * DP + 64), "operand form exceeds its workspace slot");
     const int nslots = p.last_slot - p.first_slot + 1;
     // largest chunk (<= 256 TMEM columns) whose buffers fit: one chunk keeps
-    // three staged tiles and two A buffers; several chunks keep one staged
-    // tile, one A buffer and a ring of kBRing chunk buffers
+    // three staged tiles and two A buffers; several chunks keep one A buffer
+    // and a ring of kBRing chunk buffers, with one staged tile or none
     int chunk = min(nslots, 256 / DP), nch = 1, stages = 1;
     size_t smem = 0;
     for (; chunk >= 1; --chunk) {
@@ -539,8 +569,12 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
             stages = 3;
             smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)NPART * chunk * B_COMP + (size_t)DP * 4;
         } else {
-            stages = 1;
-            smem = stages * RAW_BYTES + NPART * A_PART + (size_t)kBRing * NPART * chunk * B_COMP + (size_t)DP * 4;
+            // a staged tile if it fits beside the operand ring; else the
+            // converters read their rows from global memory (no staged
+            // tile), which leaves room for larger chunks
+            const size_t rest = NPART * A_PART + (size_t)kBRing * NPART * chunk * B_COMP + (size_t)DP * 4;
+            stages = RAW_BYTES + rest <= kTcMaxSmem ? 1 : 0;
+            smem = stages * RAW_BYTES + rest;
         }
         if (smem <= kTcMaxSmem) break;
     }
@@ -551,7 +585,9 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     { tc_prepare_kernel<KIND, SPLIT, DP><<<nslots, 256, 0, stream>>>(w, loc, p.d, p.first_slot, chunk, cslot, ops,
                                                                        center);
       note_launch(); }
-    auto kern = mixture_tc_kernel<KIND, SPLIT, DP>;
+    // DIRECT (no staged tile; converters read rows from global memory) is a
+    // separate instantiation so the staged form keeps its registers
+    auto kern = stages == 0 ? mixture_tc_kernel<KIND, SPLIT, DP, true> : mixture_tc_kernel<KIND, SPLIT, DP, false>;
     const int st = allow_dynamic_smem((const void *)kern);
     if (st) return st;
     int occ = 1;
