@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(256) tc_prepare_kernel(const float *__restrict
 
 struct TcParams {
     int d, mode, family, den_kind, fixed_slot;
-    int first_slot, last_slot, chunk, nchunks, ntiles, raw_stages;
+    int first_slot, last_slot, chunk, nchunks, ntiles, raw_stages, bring;
     int64_t n;
     const float *x;
     const unsigned char *ops;
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     // several chunks: one A buffer (a tile is converted once per nchunks items)
     // and a ring of kBRing operand buffers filled kBRing - 1 items ahead
     const int nbufA = nchunks > 1 ? 1 : 2;
-    const int nbufB = nchunks > 1 ? kBRing : 1;
+    const int nbufB = nchunks > 1 ? p.bring : 1;
     const uint32_t LBO_B = (uint32_t)(chunk * DP * 16);
     const uint32_t CHUNK_BYTES = (uint32_t)(NPART * chunk * B_COMP);
 
@@ -561,7 +561,7 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     // largest chunk (<= 256 TMEM columns) whose buffers fit: one chunk keeps
     // three staged tiles and two A buffers; several chunks keep one A buffer
     // and a ring of kBRing chunk buffers, with one staged tile or none
-    int chunk = min(nslots, 256 / DP), nch = 1, stages = 1;
+    int chunk = min(nslots, 256 / DP), nch = 1, stages = 1, bring = kBRing;
     size_t smem = 0;
     for (; chunk >= 1; --chunk) {
         nch = (nslots + chunk - 1) / chunk;
@@ -569,12 +569,15 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
             stages = 3;
             smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)NPART * chunk * B_COMP + (size_t)DP * 4;
         } else {
-            // a staged tile if it fits beside the operand ring; else the
-            // converters read their rows from global memory (no staged
-            // tile), which leaves room for larger chunks
-            const size_t rest = NPART * A_PART + (size_t)kBRing * NPART * chunk * B_COMP + (size_t)DP * 4;
-            stages = RAW_BYTES + rest <= kTcMaxSmem ? 1 : 0;
-            smem = stages * RAW_BYTES + rest;
+            // a staged tile if it fits beside a kBRing-deep operand ring; else
+            // the converters read their rows from global memory (no staged
+            // tile), with a kBRing- or 2-deep ring, which leaves room for
+            // larger chunks (fewer, wider MMA items per tile)
+            const size_t base = NPART * A_PART + (size_t)DP * 4, cb = (size_t)NPART * chunk * B_COMP;
+            bring = kBRing;
+            stages = RAW_BYTES + base + kBRing * cb <= kTcMaxSmem ? 1 : 0;
+            if (stages == 0 && base + kBRing * cb > kTcMaxSmem) bring = 2;
+            smem = stages * RAW_BYTES + base + bring * cb;
         }
         if (smem <= kTcMaxSmem) break;
     }
@@ -582,6 +585,7 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     p.chunk = chunk;
     p.nchunks = nch;
     p.raw_stages = stages;
+    p.bring = bring;
     { tc_prepare_kernel<KIND, SPLIT, DP><<<nslots, 256, 0, stream>>>(w, loc, p.d, p.first_slot, chunk, cslot, ops,
                                                                        center);
       note_launch(); }
