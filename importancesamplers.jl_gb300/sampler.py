@@ -17,7 +17,7 @@ import torch
 
 from . import native, ops
 from .bank import DeviceHistory, pack
-from .methods import (AMIS, NPMC, DeterministicMixturePMC, GlobalResampling, ImportanceSampling, LocalResampling,
+from .methods import (AMIS, NPMC, DeterministicMixturePMC, ImportanceSampling, LocalResampling,
                       PartialDeterministicMixture, RandomMixture, StandardMIS)
 from .proposals import GAUSSIAN, STUDENT_T
 from .results import (AMISRoundError, DMPMCRoundError, NPMCRoundError, SamplerExecutionError, WeightedSamples,
