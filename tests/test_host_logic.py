@@ -126,3 +126,33 @@ def test_no_cpu_fallback(issm):
     with pytest.raises(RuntimeError):
         issm.prepare_sampler(0, issm.StandardNormalTarget(1),
                              issm.ImportanceSampling(issm.SphericalGaussian(np.zeros(1), 1.0), nsamples=8))
+
+
+def test_carved_state_is_aligned_and_zero(issm):
+    """The small per-run state is carved from one allocation per dtype; every
+    part starts on a 256-byte boundary (vectorised kernels read it) and is
+    zeroed."""
+    import torch
+
+    parts = issm.sampler._carve(torch.float64, torch.device("cpu"), (5, 3), (33,), (33, 33), (33,))
+    assert [tuple(p.shape) for p in parts] == [(5, 3), (33,), (33, 33), (33,)]
+    base = parts[0].data_ptr()
+    for p in parts:
+        assert (p.data_ptr() - base) % 256 == 0 and p.is_contiguous()
+        assert float(p.abs().sum()) == 0.0
+    ends = sorted((p.data_ptr(), p.data_ptr() + p.numel() * 8) for p in parts)
+    assert all(ends[i][1] <= ends[i + 1][0] for i in range(len(ends) - 1))
+
+
+def test_serve_footprint_grows_with_the_run(issm):
+    import numpy as np
+
+    def req(d, rounds, size):
+        p = issm.FactorGaussian(np.zeros(d, dtype=np.float32), np.eye(d, dtype=np.float32))
+        return issm.serving.ServeRequest(0, None, p, rounds=rounds, round_size=size, seed=0)
+
+    a = req(8, 4, 1000).footprint()
+    assert req(8, 4, 2000).footprint() > a
+    assert req(16, 4, 1000).footprint() > a
+    assert req(8, 8, 1000).footprint() > a
+    assert req(8, 4, 1000).footprint() >= 4 * 1000 * 8 * 4  # at least the retained samples
