@@ -25,6 +25,7 @@ import torch
 
 from . import native
 from .methods import AMIS
+from .results import RoundError, SamplerExecutionError
 from .sampler import (SamplerBusyError, _finish_moment_summary, _moment_body, _native_body, native_body_eligible,
                       prepare_sampler)
 
@@ -54,10 +55,15 @@ class ServeRequest:
 
 
 class ServeResult:
-    def __init__(self, request, posterior_mean, logz, ess, start, end):
+    """A finished run: posterior mean, final-round log Z and ESS, timings; or,
+    when the run failed (AMISRoundError and the like), `error` with NaN
+    outputs. A failed run never stops the loop."""
+
+    def __init__(self, request, posterior_mean, logz, ess, start, end, error=None):
         self.rid = request.rid
         self.posterior_mean, self.logz, self.ess = posterior_mean, logz, ess
         self.arrival, self.start, self.end = request.arrival, start, end
+        self.error = error
 
     @property
     def latency(self):
@@ -108,13 +114,17 @@ class ServeLoop:
 
     def _retire(self, run, now):
         s = run.sampler
+        error = None
         with torch.cuda.stream(run.stream), native.workspace_scope(s.scope):
             try:
                 pm, logz, ess = _finish_moment_summary(s)
+            except (RoundError, SamplerExecutionError) as e:  # this run failed; the others go on
+                d = run.request.proposal.dimension
+                pm, logz, ess, error = np.full(d, np.nan), float("nan"), 0.0, e
             finally:
                 s.busy = False
         native.release_scope(s.scope)
-        return ServeResult(run.request, pm, logz, ess, run.start, now)
+        return ServeResult(run.request, pm, logz, ess, run.start, now, error)
 
     def run(self, requests, clock=time.perf_counter):
         """Serve `requests` (their `arrival` is seconds after the call) and

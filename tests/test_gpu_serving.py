@@ -164,3 +164,21 @@ def test_serving_falls_back_for_student_t_proposals(issm, cuda):
     mixed = {r.rid: r for r in issm.serving.ServeLoop(cuda, max_inflight=2).run([mk(0), mk(1)])}
     assert np.array_equal(alone.posterior_mean, mixed[0].posterior_mean) and alone.logz == mixed[0].logz
     assert np.all(np.isfinite(mixed[1].posterior_mean))
+
+
+def test_failed_run_is_reported_and_the_loop_continues(issm, cuda):
+    """A request whose target returns NaN fails in round 1: its result
+    carries the AMISRoundError and NaN outputs, and the runs around it
+    finish with the same numbers as alone."""
+    reqs, _ = _requests(issm, SPEC[:3])
+    d = 4
+    bad = issm.serving.ServeRequest(99, issm.QuadraticTarget(np.zeros(d), float("nan")),
+                                    issm.FactorGaussian(np.zeros(d, dtype=np.float32), np.eye(d, dtype=np.float32)),
+                                    rounds=3, round_size=500, seed=5)
+    out = {r.rid: r for r in issm.serving.ServeLoop(cuda, max_inflight=4).run(reqs[:1] + [bad] + reqs[1:])}
+    assert isinstance(out[99].error, issm.AMISRoundError) and np.all(np.isnan(out[99].posterior_mean))
+    reqs2, _ = _requests(issm, SPEC[:3])
+    for r in reqs2:
+        alone = issm.serving.ServeLoop(cuda, max_inflight=1).run([r])[0]
+        assert out[r.rid].error is None
+        assert np.array_equal(out[r.rid].posterior_mean, alone.posterior_mean) and out[r.rid].logz == alone.logz
