@@ -53,6 +53,7 @@ int issm_amis_run(const issm_amis_run_desc *r, issm_stream_t stream) {
     if (d < 1 || d > 64 || rounds < 1 || h.count < rounds) return ISSM_E_SIZE;
     if (h.family != ISSM_GAUSSIAN || h.scale_kind != ISSM_SCALE_FACTOR) return ISSM_E_UNSUPPORTED;
     if (h.dtype != ISSM_F32 && h.dtype != ISSM_F64) return ISSM_E_DTYPE;
+    if (!h.locations || !h.scales || !h.lognormalizers) return ISSM_E_NULL;
     const bool tc = r->precision != ISSM_PREC_NATIVE;
     if (tc && (h.dtype != ISSM_F32 || !h.inverse_factors)) return ISSM_E_UNSUPPORTED;
     if (!r->samples || !r->logtargets || !r->lognum || !r->logweights || !r->round_ids || !r->round_ids_init ||

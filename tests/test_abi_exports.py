@@ -79,6 +79,17 @@ def test_run_descriptor_layout_matches_binding(issm):
     assert D.workspace_bytes.offset == lib.issm_amis_run_desc_workspace_offset()
     assert lib.issm_amis_run(None, None) == -1
     assert lib.issm_amis_run_workspace_bytes(0, 10, 4) == 0
+    # a history without its arrays is rejected before any launch
+    tgt = issm.native.Target(0, 4, 0, 0, None, None, None, 0.0, 0.0)
+    sizes = (ctypes.c_int64 * 2)(10, 10)
+    desc = D()
+    desc.history = issm.native.Bank(4, 2, 0, issm.native.SCALE_FACTOR, 0, 0, None, None, None, None, None, None)
+    desc.target = ctypes.cast(ctypes.byref(tgt), ctypes.c_void_p)
+    desc.rounds = 2
+    desc.round_sizes = ctypes.cast(sizes, ctypes.c_void_p)
+    assert lib.issm_amis_run(ctypes.byref(desc), None) == -1
+    desc.history.count = 1  # fewer history slots than rounds
+    assert lib.issm_amis_run(ctypes.byref(desc), None) == -2
 
 
 def test_draw_philox_argument_errors_need_no_gpu(issm):
