@@ -17,7 +17,7 @@ from .results import (AllZeroWeightsError, AMISRoundError, DMPMCRoundError, NPMC
                       UnweightedSamples, WeightedSamples, cov, effective_sample_size, lognormalizer, mean,
                       normalized_weights, resample, var)
 from .sampler import (SamplerBusyError, current_proposal, deterministic_allocation_plan, importance_sample,
-                      importance_sample_, prepare_sampler)
+                      importance_sample_, prepare_sampler, reweigh_amis, share_normal_stream)
 from .targets import (GaussianMixtureTarget, LinearRegressionTarget, LogisticRegressionTarget, LogTarget,
                       QuadraticTarget, StandardNormalTarget, StudentTTarget)
 

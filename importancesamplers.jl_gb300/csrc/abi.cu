@@ -17,6 +17,22 @@ namespace issm {
 static std::atomic<unsigned long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+int device_sms() {
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cached[kMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return kSMs;
+    if (dev < kMaxDevices) {
+        const int c = cached[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) return kSMs;
+    if (sms > kSMs) sms = kSMs;  // scratch is sized for at most kSMs
+    if (dev < kMaxDevices) cached[dev].store(sms, std::memory_order_relaxed);
+    return sms;
+}
+
 int allow_dynamic_smem(const void *kernel) {
     static std::mutex mu;
     static std::vector<std::pair<int, const void *>> done;
@@ -442,18 +458,27 @@ int issm_weighted_moments(const void *x, int32_t d, int64_t n, const void *logwe
                             (cudaStream_t)stream);
 }
 
-int issm_fit_factor_ex(const double *mean, const double *cov, int32_t d, const void *previous_factor, double dof,
-                       double logconstant, int32_t dtype, void *out_location, void *out_factor,
-                       void *out_lognormalizer, float *out_inverse, uint64_t *failures, int64_t failure_index,
-                       issm_stream_t stream) {
+int issm_fit_factor_reg(const double *mean, const double *cov, int32_t d, const void *previous_factor, double dof,
+                        double logconstant, int32_t dtype, double regularization, void *out_location,
+                        void *out_factor, void *out_lognormalizer, float *out_inverse, uint64_t *failures,
+                        int64_t failure_index, issm_stream_t stream) {
     if (d < 1) return ISSM_E_SIZE;
     if (d > 64) return ISSM_E_UNSUPPORTED;
     if (!mean || !cov || !previous_factor || !out_location || !out_factor || !out_lognormalizer)
         return ISSM_E_NULL;
     if (dof > 0.0 && !(dof > 2.0)) return ISSM_E_KIND;
+    if (regularization != regularization) return ISSM_E_KIND;  // NaN
     ISSM_TRY(check_dtype(dtype));
     return fit_factor(mean, cov, d, previous_factor, dof, logconstant, dtype, out_location, out_factor,
-                      out_lognormalizer, failures, failure_index, out_inverse, (cudaStream_t)stream);
+                      out_lognormalizer, failures, failure_index, out_inverse, regularization, (cudaStream_t)stream);
+}
+
+int issm_fit_factor_ex(const double *mean, const double *cov, int32_t d, const void *previous_factor, double dof,
+                       double logconstant, int32_t dtype, void *out_location, void *out_factor,
+                       void *out_lognormalizer, float *out_inverse, uint64_t *failures, int64_t failure_index,
+                       issm_stream_t stream) {
+    return issm_fit_factor_reg(mean, cov, d, previous_factor, dof, logconstant, dtype, -1.0, out_location, out_factor,
+                               out_lognormalizer, out_inverse, failures, failure_index, stream);
 }
 
 int issm_fit_factor(const double *mean, const double *cov, int32_t d, const void *previous_factor, double dof,

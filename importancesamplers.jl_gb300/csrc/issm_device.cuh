@@ -14,7 +14,14 @@
 
 namespace issm {
 
-constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+// GB300: 2 dies x 76 SMs. The largest SM count that per-CTA scratch
+// (summary partials, moment partials) is sized for; grids of persistent
+// kernels take the current device's own count from device_sms().
+constexpr int kSMs = 152;
+
+// SM count of the current device (cudaDevAttrMultiProcessorCount, cached per
+// device), at most kSMs.
+int device_sms();
 
 template <typename T> struct num;
 template <> struct num<float> {
@@ -125,7 +132,7 @@ int allow_dynamic_smem(const void *kernel);
 
 inline int grid_for(int64_t n, int threads, int per_sm = 8) {
     int64_t blocks = (n + threads - 1) / threads;
-    int64_t cap = (int64_t)kSMs * per_sm * 64;
+    int64_t cap = (int64_t)device_sms() * per_sm * 64;
     if (blocks > cap) blocks = cap;
     return blocks < 1 ? 1 : (int)blocks;
 }

@@ -55,7 +55,7 @@ int weighted_moments(const void *x, int d, int64_t n, const void *lw, int dtype,
                      cudaStream_t stream);
 int fit_factor(const double *mean, const double *cov, int d, const void *prev, double dof, double logconst,
                int dtype, void *out_loc, void *out_factor, void *out_lognorm, uint64_t *failures,
-               int64_t failure_index, float *out_inverse, cudaStream_t stream);
+               int64_t failure_index, float *out_inverse, double regularization, cudaStream_t stream);
 
 // elementwise (elementwise.cu)
 int static_assign(const void *cdf, int k, const void *u, int64_t n, int stratified, int32_t *slots, int dtype,

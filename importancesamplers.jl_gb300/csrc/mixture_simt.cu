@@ -744,7 +744,7 @@ static int launch_simt(MixParams<T> p, cudaStream_t stream) {
             if (e) return e;
         }
         const int64_t tiles = (p.n + kDrawRows - 1) / kDrawRows;
-        const int blocks = (int)min(tiles, (int64_t)kSMs * 64);
+        const int blocks = (int)min(tiles, (int64_t)device_sms() * 64);
         if (blocks < 1) return 0;
         { kern<<<blocks, kDrawRows * kDrawParts, smem, stream>>>(p); note_launch(); }
         return (int)cudaGetLastError();

@@ -601,7 +601,7 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     const int ncols = nw2 <= 32 ? 32 : nw2 <= 64 ? 64 : nw2 <= 128 ? 128 : nw2 <= 256 ? 256 : 512;
     occ = max(1, min(occ, 512 / ncols));  // TMEM allocations never wait
     p.ntiles = (int)((p.n + kTcTile - 1) / kTcTile);
-    const int blocks = min(p.ntiles, kSMs * occ);
+    const int blocks = min(p.ntiles, device_sms() * occ);
     if (blocks < 1) return 0;
     { kern<<<blocks, kTcThreads, smem, stream>>>(p); note_launch(); }
     return (int)cudaGetLastError();

@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
 
 int fit_factor(const double *mean, const double *cov, int d, const void *prev, double dof, double logconst,
                int dtype, void *out_loc, void *out_factor, void *out_lognorm, uint64_t *failures,
-               int64_t failure_index, float *out_inverse, cudaStream_t stream) {
+               int64_t failure_index, float *out_inverse, double regularization, cudaStream_t stream) {
     if (d > 64) return ISSM_E_UNSUPPORTED;
     size_t smem = sizeof(double) * (size_t)d * d;
     if (out_inverse != nullptr) {
@@ -443,7 +443,9 @@ int fit_factor(const double *mean, const double *cov, int d, const void *prev, d
     }
     // scalar constants formed once on the host
     const double mult = dof > 0.0 ? dof / (dof - 2.0) : 1.0;
-    const double reg = dtype == ISSM_F32 ? sqrt((double)FLT_EPSILON) : sqrt(DBL_EPSILON);
+    // sqrt(eps(T)) of the factor type unless the caller gives the coefficient
+    const double reg = regularization >= 0.0 ? regularization
+                       : dtype == ISSM_F32 ? sqrt((double)FLT_EPSILON) : sqrt(DBL_EPSILON);
     const double ridge_scale = reg * mult / (double)d;
     const double ridge_fallback = reg != 0.0 ? sqrt(reg) * sqrt(mult / (double)d) : 0.0;
     const double lognorm_const = dof > 0.0 ? logconst : -0.5 * (double)d * log(2.0 * 3.14159265358979323846);

@@ -381,7 +381,8 @@ constexpr int kMtMaxBlocks = kSMs * kMtCtasPerSm;
 
 static int moments_tc_blocks(int64_t n) {
     const int64_t t = (n + kMtTile - 1) / kMtTile;
-    return (int)(t < kMtMaxBlocks ? (t < 1 ? 1 : t) : kMtMaxBlocks);
+    const int64_t cap = (int64_t)device_sms() * kMtCtasPerSm;  // <= kMtMaxBlocks, the scratch bound
+    return (int)(t < cap ? (t < 1 ? 1 : t) : cap);
 }
 
 size_t moments_tc_workspace_bytes(int64_t n) {

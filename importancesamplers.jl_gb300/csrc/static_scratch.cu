@@ -15,6 +15,8 @@
 // One array per device means calls that overlap in time on the same device
 // (different streams, or host threads) race on it and corrupt each other's
 // results; callers serialise them.
+#include <cuda.h>
+
 #include <mutex>
 
 #include "issm_device.cuh"
@@ -35,25 +37,79 @@ static_assert(256 + 3 * sizeof(double) * (size_t)(kSMs * 8) <= kStaticCdfScratch
 
 static __device__ __align__(256) unsigned char g_cdf_scratch[kStaticCdfScratchBytes];
 
-constexpr int kMaxDevices = 64;
-static void *g_scratch_address[kMaxDevices];
+// The array's address belongs to a CUDA context, not to a device: a device
+// reset (cudaDeviceReset) destroys the primary context and the next one maps
+// the module elsewhere, and a host that creates its own contexts (CUDA.jl can)
+// has several per device. Addresses are therefore cached by the unique id of
+// the context current at the call (cuCtxGetId; ids are never reused within a
+// process), and a context seen for the first time is looked up afresh.
+constexpr int kMaxContexts = 64;
+static unsigned long long g_ctx_id[kMaxContexts];
+static void *g_scratch_address[kMaxContexts];
+static int g_contexts = 0;
 static std::mutex g_scratch_mutex;
 
-// Device address of g_cdf_scratch on the current device, looked up once per
-// device (the first lookup may load the module on that device).
-static int scratch_address(void **out) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
+static int driver_status(CUresult r) { return r == CUDA_SUCCESS ? ISSM_OK : (int)cudaErrorUnknown; }
+
+// The two driver calls are resolved through the runtime (the library does not
+// link libcuda, so it still loads on a machine without a driver).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+static CtxGetCurrentFn g_ctx_get_current = nullptr;
+static CtxGetIdFn g_ctx_get_id = nullptr;
+
+static int resolve_driver_calls() {
+    if (g_ctx_get_current && g_ctx_get_id) return ISSM_OK;
+    void *a = nullptr, *b = nullptr;
+    cudaDriverEntryPointQueryResult qa = cudaDriverEntryPointSymbolNotFound, qb = cudaDriverEntryPointSymbolNotFound;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa);
     if (e != cudaSuccess) return (int)e;
-    if (dev < 0 || dev >= kMaxDevices) return ISSM_E_UNSUPPORTED;
+    e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb);
+    if (e != cudaSuccess) return (int)e;
+    if (qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b)
+        return (int)cudaErrorSymbolNotFound;
+    g_ctx_get_current = (CtxGetCurrentFn)a;
+    g_ctx_get_id = (CtxGetIdFn)b;
+    return ISSM_OK;
+}
+
+// Device address of g_cdf_scratch in the current context. The first call in a
+// context makes that context current if the runtime had not yet done so, may
+// load the module, and looks the symbol up.
+static int scratch_address(void **out) {
     std::lock_guard<std::mutex> lock(g_scratch_mutex);
-    if (!g_scratch_address[dev]) {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_cdf_scratch);
+    int st = resolve_driver_calls();
+    if (st) return st;
+    CUcontext ctx = nullptr;
+    st = driver_status(g_ctx_get_current(&ctx));
+    if (st) return st;
+    void *fresh = nullptr;
+    if (!ctx) {  // no context yet: the runtime creates the device's primary context
+        cudaError_t e = cudaGetSymbolAddress(&fresh, g_cdf_scratch);
         if (e != cudaSuccess) return (int)e;
-        g_scratch_address[dev] = p;
+        st = driver_status(g_ctx_get_current(&ctx));
+        if (st) return st;
+        if (!ctx) return (int)cudaErrorNoDevice;
     }
-    *out = g_scratch_address[dev];
+    unsigned long long id = 0;
+    st = driver_status(g_ctx_get_id(ctx, &id));
+    if (st) return st;
+    for (int i = 0; i < g_contexts; ++i) {
+        if (g_ctx_id[i] == id) {
+            *out = g_scratch_address[i];
+            return ISSM_OK;
+        }
+    }
+    if (!fresh) {
+        cudaError_t e = cudaGetSymbolAddress(&fresh, g_cdf_scratch);
+        if (e != cudaSuccess) return (int)e;
+    }
+    if (g_contexts < kMaxContexts) {  // beyond the table the lookup simply repeats every call
+        g_ctx_id[g_contexts] = id;
+        g_scratch_address[g_contexts] = fresh;
+        ++g_contexts;
+    }
+    *out = fresh;
     return ISSM_OK;
 }
 

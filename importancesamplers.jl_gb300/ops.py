@@ -273,10 +273,13 @@ def weighted_moments(x, logweights, summary, shift, mean=None, cov=None, precisi
 
 
 def fit_factor(mean, cov, previous_factor, out_location, out_factor, out_lognorm, dof=0.0, logconstant=0.0,
-               failures=None, failure_index=0, out_inverse=None):
+               failures=None, failure_index=0, out_inverse=None, regularization=None):
+    """FP64 ridge + Cholesky fit into a history slot. regularization=None
+    keeps the reference's sqrt(eps(T)) of the factor type."""
     d = mean.numel()
-    native.call("issm_fit_factor_ex", native.ptr(mean), native.ptr(cov), d, native.ptr(previous_factor), float(dof),
-                float(logconstant), _dt(out_factor), native.ptr(out_location), native.ptr(out_factor),
+    reg = -1.0 if regularization is None else float(regularization)
+    native.call("issm_fit_factor_reg", native.ptr(mean), native.ptr(cov), d, native.ptr(previous_factor), float(dof),
+                float(logconstant), _dt(out_factor), reg, native.ptr(out_location), native.ptr(out_factor),
                 native.ptr(out_lognorm), native.ptr(out_inverse), native.ptr(failures), int(failure_index), _s())
 
 

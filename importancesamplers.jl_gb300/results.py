@@ -147,26 +147,44 @@ class UnweightedSamples:
         return self.samples.shape[0]
 
 
-def resample(seed, result, count=None, method=None):
+def resample(seed, result, count=None, method=None, cdf="exact"):
     """resample(rng, result, count; method) (src/resampling.jl:245-283).
 
     Multinomial draws `count` device uniforms from the seed; systematic draws
-    one. Both select on the exact fixed-point CDF (bit-identical ancestors on
-    any device)."""
+    one, u_i = (i + u) / count.
+
+    cdf="exact" (default) selects on the exact 64-bit fixed-point CDF: the
+    ancestors depend only on the weights and uniforms, bit-identical on any
+    device and in any scan order. cdf="reference" builds the CDF the way the
+    reference does, cumsum(exp(l - max)) / total in the weights' type
+    (_resampling_cdf!, src/resampling.jl:199-225), and selects with its
+    strict-< search and -Inf plateau repair (:92-118). The two rules pick
+    different ancestors only for a uniform within the reference CDF's
+    rounding of a boundary."""
     count = len(result) if count is None else int(count)
     if count <= 0:
         raise ValueError("resampling count must be positive")
+    if cdf not in ("exact", "reference"):
+        raise ValueError('cdf must be "exact" or "reference"')
     method = method or MultinomialResampling()
     sm = result.summary()
     if float(sm[1]) == 0.0:
         raise AllZeroWeightsError()
     dev = result.logweights.device
+    lw = result.logweights
     if isinstance(method, SystematicResampling):
         u = float(ops.fill_uniforms(1, torch.float64, dev, seed).item())
-        anc = ops.resample_systematic(result.logweights, u, count)
+        if cdf == "exact":
+            anc = ops.resample_systematic(lw, u, count)
+        else:
+            grid = (torch.arange(count, dtype=torch.float64, device=dev) + u) / count
+            anc = ops.resample_select(ops.resampling_cdf(lw), lw, grid.to(lw.dtype))
     elif isinstance(method, MultinomialResampling):
         u = ops.fill_uniforms(count, torch.float64, dev, seed)
-        anc = ops.resample_multinomial(result.logweights, u)
+        if cdf == "exact":
+            anc = ops.resample_multinomial(lw, u)
+        else:
+            anc = ops.resample_select(ops.resampling_cdf(lw), lw, u.to(lw.dtype))
     else:
         raise TypeError("unknown resampling method")
     x = result.samples

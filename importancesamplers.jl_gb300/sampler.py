@@ -127,8 +127,9 @@ class _Span:
 
 
 class PreparedSampler:
-    def __init__(self, seed, target, algorithm, device, precision, graphs=True):
+    def __init__(self, seed, target, algorithm, device, precision, graphs=True, regularization=None):
         self.profile = None  # list of (name, start, end, algorithmic bytes) when profiling
+        self.regularization = regularization
         self.seed = int(seed) & (2 ** 64 - 1)
         self.offset = 0
         self.target = target
@@ -172,16 +173,22 @@ class PreparedSampler:
         return out
 
 
-def prepare_sampler(seed, target, algorithm, device="cuda", precision=native.PREC_NATIVE, graphs=True):
+def prepare_sampler(seed, target, algorithm, device="cuda", precision=native.PREC_NATIVE, graphs=True,
+                    regularization=None):
     """prepare_sampler(rng, logtarget, alg) with the device applied: packs the
     proposal(s) and allocates every buffer on the device.
 
     graphs=True lets an AMIS sampler with a native target record its whole
     run as one CUDA graph on the second call and replay it afterwards (the
-    first call runs eagerly and sizes every workspace)."""
+    first call runs eagerly and sizes every workspace).
+
+    regularization: the moment fit's ridge coefficient. None keeps the
+    reference's sqrt(eps(T)) of the sample type; an FP64 sampler given
+    sqrt(eps(Float32)) fits exactly as an FP32 one would, which is how an FP64
+    run is compared with a reduced-precision run on the same draws."""
     native.require()
     device = torch.device(device)
-    s = PreparedSampler(seed, target, algorithm, device, precision, graphs)
+    s = PreparedSampler(seed, target, algorithm, device, precision, graphs, regularization)
     if isinstance(algorithm, ImportanceSampling):
         _prepare_static(s)
     elif isinstance(algorithm, (AMIS, NPMC)):
@@ -428,7 +435,8 @@ def _moment_body(s, is_npmc):
             if not last and s.precision != native.PREC_NATIVE and getattr(h, "inverse_factors", None) is not None:
                 inv = h.inverse_factors[t + 1]
             ops.fit_factor(s.mean, s.cov, h.scales[t], out_loc, out_fac, out_ln, dof=h.dof,
-                           logconstant=h.logconstant, failures=fail, failure_index=n_tot + 1, out_inverse=inv)
+                           logconstant=h.logconstant, failures=fail, failure_index=n_tot + 1, out_inverse=inv,
+                           regularization=s.regularization)
     ops.counter_advance(s.counter, s.offset)
 
 
@@ -511,8 +519,20 @@ def _finish_moment_summary(s):
 
 
 def _finish_moment(s, is_npmc):
-    words = s.round_failures.cpu().numpy()
-    summaries = s.summaries.cpu().numpy()
+    """Read the failure records, the per-round summaries and the last fit's
+    FP64 weighted mean back in one copy, raise on the first failed round and
+    build the result.
+
+    The result's `samples` is a view of the sampler's retained-sample buffer
+    (at d = 64, 40 x 50,000 samples that buffer is 512 MB, and copying it
+    would double the run's HBM traffic beyond the moments pass): it stays
+    valid until the sampler's next run, which overwrites it. Clone it to keep
+    it longer. The log weights and round ids are copies, as in the reference
+    (src/adaptive_gaussian_execution.jl:1090-1100 copies the log weights)."""
+    packed = torch.cat([s.round_failures.view(torch.float64).reshape(-1), s.summaries.reshape(-1), s.mean]).cpu()
+    words = packed[:3 * s.rounds].view(torch.int64).numpy().reshape(s.rounds, 3)
+    summaries = packed[3 * s.rounds:6 * s.rounds].numpy().reshape(s.rounds, 3)
+    moment_mean = packed[6 * s.rounds:].numpy().copy()
     if s.precision != native.PREC_NATIVE:
         if getattr(s, "run_workspace", None) is not None:
             _run_workspace_errors(s)
@@ -532,11 +552,80 @@ def _finish_moment(s, is_npmc):
         logz[t] = -np.inf if sm == 0 else m + np.log(sm) - np.log(n_t)
     for dst, src in zip(s.committed, (s.cand_loc, s.cand_factor, s.cand_lognorm[0])):
         dst.copy_(src)
+    # AMIS: the last round's moment pass runs over every retained sample with
+    # the final weights, so its mean is the weighted posterior mean. NPMC fits
+    # on the last round's clipped weights, so its mean is that fit's centre.
     diagnostics = {"method": "npmc" if is_npmc else "amis", "rounds": s.rounds, "round_sizes": list(s.schedule),
                    "round_ess": ess, "round_lognormalizers": logz, "target_evaluations": total,
-                   "proposal_evaluations": total if is_npmc else s.rounds * total, "failures": 0}
-    return WeightedSamples(s.samples.clone(), s.logweights.clone(), provenance={"round": s.round_ids.clone()},
+                   "proposal_evaluations": total if is_npmc else s.rounds * total, "failures": 0,
+                   "moment_mean": moment_mean}
+    return WeightedSamples(s.samples, s.logweights.clone(), provenance={"round": s.round_ids.clone()},
                            diagnostics=diagnostics)
+
+
+def reweigh_amis(sampler, precision=native.PREC_NATIVE, dtype=None):
+    """The final AMIS weights of a completed run, recomputed from scratch in
+    another precision form on the same retained samples and the same proposal
+    history: the full deterministic mixture log sum_t n_t q_t(x) over all T
+    slots (the closed form of the append recurrence,
+    src/amis_execution.jl:12-35), the weights log pi - log mixture + log N_T,
+    their summary, and the weighted mean.
+
+    This is the comparison of precision forms with the adaptation held fixed:
+    a whole adaptive run amplifies any difference in a fit into the next
+    round's draws, so two runs from the same draws part ways by more than
+    their arithmetic; re-weighing one run's samples under its own history
+    isolates the arithmetic. dtype: the sample/bank type of the form
+    (float32 for the tensor-core forms; default: the run's own).
+
+    Returns (log Z, FP64 weighted mean (d,), log weights (N,))."""
+    h = sampler.history
+    dtype = h.dtype if dtype is None else dtype
+    if precision != native.PREC_NATIVE and dtype != torch.float32:
+        raise ValueError("the tensor-core forms take float32 samples and proposals")
+    rounds, d, dev = sampler.rounds, h.d, sampler.device
+    total = int(sampler.offsets[-1])
+    bank = h.__class__(d, rounds, h.family, h.scale_kind, dtype, h.locations.to(dtype).contiguous(),
+                       h.scales.to(dtype).contiguous(), h.lognormalizers.to(dtype).contiguous(),
+                       None if h.dofs is None else h.dofs.to(dtype).contiguous(), h.range_risk)
+    if precision != native.PREC_NATIVE:
+        bank.attach_inverse_factors()
+    x = sampler.samples if sampler.samples.dtype == dtype else sampler.samples.to(dtype)
+    logtargets = sampler.target.bind(dev, dtype).evaluate(x, precision=precision)
+    logcounts = sampler.logcounts.to(dtype)
+    den = ops.denominator(native.DENOM_PREFIX, logcounts, terms=rounds)
+    lognum = ops.mixture_logdensity(bank, den, x, fixed_slot=rounds - 1, precision=precision)
+    lw = torch.empty(total, dtype=dtype, device=dev)
+    summary = torch.zeros(3, dtype=torch.float64, device=dev)
+    ops.amis_form_summary(logtargets, lognum, math.log(total), lw, summary)
+    shift = h.locations[rounds - 1].double().contiguous()
+    mean, _ = ops.weighted_moments(x, lw, summary, shift, precision=precision)
+    m, s, _ = summary.cpu().numpy()
+    logz = -math.inf if s == 0 else float(m + np.log(s) - np.log(total))
+    return logz, mean.cpu().numpy(), lw
+
+
+def share_normal_stream(sampler, dtype=torch.float32):
+    """Make `sampler` draw its standard normals from the `dtype` normal stream
+    of its own seed, converted to its sample type.
+
+    FP32 and FP64 normal streams of one seed are different numbers (an FP32
+    Philox block yields four 24-bit uniforms, an FP64 block two 53-bit ones).
+    An FP64 sampler set up this way draws, call for call, the same normals as
+    an FP32 or tensor-core sampler with the same seed, so the two runs differ
+    only by their arithmetic: this is how a reduced-precision run is compared
+    with an FP64 run on the same draws. The normals pass through a device
+    buffer, so the sampler runs its rounds eagerly (no whole-run graph)."""
+    def normals(n, dt):
+        if sampler.counter is not None:
+            out = ops.fill_normals_at(n, dtype, sampler.device, sampler.seed, sampler.counter, sampler.offset)
+        else:
+            out = ops.fill_normals(n, dtype, sampler.device, sampler.seed, sampler.offset)
+        sampler.offset += int(n) + 8
+        return out.to(dt)
+
+    sampler.normals = normals
+    return sampler
 
 
 def _npmc_clipped(lw):

@@ -95,35 +95,48 @@ class ServeLoop:
         return native.PREC_NATIVE
 
     def _launch(self, request, stream, now):
+        """Prepare and issue one run on `stream`. Returns the running run, or
+        the exception that stopped it from being issued (an allocation
+        failure, an argument the library rejects): that run is reported
+        failed and its scratch released, and the loop goes on."""
         scope = ("serve", next(self._ids))
-        with torch.cuda.stream(stream), native.workspace_scope(scope):
-            s = prepare_sampler(request.seed, request.target,
-                                AMIS(request.proposal, rounds=request.rounds, round_size=request.round_size),
-                                device=self.device, precision=self._form(request), graphs=False)
-            if s.busy:
-                raise SamplerBusyError("prepared sampler is already running")
-            s.busy = True
-            if native_body_eligible(s):
-                _native_body(s)  # every launch of the run in one native call
-            else:
-                _moment_body(s, False)
-            event = torch.cuda.Event()
-            event.record(stream)
+        try:
+            with torch.cuda.stream(stream), native.workspace_scope(scope):
+                s = prepare_sampler(request.seed, request.target,
+                                    AMIS(request.proposal, rounds=request.rounds, round_size=request.round_size),
+                                    device=self.device, precision=self._form(request), graphs=False)
+                if s.busy:
+                    raise SamplerBusyError("prepared sampler is already running")
+                s.busy = True
+                if native_body_eligible(s):
+                    _native_body(s)  # every launch of the run in one native call
+                else:
+                    _moment_body(s, False)
+                event = torch.cuda.Event()
+                event.record(stream)
+        except Exception as e:  # noqa: BLE001 - any launch failure fails this run only
+            # work issued before the failure may still be running on the
+            # stream: let it finish before the scope's buffers are freed
+            stream.synchronize()
+            native.release_scope(scope)
+            return e
         s.scope = scope
         return _Running(request, s, stream, event, now)
 
     def _retire(self, run, now):
         s = run.sampler
         error = None
-        with torch.cuda.stream(run.stream), native.workspace_scope(s.scope):
-            try:
-                pm, logz, ess = _finish_moment_summary(s)
-            except (RoundError, SamplerExecutionError) as e:  # this run failed; the others go on
-                d = run.request.proposal.dimension
-                pm, logz, ess, error = np.full(d, np.nan), float("nan"), 0.0, e
-            finally:
-                s.busy = False
-        native.release_scope(s.scope)
+        try:
+            with torch.cuda.stream(run.stream), native.workspace_scope(s.scope):
+                try:
+                    pm, logz, ess = _finish_moment_summary(s)
+                except (RoundError, SamplerExecutionError, RuntimeError) as e:  # this run failed; the others go on
+                    d = run.request.proposal.dimension
+                    pm, logz, ess, error = np.full(d, np.nan), float("nan"), 0.0, e
+                finally:
+                    s.busy = False
+        finally:
+            native.release_scope(s.scope)
         return ServeResult(run.request, pm, logz, ess, run.start, now, error)
 
     def run(self, requests, clock=time.perf_counter):
@@ -154,8 +167,15 @@ class ServeLoop:
             while queue and free and used + queue[0][2].footprint() <= self.memory_budget:
                 _, _, req = heapq.heappop(queue)
                 slot = free.pop()
-                running[slot] = self._launch(req, self.streams[slot], clock() - t0)
-                used += req.footprint()
+                launched = self._launch(req, self.streams[slot], clock() - t0)
+                if isinstance(launched, _Running):
+                    running[slot] = launched
+                    used += req.footprint()
+                else:  # not issued: reported failed now, slot and memory stay free
+                    t = clock() - t0
+                    results.append(ServeResult(req, np.full(req.proposal.dimension, np.nan), float("nan"), 0.0, t, t,
+                                               launched))
+                    free.append(slot)
             if not running and not queue and i < len(pending):
                 time.sleep(max(0.0, min(pending[i].arrival - (clock() - t0), 0.001)))
             elif running:

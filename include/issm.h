@@ -322,9 +322,11 @@ int issm_resampling_cdf(const void *logweights, int64_t n, int32_t dtype,
  * fixed device-memory budget): the workspace is one fixed 264 KiB __device__
  * array inside the library, so the call allocates nothing. At most
  * issm_resampling_cdf_static_max() = 2^27 log weights; larger n returns
- * ISSM_E_SCRATCH_LIMIT. The first call on each device looks up the array's
- * address (cudaGetSymbolAddress), which may load the module: make it before
- * any stream capture. The array is shared by all calls on a device, so calls
+ * ISSM_E_SCRATCH_LIMIT. The first call in each CUDA context (each device's
+ * primary context, again after a device reset, and any context the host
+ * creates itself) looks up the array's address there (cudaGetSymbolAddress),
+ * which may load the module: make that call before any stream capture. The
+ * array is shared by all calls on a device, so calls
  * that overlap in time there (other streams or threads) race and corrupt each
  * other's results: serialise them. Same results as issm_resampling_cdf. */
 int64_t issm_resampling_cdf_static_max(void);
@@ -418,6 +420,19 @@ int issm_fit_factor_ex(const double *mean, const double *cov, int32_t d,
                        void *out_factor, void *out_lognormalizer,
                        float *out_inverse, uint64_t *failures,
                        int64_t failure_index, issm_stream_t stream);
+/* As issm_fit_factor_ex with the ridge coefficient given: `regularization`
+ * >= 0 replaces sqrt(eps(T)) of _factor_scale_aware_ridge
+ * (src/adaptive_gaussian_execution.jl:385-389, which fixes it to the
+ * element type); a negative value keeps sqrt(eps(T)). An FP64 run that
+ * passes sqrt(eps(Float32)) fits with the same ridge as an FP32 run, so the
+ * two differ by their arithmetic alone. NaN is ISSM_E_KIND. */
+int issm_fit_factor_reg(const double *mean, const double *cov, int32_t d,
+                        const void *previous_factor, double dof,
+                        double logconstant, int32_t dtype,
+                        double regularization, void *out_location,
+                        void *out_factor, void *out_lognormalizer,
+                        float *out_inverse, uint64_t *failures,
+                        int64_t failure_index, issm_stream_t stream);
 
 /* ---- built-in batch targets ------------------------------------------------
  * Native equivalents of the batch callbacks the benchmark workloads pass to

@@ -753,6 +753,7 @@ void orc_philox_uniforms(uint64_t seed, uint64_t offset, int64_t n, double *out)
     }
 }
 void orc_philox_normals(uint64_t seed, uint64_t offset, int64_t n, double *out) {
+#pragma omp parallel for schedule(static) num_threads(orc_num_threads()) if (n > 65536)
     for (int64_t i = 0; i < n; ++i) {
         uint64_t e = offset + (uint64_t)i;
         uint32_t o[4];

@@ -237,6 +237,44 @@ def test_amis_graph_replay_matches_eager(issm, cuda, precision):
         assert torch.allclose(rg.samples, re_.samples, rtol=1e-6, atol=1e-6)
         assert torch.allclose(rg.logweights, re_.logweights, rtol=1e-5, atol=1e-5)
         assert np.allclose(rg.diagnostics["round_ess"], re_.diagnostics["round_ess"], rtol=1e-5)
-    # successive calls draw fresh numbers
-    assert not torch.equal(rg.samples[:100], issm.importance_sample_(g).samples[:100])
+    # successive calls draw fresh numbers (a result's samples view the
+    # sampler's buffer until its next run, so keep a copy)
+    first = rg.samples[:100].clone()
+    assert not torch.equal(first, issm.importance_sample_(g).samples[:100])
     assert int(g.counter.item()) == int(e.counter.item()) + g.offset
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_resampling_rules_disagree_only_at_rounded_boundaries(issm, cuda, dtype):
+    """The exact fixed-point rule and the reference's float CDF rule
+    (src/resampling.jl:92-118,199-225) on 2^20 random weights and uniforms:
+    they pick different ancestors only where a uniform lies within the float
+    CDF's rounding of the interval boundaries between the two picks (a float
+    CDF can merge several tiny-weight intervals into one rounding step). The
+    measured disagreement rate is bounded by n times the CDF's rounding."""
+    n = 1 << 20
+    g = torch.Generator(device=cuda).manual_seed(11)
+    lw = (torch.randn(n, generator=g, device=cuda, dtype=torch.float64) * 2.0).to(dtype)
+    res = issm.WeightedSamples(torch.arange(n, device=cuda, dtype=dtype), lw)
+    exact = issm.resample(5, res, n).ancestors.cpu().numpy()
+    ref = issm.resample(5, res, n, cdf="reference").ancestors.cpu().numpy()
+    u = issm.ops.fill_uniforms(n, torch.float64, cuda, 5).to(dtype).double().cpu().numpy()
+    w = np.exp(lw.double().cpu().numpy() - float(lw.max()))
+    cdf = np.cumsum(w) / w.sum()  # FP64 reference for the boundaries
+    diff = np.nonzero(exact != ref)[0]
+    eps = float(torch.finfo(dtype).eps)
+    # FP64 disagreements come from the fixed-point CDF's own quantisation
+    # (2^-42 of the largest weight per term at this n), not from the float CDF
+    tol = max(8 * eps, 1e-11)
+    rate = diff.size / n
+    assert rate <= 4 * n * eps + 1e-5, rate
+    for i in diff:
+        lo, hi = sorted((int(exact[i]), int(ref[i])))
+        # every boundary between the two picks (cdf[lo - 1] .. cdf[hi - 2],
+        # 0-based) lies within the rounding of the uniform
+        assert abs(u[i] - cdf[lo - 1]) <= tol, (i, u[i], cdf[lo - 1])
+        assert abs(u[i] - cdf[hi - 2]) <= tol, (i, u[i], cdf[hi - 2])
+    # systematic under both rules
+    exact_s = issm.resample(6, res, n, method=issm.SystematicResampling()).ancestors.cpu().numpy()
+    ref_s = issm.resample(6, res, n, method=issm.SystematicResampling(), cdf="reference").ancestors.cpu().numpy()
+    assert np.mean(exact_s != ref_s) <= 4 * n * eps + 1e-5

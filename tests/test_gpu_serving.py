@@ -182,3 +182,26 @@ def test_failed_run_is_reported_and_the_loop_continues(issm, cuda):
         alone = issm.serving.ServeLoop(cuda, max_inflight=1).run([r])[0]
         assert out[r.rid].error is None
         assert np.array_equal(out[r.rid].posterior_mean, alone.posterior_mean) and out[r.rid].logz == alone.logz
+
+
+def test_launch_failure_is_reported_and_the_loop_continues(issm, cuda):
+    """A request that cannot be issued (its batch target raises while the
+    run's launches are being queued) is reported with that error and NaN
+    outputs; its slot and memory return to the loop and the other runs
+    finish with their numbers alone."""
+    reqs, _ = _requests(issm, SPEC[:2])
+    d = 4
+
+    def broken(samples):
+        raise ValueError("target evaluation failed")
+
+    bad = issm.serving.ServeRequest(77, issm.LogTarget(batch=broken),
+                                    issm.FactorGaussian(np.zeros(d, dtype=np.float32), np.eye(d, dtype=np.float32)),
+                                    rounds=2, round_size=500, seed=3)
+    out = {r.rid: r for r in issm.serving.ServeLoop(cuda, max_inflight=2).run([bad] + reqs)}
+    assert isinstance(out[77].error, ValueError) and np.all(np.isnan(out[77].posterior_mean))
+    reqs2, _ = _requests(issm, SPEC[:2])
+    for r in reqs2:
+        alone = issm.serving.ServeLoop(cuda, max_inflight=1).run([r])[0]
+        assert out[r.rid].error is None
+        assert np.array_equal(out[r.rid].posterior_mean, alone.posterior_mean) and out[r.rid].logz == alone.logz
