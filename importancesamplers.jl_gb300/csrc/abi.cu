@@ -488,6 +488,76 @@ int issm_fit_factor(const double *mean, const double *cov, int32_t d, const void
                               out_lognormalizer, nullptr, failures, failure_index, stream);
 }
 
+size_t issm_select_workspace_bytes(void) { return select_workspace_bytes(); }
+
+int issm_select_kth(const void *values, int64_t n, int64_t k, int32_t dtype, void *out, void *workspace,
+                    size_t workspace_bytes, issm_stream_t stream) {
+    if (n < 1 || k < 1 || k > n) return ISSM_E_SIZE;
+    if (!values || !out || !workspace) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    if (workspace_bytes < select_workspace_bytes()) return ISSM_E_WORKSPACE;
+    return select_kth(values, n, k, dtype, out, workspace, (cudaStream_t)stream);
+}
+
+int issm_npmc_clip(const void *raw_logweights, int64_t n, int32_t dtype, void *clipped, void *threshold,
+                   void *workspace, size_t workspace_bytes, issm_stream_t stream) {
+    if (n < 1) return ISSM_E_SIZE;
+    if (!raw_logweights || !clipped || !threshold || !workspace) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    if (workspace_bytes < select_workspace_bytes()) return ISSM_E_WORKSPACE;
+    int64_t r = (int64_t)std::sqrt((double)n);  // isqrt(n)
+    while (r * r > n) --r;
+    while ((r + 1) * (r + 1) <= n) ++r;
+    ISSM_TRY(select_kth(raw_logweights, n, n - r + 1, dtype, threshold, workspace, (cudaStream_t)stream));
+    return clip_logweights(raw_logweights, n, dtype, threshold, clipped, (cudaStream_t)stream);
+}
+
+int issm_population_local_weights(const void *local_logweights, const void *samples, int32_t d, int32_t dtype,
+                                  const int64_t *starts, const int64_t *counts, const double *thresholds,
+                                  int32_t k, double tolerance, int32_t max_iterations, void *normalized_weights,
+                                  void *local_ess, void *tempering_powers, uint8_t *status, void *raw_means,
+                                  issm_stream_t stream) {
+    if (k < 0 || d < 1 || max_iterations < 0) return ISSM_E_SIZE;
+    if (k == 0) return ISSM_OK;
+    if (!local_logweights || !starts || !counts || !thresholds || !normalized_weights || !local_ess ||
+        !tempering_powers || !status)
+        return ISSM_E_NULL;
+    if (raw_means && !samples) return ISSM_E_NULL;
+    if (!(tolerance >= 0.0)) return ISSM_E_KIND;
+    ISSM_TRY(check_dtype(dtype));
+    return population_local_weights(local_logweights, samples, d, dtype, starts, counts, thresholds, k, tolerance,
+                                    max_iterations, normalized_weights, local_ess, tempering_powers, status,
+                                    raw_means, (cudaStream_t)stream);
+}
+
+int issm_population_covariances(const void *samples, int32_t d, int32_t dtype, const void *normalized_weights,
+                                const void *tempering_powers, const uint8_t *status, const void *locations,
+                                const issm_bank *current, const int64_t *starts, const int64_t *counts, int32_t k,
+                                void *centres, void *covariances, issm_stream_t stream) {
+    if (k < 0 || d < 1) return ISSM_E_SIZE;
+    if (d > 64) return ISSM_E_UNSUPPORTED;
+    if (k == 0) return ISSM_OK;
+    if (!samples || !normalized_weights || !tempering_powers || !status || !locations || !current || !starts ||
+        !counts || !centres || !covariances || !current->scales)
+        return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    if (current->dtype != dtype || current->dim != d || current->count < k) return ISSM_E_DTYPE;
+    if (current->scale_kind < ISSM_SCALE_FACTOR || current->scale_kind > ISSM_SCALE_SPHERICAL) return ISSM_E_KIND;
+    if (current->family == ISSM_STUDENT_T && !current->dofs) return ISSM_E_NULL;
+    return population_covariances(samples, d, dtype, normalized_weights, tempering_powers, status, locations, current,
+                                  starts, counts, k, centres, covariances, (cudaStream_t)stream);
+}
+
+int issm_population_factors(const void *covariances, int32_t d, int32_t k, int32_t dtype, const uint8_t *status,
+                            const void *dofs, void *factors, int32_t *info, issm_stream_t stream) {
+    if (k < 0 || d < 1) return ISSM_E_SIZE;
+    if (d > 64) return ISSM_E_UNSUPPORTED;
+    if (k == 0) return ISSM_OK;
+    if (!covariances || !status || !factors || !info) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    return population_factors(covariances, d, k, dtype, status, dofs, factors, info, (cudaStream_t)stream);
+}
+
 int issm_target_logdensity(const issm_target *target, const void *x, int64_t n, void *out, issm_stream_t stream) {
     if (!target) return ISSM_E_NULL;
     if (n < 0 || target->dim < 1) return ISSM_E_SIZE;

@@ -57,6 +57,23 @@ int fit_factor(const double *mean, const double *cov, int d, const void *prev, d
                int dtype, void *out_loc, void *out_factor, void *out_lognorm, uint64_t *failures,
                int64_t failure_index, float *out_inverse, double regularization, cudaStream_t stream);
 
+// population local weights, covariances, factors (population.cu)
+int population_local_weights(const void *lw, const void *x, int d, int dtype, const int64_t *starts,
+                             const int64_t *counts, const double *thresholds, int k, double tolerance,
+                             int max_iterations, void *weights, void *local_ess, void *powers, uint8_t *status,
+                             void *raw_means, cudaStream_t stream);
+int population_covariances(const void *x, int d, int dtype, const void *weights, const void *powers,
+                           const uint8_t *status, const void *locations, const issm_bank *bank,
+                           const int64_t *starts, const int64_t *counts, int k, void *centres, void *covs,
+                           cudaStream_t stream);
+int population_factors(const void *covs, int d, int k, int dtype, const uint8_t *status, const void *dofs,
+                       void *factors, int32_t *info, cudaStream_t stream);
+
+// order statistic and N-PMC clipping (select.cu)
+size_t select_workspace_bytes();
+int select_kth(const void *v, int64_t n, int64_t k, int dtype, void *out, void *ws, cudaStream_t stream);
+int clip_logweights(const void *raw, int64_t n, int dtype, const void *threshold, void *out, cudaStream_t stream);
+
 // elementwise (elementwise.cu)
 int static_assign(const void *cdf, int k, const void *u, int64_t n, int stratified, int32_t *slots, int dtype,
                   cudaStream_t stream);

@@ -138,8 +138,10 @@ constexpr int kConvWarps = 8;  // stage sample tiles and build the A operand
 constexpr int kEpiWarps = 4;   // one per TMEM lane quadrant
 constexpr int kConvThreads = 32 * kConvWarps;
 constexpr int kFirstEpiWarp = 1 + kConvWarps;
-constexpr int kTcThreads = 32 * (1 + kConvWarps + kEpiWarps);
+constexpr int kStagerWarp = kFirstEpiWarp + kEpiWarps;  // bulk copies of the staged sample tiles
+constexpr int kTcThreads = 32 * (2 + kConvWarps + kEpiWarps);
 constexpr int kBRing = 3;      // operand buffers in flight when a tile needs several chunks
+constexpr int kMaxRawStages = 4;
 
 template <int KIND, int SPLIT, int DP, bool DIRECT>
 __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
@@ -170,8 +172,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     unsigned char *s_b = s_a + (size_t)nbufA * NPART * A_PART;
     float *s_c = reinterpret_cast<float *>(s_b + (size_t)nbufB * CHUNK_BYTES);
     __shared__ __align__(8) uint64_t a_full[2], a_empty[2], b_full[kBRing], b_empty[kBRing], d_full[2], d_empty[2];
+    __shared__ __align__(8) uint64_t raw_full[kMaxRawStages], raw_empty[kMaxRawStages];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_flag;
+    // staged tiles with rows of 16-byte multiples at 16-byte aligned
+    // addresses arrive by one bulk copy per row from the stager warp
+    const bool vec = (p.d % 4 == 0) && ((reinterpret_cast<uintptr_t>(p.x) & 15) == 0);
+    const bool bulk = !DIRECT && S > 0 && vec;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int NW = chunk * DP;  // TMEM columns of one accumulator
@@ -187,6 +194,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
         for (int b = 0; b < kBRing; ++b) {
             tc::mbar_init(&b_full[b], 1);
             tc::mbar_init(&b_empty[b], 1);
+        }
+        for (int s = 0; s < kMaxRawStages; ++s) {
+            tc::mbar_init(&raw_full[s], 1);
+            tc::mbar_init(&raw_empty[s], kConvWarps);
         }
         tc::fence_mbar_init();
         abort_flag = 0;
@@ -297,37 +308,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     } else if (warp < kFirstEpiWarp) {
         // ================= converters: sample tiles -> A operand =================
         const int ctid = tid - 32;
-        const bool vec = (p.d % 4 == 0) && ((reinterpret_cast<uintptr_t>(p.x) & 15) == 0);
-        auto issue_raw = [&](int it) {
+        auto issue_raw = [&](int it) {  // 4-byte cp.async staging (rows without bulk copies)
             if (it < my_tiles) {
                 const int64_t row0 = tile_of(it) * kTcTile;
                 const int rows = (int)min((int64_t)kTcTile, p.n - row0);
                 float *dst = reinterpret_cast<float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
                 const float *src = p.x + row0 * p.d;
-                if (vec && p.d == DP) {
-                    constexpr int Q4 = DP / 4;
-                    const int total = rows * Q4;
-                    for (int e = ctid; e < total; e += kConvThreads) {
-                        const int r = e / Q4, c4 = e % Q4;
-                        tc::cp_async16(dst + r * RS + c4 * 4, src + (size_t)e * 4);
-                    }
-                } else if (vec) {
-                    const int q4 = p.d >> 2, total = rows * q4;
-                    for (int e = ctid; e < total; e += kConvThreads) {
-                        const int r = e / q4, c4 = e - r * q4;
-                        tc::cp_async16(dst + r * RS + c4 * 4, src + (size_t)r * p.d + c4 * 4);
-                    }
-                } else {
-                    const int total = rows * p.d;
-                    for (int e = ctid; e < total; e += kConvThreads) {
-                        const int r = e / p.d, c = e - r * p.d;
-                        tc::cp_async4(dst + r * RS + c, src + (size_t)r * p.d + c);
-                    }
+                const int total = rows * p.d;
+                for (int e = ctid; e < total; e += kConvThreads) {
+                    const int r = e / p.d, c = e - r * p.d;
+                    tc::cp_async4(dst + r * RS + c, src + (size_t)r * p.d + c);
                 }
             }
             tc::cp_async_commit();
         };
-        for (int s = 0; s < S; ++s) issue_raw(s);
+        if (!DIRECT && !bulk)
+            for (int s = 0; s < S; ++s) issue_raw(s);
         const int row = ctid & (kTcTile - 1), half = ctid >> 7;
         constexpr int HV = DP / 8;  // float4s of this thread's half row
         for (int it = 0; it < my_tiles; ++it) {
@@ -350,15 +346,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
                                             active && c + 3 < p.d ? xr[c + 3] : 0.f);
                     }
                 }
-            } else {
-                if (S == 1) tc::cp_async_wait<0>();
-                else if (S == 2) tc::cp_async_wait<1>();
-                else tc::cp_async_wait<2>();
-                tc::named_sync(1, kConvThreads);
             }
             bool ok = true;
+            if (!DIRECT) {
+                if (bulk) {
+                    // every lane acquires the stage's bytes itself; the outcome is made warp-uniform
+                    ok = __all_sync(0xffffffffu, wait(&raw_full[it % S], (uint32_t)((it / S) & 1)));
+                } else {
+                    if (S == 1) tc::cp_async_wait<0>();
+                    else if (S == 2) tc::cp_async_wait<1>();
+                    else tc::cp_async_wait<2>();
+                    tc::named_sync(1, kConvThreads);
+                }
+            }
             const int abuf = it % nbufA;
-            if (it >= nbufA) {
+            if (it >= nbufA && ok) {
                 if (lane == 0) ok = wait(&a_empty[abuf], (uint32_t)(((it - nbufA) / nbufA) & 1));
                 ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
             }
@@ -406,12 +408,41 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
             tc::fence_proxy_async();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&a_full[it % nbufA]);
-            if (!DIRECT) {
+            if (bulk) {
+                if (lane == 0) tc::mbar_arrive(&raw_empty[it % S]);  // this warp is done with the stage
+            } else if (!DIRECT) {
                 tc::named_sync(1, kConvThreads);  // the stage is consumed: refill it
                 issue_raw(it + S);
             }
         }
         tc::cp_async_wait_all();
+    } else if (warp == kStagerWarp) {
+        // ================= stager: one bulk copy per sample row into the padded ring =================
+        if (bulk) {
+            int issued = 0;
+            const uint32_t rb = (uint32_t)p.d * 4u;
+            for (int it = 0; it < my_tiles; ++it) {
+                const int s = it % S;
+                if (it >= S) {
+                    int fine = 1;
+                    if (lane == 0) fine = wait(&raw_empty[s], (uint32_t)(((it / S) - 1) & 1));
+                    if (!__shfl_sync(0xffffffffu, fine, 0)) break;
+                }
+                const int64_t row0 = tile_of(it) * kTcTile;
+                const int rows = (int)min((int64_t)kTcTile, p.n - row0);
+                float *dst = reinterpret_cast<float *>(s_raw + (size_t)s * RAW_BYTES);
+                if (lane == 0) tc::mbar_arrive_expect_tx(&raw_full[s], (uint32_t)rows * rb);
+                __syncwarp();
+                for (int r = lane; r < rows; r += 32)
+                    tc::bulk_copy_g2s(dst + r * RS, p.x + (row0 + r) * p.d, rb, &raw_full[s]);
+                issued = it + 1;
+            }
+            // every copy lands before the CTA can exit (the converters consume
+            // them all unless a wait timed out)
+            if (lane == 0)
+                for (int it = max(0, issued - S); it < issued; ++it)
+                    tc::mbar_wait(&raw_full[it % S], (uint32_t)((it / S) & 1));
+        }
     } else {
         // ================= epilogue: radial densities and the log-sum-exp =================
         const int qd = warp & 3;

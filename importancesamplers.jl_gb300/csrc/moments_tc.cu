@@ -24,11 +24,15 @@
 //
 // A is stored MN-major: each sample's 8-coordinate groups are 16-byte chunks,
 // so two threads convert a sample row straight from the staged tile. Warp
-// roles: warp 0 issues the MMAs; warps 1..8 stage tiles with cp.async into a
-// three-deep ring of padded stages and build A (double-buffered), handing
-// buffers over through mbarriers. Per-CTA partials are summed across CTAs
-// (compensated FP32) and mean = c + S1/S0, cov = S2/S0 - (S1/S0)(S1/S0)^T
-// in FP64.
+// roles: warp 0 issues the MMAs; warps 1..8 build A (double-buffered) from
+// the staged tiles; warp 9 stages the tiles. When rows are 16-byte multiples
+// (d % 4 == 0, aligned arrays) the stager keeps a four-deep ring of padded
+// stages filled with one bulk copy per sample row (cp.async.bulk, completion
+// counted in bytes on the stage's mbarrier); converters wait on that
+// mbarrier and release the stage with one arrival per warp, so no role ever
+// waits on a CTA-wide barrier. Other shapes stage with 4-byte cp.async from
+// the converters. Per-CTA partials are summed across CTAs (compensated FP32)
+// and mean = c + S1/S0, cov = S2/S0 - (S1/S0)(S1/S0)^T in FP64.
 #include "issm_device.cuh"
 #include "issm_internal.h"
 #include "tcgen05.cuh"
@@ -37,14 +41,15 @@ namespace issm {
 
 constexpr int kMtConvWarps = 8;
 constexpr int kMtConvThreads = 32 * kMtConvWarps;
-constexpr int kMtThreads = 32 * (1 + kMtConvWarps);
+constexpr int kMtStagerWarp = 1 + kMtConvWarps;
+constexpr int kMtThreads = 32 * (2 + kMtConvWarps);  // issuer, converters, stager
 constexpr int kMtTile = 128;   // samples per tile = MMA K extent per tile
 constexpr int kMtTPR = kMtConvThreads / kMtTile;  // converter threads per sample row
 constexpr int kMtGPT = 8 / kMtTPR;                // coordinate groups (of 8) per converter thread
 constexpr int kMtCtasPerSm = 1;  // CTAs per SM (two 64-sample pipelines measured the same)
 constexpr int kMtCols = 80;    // MMA N (64 coordinates + sqrt(w) + padding)
-constexpr int kMtStages = 3;   // staged sample tiles in flight
-constexpr int kMtRS = 68;      // padded row of a staged tile (floats)
+constexpr int kMtStages = 4;   // staged sample tiles in flight
+constexpr int kMtRS = 68;      // padded row of a staged tile (floats): conflict-free row reads
 constexpr int kMtRawBytes = kMtTile * kMtRS * 4 + kMtTile * 4;  // rows, then the tile's log weights
 // Rows 0..71 (9 row groups: 64 coordinates, sqrt(w), zeros) are stored; the
 // MMA's M = 128 also reads row groups 9..15, which land in the next buffer or
@@ -54,6 +59,7 @@ constexpr int kMtGroups = 9;
 constexpr int kMtPart = kMtGroups * kMtTile * 16;
 constexpr size_t kMtSmem = (size_t)2 * 2 * kMtPart + (size_t)kMtStages * kMtRawBytes + 256;
 static_assert((size_t)3 * kMtPart + (size_t)16 * kMtTile * 16 <= kMtSmem, "M = 128 reads stay inside the CTA's shared memory");
+static_assert(kMtSmem <= 232448 - 1024, "dynamic shared memory per CTA");
 constexpr int kMtPartial = 65 * kMtCols;  // P = H / 2 + X of one CTA (S = P + P^T: H is symmetric)
 
 __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(const float *__restrict__ x, int d, int64_t n,
@@ -67,7 +73,7 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
     unsigned char *s_a = smem;                                    // [buf][part] x kMtPart
     unsigned char *s_raw = smem + (size_t)2 * 2 * kMtPart;
     float *s_c = reinterpret_cast<float *>(s_raw + (size_t)kMtStages * kMtRawBytes);
-    __shared__ __align__(8) uint64_t a_full[2], a_empty[2];
+    __shared__ __align__(8) uint64_t a_full[2], a_empty[2], raw_full[kMtStages], raw_empty[kMtStages];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_flag;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -76,6 +82,10 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&a_full[b], kMtConvWarps);
             tc::mbar_init(&a_empty[b], 1);
+        }
+        for (int s = 0; s < kMtStages; ++s) {
+            tc::mbar_init(&raw_full[s], 1);
+            tc::mbar_init(&raw_empty[s], kMtConvWarps);
         }
         tc::fence_mbar_init();
         abort_flag = 0;
@@ -90,6 +100,7 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
     const int64_t ntiles = (n + kMtTile - 1) / kMtTile;
     const int my_tiles = (int)((ntiles - (int64_t)blockIdx.x + gridDim.x - 1) / gridDim.x);
     auto tile_of = [&](int it) -> int64_t { return (int64_t)blockIdx.x + (int64_t)it * gridDim.x; };
+    auto tile_rows = [&](int it) -> int { return (int)min((int64_t)kMtTile, n - tile_of(it) * kMtTile); };
     auto wait = [&](uint64_t *bar, uint32_t parity) -> bool {
         if (abort_flag) return false;
         if (tc::mbar_wait(bar, parity)) return true;
@@ -97,6 +108,9 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
         abort_flag = 1;
         return false;
     };
+    // rows of 16-byte multiples at 16-byte aligned addresses: bulk copies
+    const bool bulk = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0) &&
+                      ((reinterpret_cast<uintptr_t>(lw) & 15) == 0);
 
     if (warp == 0) {
         // ---- issuer: H += Ah Ah^T + Al Al^T, X += Al Ah^T per K slice ----
@@ -122,66 +136,80 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
             }
             __syncwarp();
         }
+    } else if (warp == kMtStagerWarp) {
+        // ---- stager: one bulk copy per sample row into the padded ring, the
+        // tile's log weights (whole 16-byte groups) in one more ----
+        if (bulk) {
+            int issued = 0;
+            for (int it = 0; it < my_tiles; ++it) {
+                const int s = it % kMtStages;
+                if (it >= kMtStages) {
+                    int ok = 1;
+                    if (lane == 0) ok = wait(&raw_empty[s], (uint32_t)(((it / kMtStages) - 1) & 1));
+                    if (!__shfl_sync(0xffffffffu, ok, 0)) break;
+                }
+                const int64_t row0 = tile_of(it) * kMtTile;
+                const int rows = tile_rows(it);
+                const uint32_t rb = (uint32_t)d * 4u, wb = (uint32_t)(rows & ~3) * 4u;
+                float *dst = reinterpret_cast<float *>(s_raw + (size_t)s * kMtRawBytes);
+                if (lane == 0) tc::mbar_arrive_expect_tx(&raw_full[s], (uint32_t)rows * rb + wb);
+                __syncwarp();
+                for (int r = lane; r < rows; r += 32)
+                    tc::bulk_copy_g2s(dst + r * kMtRS, x + (row0 + r) * d, rb, &raw_full[s]);
+                if (lane == 0 && wb > 0) tc::bulk_copy_g2s(dst + kMtTile * kMtRS, lw + row0, wb, &raw_full[s]);
+                issued = it + 1;
+            }
+            // every copy lands before the CTA can exit (the converters consume
+            // them all unless a wait timed out)
+            if (lane == 0)
+                for (int it = max(0, issued - kMtStages); it < issued; ++it)
+                    tc::mbar_wait(&raw_full[it % kMtStages], (uint32_t)((it / kMtStages) & 1));
+        }
     } else {
-        // ---- converters: stage tiles and build A = sqrt(w) (x - c) ----
+        // ---- converters: build A = sqrt(w) (x - c) from the staged tiles ----
         const int ctid = tid - 32;
-        const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0) &&
-                         ((reinterpret_cast<uintptr_t>(lw) & 15) == 0);
-        auto issue_raw = [&](int it) {
+        auto issue_raw = [&](int it) {  // 4-byte cp.async staging (shapes without bulk copies)
             if (it < my_tiles) {
                 const int64_t row0 = tile_of(it) * kMtTile;
-                const int rows = (int)min((int64_t)kMtTile, n - row0);
+                const int rows = tile_rows(it);
                 float *dst = reinterpret_cast<float *>(s_raw + (size_t)(it % kMtStages) * kMtRawBytes);
                 float *dlw = dst + kMtTile * kMtRS;
                 const float *src = x + row0 * d;
-                if (vec && d == 64) {
-                    const int total = rows * 16;
-                    for (int e = ctid; e < total; e += kMtConvThreads)
-                        tc::cp_async16(dst + (e >> 4) * kMtRS + (e & 15) * 4, src + (size_t)e * 4);
-                    if (rows == kMtTile) {
-                        if (ctid < kMtTile / 4) tc::cp_async16(dlw + ctid * 4, lw + row0 + ctid * 4);
-                    } else {
-                        for (int r = ctid; r < rows; r += kMtConvThreads) tc::cp_async4(dlw + r, lw + row0 + r);
-                    }
-                } else if (vec) {
-                    const int q4 = d >> 2, total = rows * q4;
-                    for (int e = ctid; e < total; e += kMtConvThreads) {
-                        const int r = e / q4, c4 = e - r * q4;
-                        tc::cp_async16(dst + r * kMtRS + c4 * 4, src + (size_t)e * 4);
-                    }
-                    if (rows == kMtTile) {
-                        if (ctid < kMtTile / 4) tc::cp_async16(dlw + ctid * 4, lw + row0 + ctid * 4);
-                    } else {
-                        for (int r = ctid; r < rows; r += kMtConvThreads) tc::cp_async4(dlw + r, lw + row0 + r);
-                    }
-                } else {
-                    for (int e = ctid; e < rows * d; e += kMtConvThreads) {
-                        const int r = e / d, c = e - r * d;
-                        tc::cp_async4(dst + r * kMtRS + c, src + (size_t)r * d + c);
-                    }
-                    for (int r = ctid; r < rows; r += kMtConvThreads) tc::cp_async4(dlw + r, lw + row0 + r);
+                for (int e = ctid; e < rows * d; e += kMtConvThreads) {
+                    const int r = e / d, c = e - r * d;
+                    tc::cp_async4(dst + r * kMtRS + c, src + (size_t)r * d + c);
                 }
+                for (int r = ctid; r < rows; r += kMtConvThreads) tc::cp_async4(dlw + r, lw + row0 + r);
             }
             tc::cp_async_commit();
         };
-        for (int s = 0; s < kMtStages; ++s) issue_raw(s);
+        if (!bulk)
+            for (int s = 0; s < kMtStages; ++s) issue_raw(s);
         const int k = ctid % kMtTile, part = ctid / kMtTile;
         for (int it = 0; it < my_tiles; ++it) {
-            const int buf = it & 1;
-            tc::cp_async_wait<kMtStages - 1>();
-            tc::named_sync(1, kMtConvThreads);
+            const int buf = it & 1, stage = it % kMtStages;
             bool ok = true;
-            if (it >= 2) {
+            if (bulk) {
+                // every lane acquires the stage's bytes itself; the outcome is made warp-uniform
+                ok = __all_sync(0xffffffffu, wait(&raw_full[stage], (uint32_t)((it / kMtStages) & 1)));
+            } else {
+                tc::cp_async_wait<kMtStages - 1>();
+                tc::named_sync(1, kMtConvThreads);
+            }
+            if (it >= 2 && ok) {
                 if (lane == 0) ok = wait(&a_empty[buf], (uint32_t)(((it - 2) >> 1) & 1));
                 ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
             }
             if (ok) {
-                const float *raw = reinterpret_cast<const float *>(s_raw + (size_t)(it % kMtStages) * kMtRawBytes);
+                const float *raw = reinterpret_cast<const float *>(s_raw + (size_t)stage * kMtRawBytes);
                 unsigned char *ah = s_a + (size_t)buf * 2 * kMtPart;
                 unsigned char *al = ah + kMtPart;
                 const int64_t i = tile_of(it) * kMtTile + k;
                 const bool active = i < n;
-                const float l = active ? raw[kMtTile * kMtRS + k] : -INFINITY;
+                // the bulk copy carries whole 16-byte groups of weights; the
+                // (at most three) beyond them come from global memory
+                const int staged_w = bulk ? (tile_rows(it) & ~3) : kMtTile;
+                const float l = !active ? -INFINITY : (k < staged_w ? raw[kMtTile * kMtRS + k] : lw[i]);
                 const float sw = l == -INFINITY ? 0.f : expf(0.5f * (l - m)) * inv_sqrt_s;
                 const bool full = active && d == 64;
 #pragma unroll
@@ -237,10 +265,14 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
             tc::fence_proxy_async();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&a_full[buf]);
-            tc::named_sync(1, kMtConvThreads);  // the stage is consumed: refill it
-            issue_raw(it + kMtStages);
+            if (bulk) {
+                if (lane == 0) tc::mbar_arrive(&raw_empty[stage]);  // this warp is done with the stage
+            } else {
+                tc::named_sync(1, kMtConvThreads);  // the stage is consumed: refill it
+                issue_raw(it + kMtStages);
+            }
         }
-        tc::cp_async_wait_all();
+        if (!bulk) tc::cp_async_wait_all();
     }
     // ---- the last commit tracks every MMA of the CTA ----
     tc::fence_before_sync();

@@ -114,6 +114,13 @@ SIGNATURES = [
     ("issm_fit_factor", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _p, _p, _p, _p, _i64, _p]),
     ("issm_fit_factor_ex", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _p, _p, _p, _p, _p, _i64, _p]),
     ("issm_fit_factor_reg", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _d, _p, _p, _p, _p, _p, _i64, _p]),
+    ("issm_select_workspace_bytes", _sz, []),
+    ("issm_select_kth", C.c_int, [_p, _i64, _i64, _i32, _p, _p, _sz, _p]),
+    ("issm_npmc_clip", C.c_int, [_p, _i64, _i32, _p, _p, _p, _sz, _p]),
+    ("issm_population_local_weights", C.c_int, [_p, _p, _i32, _i32, _p, _p, _p, _i32, _d, _i32, _p, _p, _p, _p,
+                                                _p, _p]),
+    ("issm_population_covariances", C.c_int, [_p, _i32, _i32, _p, _p, _p, _p, _bank, _p, _p, _i32, _p, _p, _p]),
+    ("issm_population_factors", C.c_int, [_p, _i32, _i32, _i32, _p, _p, _p, _p, _p]),
     ("issm_target_logdensity", C.c_int, [C.POINTER(Target), _p, _i64, _p, _p]),
     ("issm_tc_selftest", C.c_int, [_p, _p, _p, _i32, _i32, _i32, _p, _p]),
     ("issm_amis_run_workspace_bytes", _sz, [_i32, _i64, _i32]),

@@ -283,6 +283,71 @@ def fit_factor(mean, cov, previous_factor, out_location, out_factor, out_lognorm
                 native.ptr(out_lognorm), native.ptr(out_inverse), native.ptr(failures), int(failure_index), _s())
 
 
+def select_kth(values, k, out=None):
+    """The k-th smallest (1-based) of `values` into a device scalar (NaN last)."""
+    out = torch.empty(1, dtype=values.dtype, device=values.device) if out is None else out
+    ws = native.workspace(native.lib().issm_select_workspace_bytes(), values.device, "select")
+    native.call("issm_select_kth", native.ptr(values), values.numel(), int(k), _dt(values), native.ptr(out),
+                native.ptr(ws), ws.numel(), _s())
+    return out
+
+
+def npmc_clip(raw, out=None, threshold=None):
+    """min(raw, (n - isqrt(n) + 1)-th smallest of raw), on the device."""
+    out = torch.empty_like(raw) if out is None else out
+    threshold = torch.empty(1, dtype=raw.dtype, device=raw.device) if threshold is None else threshold
+    ws = native.workspace(native.lib().issm_select_workspace_bytes(), raw.device, "select")
+    native.call("issm_npmc_clip", native.ptr(raw), raw.numel(), _dt(raw), native.ptr(out), native.ptr(threshold),
+                native.ptr(ws), ws.numel(), _s())
+    return out, threshold
+
+
+def population_local_weights(local_logweights, starts, counts, thresholds, samples=None, tolerance=1e-6,
+                             max_iterations=60, raw_means=True):
+    """Per-slot normalised weights, local ESS, tempering power and status of a
+    population whose slot k owns samples starts[k] .. starts[k] + counts[k] - 1
+    (device int64 tensors; thresholds a device float64 tensor), and the
+    untempered weighted raw means (d x K as (K, d)) when `samples` is given."""
+    k = starts.numel()
+    dev, dt = local_logweights.device, local_logweights.dtype
+    weights = torch.zeros_like(local_logweights)
+    ess = torch.zeros(k, dtype=dt, device=dev)
+    powers = torch.zeros(k, dtype=dt, device=dev)
+    status = torch.zeros(k, dtype=torch.uint8, device=dev)
+    d = samples.shape[1] if samples is not None else 1
+    means = torch.zeros(k, d, dtype=dt, device=dev) if (raw_means and samples is not None) else None
+    native.call("issm_population_local_weights", native.ptr(local_logweights), native.ptr(samples), d, _dt(weights),
+                native.ptr(starts), native.ptr(counts), native.ptr(thresholds), k, float(tolerance),
+                int(max_iterations), native.ptr(weights), native.ptr(ess), native.ptr(powers), native.ptr(status),
+                native.ptr(means), _s())
+    return weights, ess, powers, status, means
+
+
+def population_covariances(samples, weights, powers, status, bank, starts, counts):
+    """Per-slot centres (K, d) and covariances (K, d, d) (symmetric, so the
+    column-major d x d x K layout reads the same)."""
+    k = starts.numel()
+    n, d = samples.shape
+    centres = torch.empty(k, d, dtype=samples.dtype, device=samples.device)
+    covs = torch.empty(k, d, d, dtype=samples.dtype, device=samples.device)
+    native.call("issm_population_covariances", native.ptr(samples), d, _dt(samples), native.ptr(weights),
+                native.ptr(powers), native.ptr(status), native.ptr(bank.locations), bank.ref(), native.ptr(starts),
+                native.ptr(counts), k, native.ptr(centres), native.ptr(covs), _s())
+    return centres, covs
+
+
+def population_factors(covariances, status, dofs=None):
+    """Lower Cholesky factors of the ready slots (column-major: element
+    (r, c) of slot k at factors[k].reshape(-1)[r + c d]) and potrf's info per
+    slot; Student-t scaling when `dofs` is given."""
+    k, d, _ = covariances.shape
+    factors = torch.zeros_like(covariances)
+    info = torch.zeros(k, dtype=torch.int32, device=covariances.device)
+    native.call("issm_population_factors", native.ptr(covariances), d, k, _dt(covariances), native.ptr(status),
+                native.ptr(dofs), native.ptr(factors), native.ptr(info), _s())
+    return factors, info
+
+
 def target_logdensity(target_struct, x, out=None):
     n = x.shape[0]
     out = torch.empty(n, dtype=x.dtype, device=x.device) if out is None else out

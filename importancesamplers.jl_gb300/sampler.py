@@ -304,6 +304,10 @@ def _prepare_moment(s):
     s.summaries, s.mean, s.cov, s.shift = _carve(torch.float64, dev, (s.rounds, 3), (d,), (d, d), (d,))
     s.round_failures, s.counter = _carve(torch.int64, dev, (s.rounds, 3), (1,))
     s.cand_loc, s.cand_factor, s.cand_lognorm = _carve(dt, dev, (d,), (d, d), (1,))
+    if isinstance(alg, NPMC):  # clipped weights of one round, the clip thresholds, the fit summaries
+        s.clipped = torch.empty(max(s.schedule), dtype=dt, device=dev)
+        s.clip_thresholds = torch.empty(s.rounds, dtype=dt, device=dev)
+        s.fit_summaries = torch.zeros(s.rounds, 3, dtype=torch.float64, device=dev)
     s.committed = (s.history.locations[0].clone(), s.history.scales[0].clone(), s.history.lognormalizers[0].clone())
     dofs = None if p.family != STUDENT_T else [float(p.dof)]
     s.rn_stride, s.ru_stride = _radial_strides(dofs)
@@ -400,10 +404,12 @@ def _moment_body(s, is_npmc):
             lq = ops.mixture_logdensity(h, den, x_new, fixed_slot=t, failures=fail, out=s.lognum[n_old:n_tot],
                                         bank_ref=view, precision=s.precision)
             ops.subtract_logweights(s.logtargets[n_old:n_tot], lq, fail, out=s.logweights[n_old:n_tot])
-            lw_fit = _npmc_clipped(s.logweights[n_old:n_tot])
+            # clip the isqrt(n) largest weights on the device (src/npmc_execution.jl:22-33)
+            lw_fit, _ = ops.npmc_clip(s.logweights[n_old:n_tot], out=s.clipped[:n_new],
+                                      threshold=s.clip_thresholds[t:t + 1])
             x_fit = x_new
             ops.logweight_summary(s.logweights[n_old:n_tot], out=s.summaries[t])
-            fit_summary = ops.logweight_summary(lw_fit)
+            fit_summary = ops.logweight_summary(lw_fit, out=s.fit_summaries[t])
         else:
             if n_old > 0:
                 with _Span(s, "amis_append", n_old * (d + 2) * es):
@@ -559,6 +565,10 @@ def _finish_moment(s, is_npmc):
                    "round_ess": ess, "round_lognormalizers": logz, "target_evaluations": total,
                    "proposal_evaluations": total if is_npmc else s.rounds * total, "failures": 0,
                    "moment_mean": moment_mean}
+    if is_npmc:  # _moment_extra_diagnostics(::NPMC) (src/npmc_execution.jl:5-6)
+        fit = s.fit_summaries.cpu().numpy()
+        diagnostics["adaptation_ess"] = np.array([0.0 if f[1] == 0 else f[1] * f[1] / f[2] for f in fit])
+        diagnostics["clipped_counts"] = [math.isqrt(int(v)) for v in s.schedule]
     return WeightedSamples(s.samples, s.logweights.clone(), provenance={"round": s.round_ids.clone()},
                            diagnostics=diagnostics)
 
@@ -626,15 +636,6 @@ def share_normal_stream(sampler, dtype=torch.float32):
 
     sampler.normals = normals
     return sampler
-
-
-def _npmc_clipped(lw):
-    """Clip the isqrt(n) largest log weights to the (n - isqrt(n) + 1)-th order
-    statistic (src/npmc_execution.jl:29-42)."""
-    n = lw.numel()
-    k = n - math.isqrt(n) + 1
-    threshold = torch.kthvalue(lw, k).values
-    return torch.minimum(lw, threshold)
 
 
 def current_proposal(sampler):

@@ -434,6 +434,72 @@ int issm_fit_factor_reg(const double *mean, const double *cov, int32_t d,
                         float *out_inverse, uint64_t *failures,
                         int64_t failure_index, issm_stream_t stream);
 
+/* ---- N-PMC weight clipping ---------------------------------------------------
+ * _moment_adaptation_workspace!(::NPMC, ...) (src/npmc_execution.jl:22-33):
+ * the isqrt(n) largest of a round's n log weights are clipped to the
+ * (n - isqrt(n) + 1)-th smallest, clipped = min(raw, threshold) (NaN when
+ * either is NaN, as Julia's min), with the order statistic of the
+ * reference's sort (NaN last) found on the device by a radix select: no host
+ * read. `threshold` is a device scalar of `dtype` that receives the order
+ * statistic. issm_select_kth is the order statistic alone: the k-th smallest
+ * (1-based) of n values into the device scalar `out`. The workspace is
+ * issm_select_workspace_bytes() bytes; calls sharing one must be ordered. */
+size_t issm_select_workspace_bytes(void);
+int issm_select_kth(const void *values, int64_t n, int64_t k, int32_t dtype,
+                    void *out, void *workspace, size_t workspace_bytes,
+                    issm_stream_t stream);
+int issm_npmc_clip(const void *raw_logweights, int64_t n, int32_t dtype,
+                   void *clipped, void *threshold, void *workspace,
+                   size_t workspace_bytes, issm_stream_t stream);
+
+/* ---- population adaptation --------------------------------------------------
+ * The per-proposal ("local") weights, covariances and factors of a
+ * population of K proposals (src/population_covariance.jl). Slot k's samples
+ * are the contiguous range starts[k] .. starts[k] + counts[k] - 1 (0-based;
+ * the reference's starts[k, round] - 1) of `samples` (d x N column-major) and
+ * of the per-sample arrays; starts/counts/thresholds are the round's columns,
+ * device arrays of K entries. status: 0 ready, 1 every local log weight is
+ * -Inf, 2 the tempering search found no feasible power. Sums and the
+ * Cholesky run in FP64; outputs are written in `dtype`. */
+
+/* _population_local_weights! (src/population_covariance.jl:115-480): per slot
+ * the normalised weights exp(l - max) / sum (into normalized_weights at the
+ * slot's samples), the local ESS, the tempering power (1 when the raw ESS
+ * reaches thresholds[k], else the largest power in (0, 1) found by bisection
+ * to `tolerance` in at most `max_iterations` steps whose tempered ESS does,
+ * with the weights re-normalised at that power) and the status. raw_means
+ * (d x K, or NULL) receives the untempered weighted mean. */
+int issm_population_local_weights(const void *local_logweights, const void *samples,
+                                  int32_t d, int32_t dtype, const int64_t *starts,
+                                  const int64_t *counts, const double *thresholds,
+                                  int32_t k, double tolerance, int32_t max_iterations,
+                                  void *normalized_weights, void *local_ess,
+                                  void *tempering_powers, uint8_t *status,
+                                  void *raw_means, issm_stream_t stream);
+/* _fit_population_covariances! (src/population_covariance.jl:482-805): for a
+ * ready slot the weighted covariance sum w (x - c)(x - c)^T about its centre
+ * c (the weighted mean when the slot was tempered, its location otherwise);
+ * a slot that is not ready keeps the current covariance of slot k of
+ * `current` (L L^T, or the squared diagonal/spherical scale, times
+ * nu / (nu - 2) for Student-t). centres (d x K) and covariances (d x d x K,
+ * symmetric) are written; d <= 64. */
+int issm_population_covariances(const void *samples, int32_t d, int32_t dtype,
+                                const void *normalized_weights,
+                                const void *tempering_powers, const uint8_t *status,
+                                const void *locations, const issm_bank *current,
+                                const int64_t *starts, const int64_t *counts,
+                                int32_t k, void *centres, void *covariances,
+                                issm_stream_t stream);
+/* _factor_population_covariances! and _scale_population_factors!
+ * (src/population_covariance.jl:807-973): the lower Cholesky factor of each
+ * ready slot's covariance (zeros above the diagonal) with potrf's info
+ * (0, the failing column, or -1 for a non-finite covariance; 0 and no write
+ * for slots that are not ready), then, when `dofs` (K entries) is given, the
+ * Student-t scaling sqrt((nu - 2) / nu) of every ready slot. d <= 64. */
+int issm_population_factors(const void *covariances, int32_t d, int32_t k,
+                            int32_t dtype, const uint8_t *status, const void *dofs,
+                            void *factors, int32_t *info, issm_stream_t stream);
+
 /* ---- built-in batch targets ------------------------------------------------
  * Native equivalents of the batch callbacks the benchmark workloads pass to
  * LogTarget(...; batch=...) (src/targets.jl:65-76, src/batched_targets.jl:54-114):

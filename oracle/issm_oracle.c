@@ -837,3 +837,225 @@ int orc_amis_run(const orc_target *target, int d, int family, double dof,
     free(dofs); free(logcounts); free(mean); free(cov);
     return status;
 }
+
+static int cmp_double_nan_last(const void *a, const void *b) {
+    const double x = *(const double *)a, y = *(const double *)b;
+    if (isnan(x)) return isnan(y) ? 0 : 1;
+    if (isnan(y)) return -1;
+    return (x > y) - (x < y);
+}
+
+/* Complete N-PMC on fed draws (src/npmc_execution.jl with the moment loop of
+ * src/adaptive_gaussian_execution.jl:897-1112): each round draws from the
+ * current proposal, weighs by the generating density alone, clips the
+ * isqrt(n) largest log weights to the (n - isqrt(n) + 1)-th smallest
+ * (:22-33, Julia's min) and fits the next proposal to the round's samples
+ * with the clipped weights. Per-round ESS / log Z of the raw weights and the
+ * ESS of the clipped ones. Returns 0 or -(round) for a failed fit. */
+int orc_npmc_run(const orc_target *target, int d, int family, double dof, const double *loc0,
+                 const double *factor0, int rounds, const int64_t *schedule, const double *normals,
+                 const double *rn, int rn_stride, const double *ru, int ru_stride, double regularization,
+                 double *samples, double *logweights, double *round_ess, double *round_logz,
+                 double *adaptation_ess, double *hist_loc, double *hist_factor, double *hist_lognorm) {
+    double logconst = family == ORC_STUDENT_T ? orc_student_t_logconstant(dof, d) : 0.0;
+    double *dofs = (double *)malloc(sizeof(double) * (size_t)rounds);
+    for (int r = 0; r < rounds; ++r) dofs[r] = dof;
+    memcpy(hist_loc, loc0, sizeof(double) * (size_t)d);
+    memcpy(hist_factor, factor0, sizeof(double) * (size_t)d * d);
+    double logabsdet = 0.0;
+    for (int c = 0; c < d; ++c) logabsdet += log(factor0[c + (size_t)c * d]);
+    hist_lognorm[0] = family == ORC_STUDENT_T ? logconst - logabsdet : orc_gaussian_lognormalizer(d, logabsdet);
+    int64_t maxn = 0;
+    for (int r = 0; r < rounds; ++r) maxn = schedule[r] > maxn ? schedule[r] : maxn;
+    double *mean = (double *)malloc(sizeof(double) * (size_t)d);
+    double *cov = (double *)malloc(sizeof(double) * (size_t)d * d);
+    double *sorted = (double *)malloc(sizeof(double) * (size_t)maxn);
+    double *clipped = (double *)malloc(sizeof(double) * (size_t)maxn);
+    double *wbuf = (double *)malloc(sizeof(double) * (size_t)maxn);
+    double *vals = (double *)malloc(sizeof(double) * (size_t)d);
+    int *exps = (int *)malloc(sizeof(int) * (size_t)d);
+    int64_t off = 0;
+    int status = 0;
+    for (int t = 0; t < rounds; ++t) {
+        orc_bank hist = {d, t + 1, family, ORC_SCALE_FACTOR, hist_loc, hist_factor, hist_lognorm, dofs, NULL};
+        const int64_t n = schedule[t];
+        double *x = samples + (size_t)off * d;
+        double *lw = logweights + off;
+        orc_draw(&hist, NULL, t, normals + (size_t)off * d, rn ? rn + (size_t)off * rn_stride : NULL, rn_stride,
+                 ru ? ru + (size_t)off * ru_stride : NULL, ru_stride, n, x, NULL);
+        for (int64_t i = 0; i < n; ++i)
+            lw[i] = orc_target_logdensity(target, x + (size_t)i * d) -
+                    orc_component_logdensity(&hist, t, x + (size_t)i * d, vals, exps);
+        double sm[3];
+        orc_logweight_summary(lw, n, sm);
+        round_ess[t] = sm[1] * sm[1] / sm[2];
+        round_logz[t] = sm[0] + log(sm[1]) - log((double)n);
+        int64_t r = (int64_t)sqrt((double)n);
+        while (r * r > n) --r;
+        while ((r + 1) * (r + 1) <= n) ++r;
+        memcpy(sorted, lw, sizeof(double) * (size_t)n);
+        qsort(sorted, (size_t)n, sizeof(double), cmp_double_nan_last);
+        const double thr = sorted[n - r];  /* the (n - r + 1)-th smallest */
+        for (int64_t i = 0; i < n; ++i)
+            clipped[i] = (isnan(lw[i]) || isnan(thr)) ? (isnan(lw[i]) ? lw[i] : thr) : (lw[i] < thr ? lw[i] : thr);
+        double cs[3];
+        orc_logweight_summary(clipped, n, cs);
+        adaptation_ess[t] = cs[1] * cs[1] / cs[2];
+        off += n;
+        if (t + 1 < rounds) {
+            orc_weighted_moments(x, d, n, clipped, mean, cov, wbuf);
+            double *L = hist_factor + (size_t)(t + 1) * d * d;
+            if (orc_fit_factor(mean, cov, d, hist_factor + (size_t)t * d * d, family == ORC_STUDENT_T ? dof : 0.0,
+                               logconst, regularization, L, hist_lognorm + t + 1) != 0) { status = -(t + 1); break; }
+            memcpy(hist_loc + (size_t)(t + 1) * d, mean, sizeof(double) * (size_t)d);
+        }
+    }
+    free(dofs); free(mean); free(cov); free(sorted); free(clipped); free(wbuf); free(vals); free(exps);
+    return status;
+}
+
+/* ---- population adaptation (src/population_covariance.jl) ------------------ */
+
+static double orc_power_ess(const double *lw, int64_t s0, int64_t cnt, double m, double p, double *total) {
+    double s = 0.0, s2 = 0.0;
+    for (int64_t i = 0; i < cnt; ++i) {
+        const double w = exp(p * (lw[s0 + i] - m));
+        s += w;
+        s2 += w * w;
+    }
+    if (total) *total = s;
+    return s * s / s2;
+}
+
+/* _population_local_weights_slot! (src/population_covariance.jl:136-233) for
+ * every slot: normalised local weights, raw ESS and weighted raw mean, then
+ * the bisection on the tempering power when the ESS is below the threshold.
+ * status: 0 ready, 1 all -Inf, 2 tempering failed. */
+void orc_population_local_weights(const double *lw, const double *x, int d, const int64_t *starts,
+                                  const int64_t *counts, const double *thresholds, int k, double tolerance,
+                                  int max_iterations, double *weights, double *local_ess, double *powers,
+                                  uint8_t *status, double *raw_means) {
+    for (int s = 0; s < k; ++s) {
+        const int64_t s0 = starts[s], cnt = counts[s];
+        double m = -INFINITY;
+        for (int64_t i = 0; i < cnt; ++i) m = lw[s0 + i] > m ? lw[s0 + i] : m;
+        if (m == -INFINITY || cnt == 0) {
+            local_ess[s] = 0.0;
+            powers[s] = 0.0;
+            status[s] = 1;
+            continue;
+        }
+        double total = 0.0, sq = 0.0;
+        for (int64_t i = 0; i < cnt; ++i) {
+            const double w = exp(lw[s0 + i] - m);
+            weights[s0 + i] = w;
+            total += w;
+            sq += w * w;
+        }
+        const double inv = 1.0 / total;
+        for (int64_t i = 0; i < cnt; ++i) weights[s0 + i] *= inv;
+        if (raw_means)
+            for (int c = 0; c < d; ++c) {
+                double a = 0.0;
+                for (int64_t i = 0; i < cnt; ++i) a += weights[s0 + i] * x[(s0 + i) * d + c];
+                raw_means[(size_t)s * d + c] = a;
+            }
+        const double ess = total * total / sq;
+        local_ess[s] = ess;
+        powers[s] = 1.0;
+        status[s] = 0;
+        if (ess >= thresholds[s]) continue;
+        double lo = 0.0, hi = 1.0, lo_ess = 0.0;
+        for (int it = 0; it < max_iterations; ++it) {
+            const double p = 0.5 * (lo + hi);
+            const double e = orc_power_ess(lw, s0, cnt, m, p, NULL);
+            if (e >= thresholds[s]) { lo = p; lo_ess = e; } else { hi = p; }
+            if (hi - lo <= tolerance) break;
+        }
+        if (lo == 0.0) {
+            powers[s] = 0.0;
+            status[s] = 2;
+            continue;
+        }
+        double t;
+        orc_power_ess(lw, s0, cnt, m, lo, &t);
+        for (int64_t i = 0; i < cnt; ++i) weights[s0 + i] = exp(lo * (lw[s0 + i] - m)) / t;
+        local_ess[s] = lo_ess;
+        powers[s] = lo;
+    }
+}
+
+/* _fit_population_covariance_slot! (src/population_covariance.jl:482-545):
+ * ready slots: centre (weighted mean when tempered, else the location) and
+ * the weighted covariance about it; other slots: the current covariance
+ * L L^T * multiplier from `factors` (d x d x K column-major) and `dofs`
+ * (NULL for Gaussian). */
+void orc_population_covariances(const double *x, int d, const double *weights, const double *powers,
+                                const uint8_t *status, const double *locations, const double *factors,
+                                const double *dofs, const int64_t *starts, const int64_t *counts, int k,
+                                double *centres, double *covs) {
+    for (int s = 0; s < k; ++s) {
+        const int64_t s0 = starts[s], cnt = counts[s];
+        double *cs = centres + (size_t)s * d;
+        double *ck = covs + (size_t)s * d * d;
+        const int tempered = status[s] == 0 && powers[s] < 1.0;
+        for (int c = 0; c < d; ++c) {
+            double a = locations[(size_t)s * d + c];
+            if (tempered) {
+                a = 0.0;
+                for (int64_t i = 0; i < cnt; ++i) a += weights[s0 + i] * x[(s0 + i) * d + c];
+            }
+            cs[c] = a;
+        }
+        for (int c = 0; c < d; ++c)
+            for (int r = c; r < d; ++r) {
+                double v = 0.0;
+                if (status[s] != 0) {
+                    const double *L = factors + (size_t)s * d * d;
+                    for (int j = 0; j <= c; ++j) v += L[r + (size_t)j * d] * L[c + (size_t)j * d];
+                    if (dofs) v *= dofs[s] / (dofs[s] - 2.0);
+                } else {
+                    for (int64_t i = 0; i < cnt; ++i)
+                        v += weights[s0 + i] * (x[(s0 + i) * d + r] - cs[r]) * (x[(s0 + i) * d + c] - cs[c]);
+                }
+                ck[r + (size_t)c * d] = v;
+                ck[c + (size_t)r * d] = v;
+            }
+    }
+}
+
+/* _factor_population_slot! and _scale_population_factors!
+ * (src/population_covariance.jl:807-828,959-973): potrf of each ready slot
+ * (info -1 for a non-finite covariance, else the failing column), zeros above
+ * the diagonal, then the Student-t scaling sqrt((nu-2)/nu) when dofs != NULL. */
+void orc_population_factors(const double *covs, int d, int k, const uint8_t *status, const double *dofs,
+                            double *factors, int32_t *info) {
+    for (int s = 0; s < k; ++s) {
+        info[s] = 0;
+        if (status[s] != 0) continue;
+        const double *ck = covs + (size_t)s * d * d;
+        double *f = factors + (size_t)s * d * d;
+        int bad = 0;
+        for (int e = 0; e < d * d; ++e) {
+            const int r = e % d, c = e / d;
+            if (!isfinite(ck[e])) bad = 1;
+            f[e] = r >= c ? ck[e] : 0.0;
+        }
+        if (bad) info[s] = -1;
+        for (int j = 0; j < d && !bad; ++j) {
+            double piv = f[j + (size_t)j * d];
+            for (int q = 0; q < j; ++q) piv -= f[j + (size_t)q * d] * f[j + (size_t)q * d];
+            if (!(isfinite(piv) && piv > 0.0)) { info[s] = j + 1; break; }
+            f[j + (size_t)j * d] = sqrt(piv);
+            for (int r = j + 1; r < d; ++r) {
+                double v = f[r + (size_t)j * d];
+                for (int q = 0; q < j; ++q) v -= f[r + (size_t)q * d] * f[j + (size_t)q * d];
+                f[r + (size_t)j * d] = v / f[j + (size_t)j * d];
+            }
+        }
+        if (dofs) {
+            const double sc = sqrt((dofs[s] - 2.0) / dofs[s]);
+            for (int e = 0; e < d * d; ++e) f[e] *= sc;
+        }
+    }
+}

@@ -105,6 +105,21 @@ int orc_fit_factor(const double *mean, const double *cov, int d,
                    const double *prev_factor, double dof, double logconstant,
                    double regularization, double *out_factor,
                    double *out_lognorm);
+int orc_npmc_run(const orc_target *target, int d, int family, double dof, const double *loc0,
+                 const double *factor0, int rounds, const int64_t *schedule, const double *normals,
+                 const double *rn, int rn_stride, const double *ru, int ru_stride, double regularization,
+                 double *samples, double *logweights, double *round_ess, double *round_logz,
+                 double *adaptation_ess, double *hist_loc, double *hist_factor, double *hist_lognorm);
+void orc_population_local_weights(const double *lw, const double *x, int d, const int64_t *starts,
+                                  const int64_t *counts, const double *thresholds, int k, double tolerance,
+                                  int max_iterations, double *weights, double *local_ess, double *powers,
+                                  uint8_t *status, double *raw_means);
+void orc_population_covariances(const double *x, int d, const double *weights, const double *powers,
+                                const uint8_t *status, const double *locations, const double *factors,
+                                const double *dofs, const int64_t *starts, const int64_t *counts, int k,
+                                double *centres, double *covs);
+void orc_population_factors(const double *covs, int d, int k, const uint8_t *status, const double *dofs,
+                            double *factors, int32_t *info);
 void orc_philox_normals(uint64_t seed, uint64_t offset, int64_t n, double *out);
 void orc_philox_uniforms(uint64_t seed, uint64_t offset, int64_t n, double *out);
 int orc_amis_run(const orc_target *target, int d, int family, double dof,

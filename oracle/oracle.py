@@ -94,6 +94,12 @@ def _declare(L):
                                p, p, p, p, p, p, p, p, p, p]
     L.orc_set_threads.argtypes = [i32]
     L.orc_num_threads.restype = i32
+    L.orc_npmc_run.restype = i32
+    L.orc_npmc_run.argtypes = [C.POINTER(Target), i32, i32, d, p, p, i32, p, p, p, i32, p, i32, d,
+                               p, p, p, p, p, p, p, p]
+    L.orc_population_local_weights.argtypes = [p, p, i32, p, p, p, i32, d, i32, p, p, p, p, p]
+    L.orc_population_covariances.argtypes = [p, i32, p, p, p, p, p, p, p, p, i32, p, p]
+    L.orc_population_factors.argtypes = [p, i32, i32, p, p, p, p]
 
 
 def _f64(a):
@@ -293,6 +299,78 @@ def fit_factor(mean, cov, prev_factor, dof=0.0, logconstant=0.0, regularization=
     st = lib().orc_fit_factor(mean.ctypes.data, cov.ctypes.data, d, prev.ctypes.data, float(dof),
                               float(logconstant), float(reg), L.ctypes.data, C.addressof(ln))
     return st, L.reshape(d, d, order="F"), ln.value
+
+
+def npmc_run(target, d, loc0, factor0, schedule, normals, family=GAUSSIAN, dof=0.0, regularization=None):
+    """Complete N-PMC on fed draws. Returns a dict of FP64 arrays."""
+    schedule = np.ascontiguousarray(schedule, dtype=np.int64)
+    rounds = schedule.size
+    total = int(schedule.sum())
+    loc0 = _f64(loc0)
+    f0 = np.asfortranarray(_f64(factor0)).reshape(-1, order="F").copy()
+    nz = _f64(normals)
+    reg = np.sqrt(np.finfo(np.float64).eps) if regularization is None else regularization
+    out = dict(samples=np.empty(total * d), logweights=np.empty(total), round_ess=np.empty(rounds),
+               round_logz=np.empty(rounds), adaptation_ess=np.empty(rounds), hist_loc=np.zeros(rounds * d),
+               hist_factor=np.zeros(rounds * d * d), hist_lognorm=np.zeros(rounds))
+    st = lib().orc_npmc_run(C.byref(target.struct), int(d), int(family), float(dof), loc0.ctypes.data,
+                            f0.ctypes.data, rounds, schedule.ctypes.data, nz.ctypes.data, None, 0, None, 0,
+                            float(reg), out["samples"].ctypes.data, out["logweights"].ctypes.data,
+                            out["round_ess"].ctypes.data, out["round_logz"].ctypes.data,
+                            out["adaptation_ess"].ctypes.data, out["hist_loc"].ctypes.data,
+                            out["hist_factor"].ctypes.data, out["hist_lognorm"].ctypes.data)
+    out["status"] = st
+    return out
+
+
+def population_local_weights(lw, x, d, starts, counts, thresholds, tolerance=1e-6, max_iterations=60):
+    """Returns (weights, local_ess, powers, status, raw_means (K, d))."""
+    lw = _f64(lw)
+    x = _f64(x)
+    starts = np.ascontiguousarray(starts, dtype=np.int64)
+    counts = np.ascontiguousarray(counts, dtype=np.int64)
+    thr = _f64(thresholds)
+    k = starts.size
+    w = np.zeros(lw.size)
+    ess, pw = np.zeros(k), np.zeros(k)
+    st = np.zeros(k, dtype=np.uint8)
+    means = np.zeros(k * d)
+    lib().orc_population_local_weights(lw.ctypes.data, x.ctypes.data, int(d), starts.ctypes.data, counts.ctypes.data,
+                                       thr.ctypes.data, k, float(tolerance), int(max_iterations), w.ctypes.data,
+                                       ess.ctypes.data, pw.ctypes.data, st.ctypes.data, means.ctypes.data)
+    return w, ess, pw, st, means.reshape(k, d)
+
+
+def population_covariances(x, d, weights, powers, status, locations, factors, dofs, starts, counts):
+    """factors: (K, d, d) with factors[k] the column-major storage (row-major
+    L^T); returns (centres (K, d), covariances (K, d, d))."""
+    x, w, pw, loc = _f64(x), _f64(weights), _f64(powers), _f64(locations)
+    fac = _f64(factors)
+    st = np.ascontiguousarray(status, dtype=np.uint8)
+    starts = np.ascontiguousarray(starts, dtype=np.int64)
+    counts = np.ascontiguousarray(counts, dtype=np.int64)
+    nu = None if dofs is None else _f64(dofs)
+    k = starts.size
+    cen = np.zeros(k * d)
+    cov = np.zeros(k * d * d)
+    lib().orc_population_covariances(x.ctypes.data, int(d), w.ctypes.data, pw.ctypes.data, st.ctypes.data,
+                                     loc.ctypes.data, fac.ctypes.data, _ptr(nu), starts.ctypes.data,
+                                     counts.ctypes.data, k, cen.ctypes.data, cov.ctypes.data)
+    return cen.reshape(k, d), cov.reshape(k, d, d)
+
+
+def population_factors(covs, d, status, dofs=None):
+    """covs: (K, d, d) (symmetric); returns (factors (K, d, d) in the same
+    column-major storage, info (K,))."""
+    c = _f64(covs)
+    k = c.shape[0]
+    st = np.ascontiguousarray(status, dtype=np.uint8)
+    nu = None if dofs is None else _f64(dofs)
+    f = np.zeros(k * d * d)
+    info = np.zeros(k, dtype=np.int32)
+    lib().orc_population_factors(c.ctypes.data, int(d), k, st.ctypes.data, _ptr(nu), f.ctypes.data,
+                                 info.ctypes.data)
+    return f.reshape(k, d, d), info
 
 
 def philox_normals(seed, offset, n):
