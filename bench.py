@@ -489,6 +489,120 @@ def run_gb300(args):
     print(json.dumps(line), flush=True)
 
 
+def run_static_mis(args):
+    """Static MIS microbench (seeded synthetic inputs): N = 4,194,304 samples,
+    d = 16, a bank of K = 64 full-covariance Gaussians (mu ~ N(0, 4 I),
+    Sigma = A A^T / d + 0.1 I with A ~ N(0, 1), L = chol(Sigma) in FP64,
+    masses ~ Dirichlet(1)), a standard-normal target. One step: stratified
+    assignment and draw, the balance-heuristic log q of every sample over all
+    64 components (the tcgen05 mixture kernel, BF16 x3), the target, the log
+    weights, their summary and normalisation, and systematic resampling of
+    all N with one uniform plus the gather of the resampled samples. The
+    mixture kernel's roofline uses its algorithmic flops N K d (d + 1)
+    against the measured burst bf16 rate."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    issm = ge.load_package()
+    issm.native.require()
+    dev = torch.device("cuda", 0)
+    n, d, k = 4_194_304, 16, 64
+    rng = np.random.default_rng(2)
+    props = []
+    for _ in range(k):
+        A = rng.normal(size=(d, d))
+        L = np.linalg.cholesky(A @ A.T / d + 0.1 * np.eye(d))
+        props.append(issm.FactorGaussian((2.0 * rng.normal(size=d)).astype(np.float32), L.astype(np.float32)))
+    bank = issm.ProposalBank(props, rng.dirichlet(np.ones(k)).astype(np.float32))
+    db = issm.pack(bank, dev)
+    prec = {"fp32": issm.native.PREC_NATIVE, "tf32": issm.native.PREC_TF32, "bf16": issm.native.PREC_BF16}[args.precision]
+    den = issm.ops.denominator(issm.native.DENOM_FULL, db.logmasses)
+    target = issm.StandardNormalTarget(d).bind(dev, torch.float32)
+    f32 = dict(dtype=torch.float32, device=dev)
+    u = torch.empty(n, **f32)
+    slots = torch.empty(n, dtype=torch.int32, device=dev)
+    normals = torch.empty(n * d, **f32)
+    x = torch.empty(n, d, **f32)
+    lq, lt, lw, w = (torch.empty(n, **f32) for _ in range(4))
+    anc = torch.empty(n, dtype=torch.int64, device=dev)
+    xr = torch.empty(n, d, **f32)
+    sm = torch.zeros(3, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+    mix_ms = []
+
+    def step(i, timed):
+        issm.ops.fill_uniforms(n, torch.float32, dev, 77, 2 * i * n * (d + 1), out=u)
+        issm.ops.static_assign(db.cdf, u, True, out=slots)
+        issm.ops.fill_normals(n * d, torch.float32, dev, 78, 2 * i * n * (d + 1), out=normals)
+        issm.ops.draw(db, normals, n, slots=slots, out=x)
+        if timed:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        issm.ops.mixture_logdensity(db, den, x, precision=prec, out=lq)
+        if timed:
+            e1.record(stream)
+            mix_ms.append((e0, e1))
+        target.evaluate(x, out=lt, precision=prec)
+        issm.ops.subtract_logweights(lt, lq, out=lw)
+        issm.ops.logweight_summary(lw, out=sm)
+        issm.ops.normalize(lw, sm, out=w)
+        issm.ops.resample_systematic(lw, 0.5 / (i + 2), n, out=anc)
+        issm.ops.gather(x, anc, out=xr)
+
+    for i in range(max(args.warmup, 3)):
+        step(i, False)
+    torch.cuda.synchronize()
+    l0 = issm.native.launches()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clocks:
+        t0.record(stream)
+        for i in range(args.steps):
+            step(100 + i, True)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    launches = int((issm.native.launches() - l0) // args.steps)
+    ms = t0.elapsed_time(t1) / args.steps
+    mix = float(np.mean([a.elapsed_time(b) for a, b in mix_ms]))
+    hbm, tflops, src = read_peaks()
+    alg = n * k * d * (d + 1)
+    achieved = alg / (mix / 1e3) / 1e12
+    peak = tflops if args.precision == "bf16" else tflops / 2
+    # parity of the mixture on a slice, against the FP64 oracle
+    from oracle import oracle as orc
+
+    sl = 4096
+    ob = orc.BankView(d, orc.GAUSSIAN, orc.SCALE_FACTOR, db.locations.double().cpu().numpy(),
+                      db.scales.double().cpu().numpy(), db.lognormalizers.double().cpu().numpy())
+    xs = x[:sl].double().cpu().numpy()
+    exp, _, _ = orc.mixture_logdensity(ob, xs.reshape(-1), orc.DENOM_FULL, db.logmasses.double().cpu().numpy())
+    err = float(np.max(np.abs(lq[:sl].double().cpu().numpy() - exp) / np.maximum(1.0, np.abs(exp))))
+    # CPU baseline: the oracle's mixture (all host cores) on a 1/16 slice
+    cpu_n = n // 16
+    xc = x[:cpu_n].double().cpu().numpy().reshape(-1)
+    c0 = time.perf_counter()
+    orc.mixture_logdensity(ob, xc, orc.DENOM_FULL, db.logmasses.double().cpu().numpy())
+    cpu_s = time.perf_counter() - c0
+    line = {"metric": "static MIS weighted samples/s", "value": n / (ms / 1e3), "unit": "weighted samples/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"fp32": "f32", "tf32": "tf32", "bf16": "bf16"}[args.precision], "data": "synthetic (seeded)",
+            "config": {"workload": "static MIS, N=4,194,304, d=16, K=64 full-covariance Gaussians, stratified "
+                                   "assignment, balance-heuristic denominator, normalise, systematic resampling",
+                       "l2": "inputs larger than L2 (268 MB of samples)"},
+            "mixture_kernel": {"ms": mix, "pairs_per_s": n * k / (mix / 1e3),
+                               "max_rel_err_vs_fp64_oracle": err},
+            "roofline": {"bound": "tensor", "kernel": "mixture_tc_kernel (K=64, BF16 x3)" if args.precision == "bf16"
+                         else "mixture kernel", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak, "peak_source": f"{src} bf16_tflops (burst)",
+                         "algorithmic_flops_per_launch": alg, "traffic": None},
+            "cpu_baseline": {"value": cpu_n / cpu_s, "unit": "weighted samples/s (mixture density only)",
+                             "cores": orc.num_threads(), "kind": "port",
+                             "sample": f"FP64 oracle mixture density of {cpu_n} samples over the 64 components"},
+            "gpu_launches": launches, "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_serve(args):
     """Serving mix (C5 shapes): independent Bayesian linear-regression
     posteriors, d ~ U{2..64}, n_obs log-uniform in [50, 5000], sample budget
@@ -571,14 +685,18 @@ def main():
     ap.add_argument("--rounds", type=int, default=ROUNDS)
     ap.add_argument("--round-size", type=int, default=ROUND_SIZE)
     ap.add_argument("--quick", action="store_true", help="skip the e2e and CPU-baseline legs (profiling runs)")
-    ap.add_argument("--workload", default="amis", choices=["amis", "serve"],
-                    help="amis: the headline AMIS d=64 run; serve: the serving-mix latency sweep")
+    ap.add_argument("--workload", default="amis", choices=["amis", "serve", "static-mis"],
+                    help="amis: the headline AMIS d=64 run; serve: the serving-mix latency sweep; "
+                         "static-mis: the N=4,194,304, d=16, K=64 static MIS microbench")
     ap.add_argument("--requests", type=int, default=200, help="serve: requests per arrival rate")
     ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0], help="serve: arrivals per second")
     ap.add_argument("--inflight", type=int, default=8, help="serve: concurrent runs (streams)")
     args = ap.parse_args()
     if args.workload == "serve":
         run_serve(args)
+        return
+    if args.workload == "static-mis":
+        run_static_mis(args)
         return
     if args.impl == "reference":
         run_reference(args)

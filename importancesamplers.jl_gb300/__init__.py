@@ -14,8 +14,8 @@ from .methods import (AMIS, NPMC, DeterministicMixturePMC, GlobalResampling, Imp
 from .proposals import (DiagonalGaussian, DiagonalStudentT, FactorGaussian, FactorStudentT, SphericalGaussian,
                         SphericalStudentT, student_t_logconstant)
 from .results import (AllZeroWeightsError, AMISRoundError, DMPMCRoundError, NPMCRoundError, SamplerExecutionError,
-                      UnweightedSamples, WeightedSamples, cov, effective_sample_size, lognormalizer, mean,
-                      normalized_weights, resample, var)
+                      UnweightedSamples, WeightedSamples, cov, effective_sample_size, lognormalizer, mean, median,
+                      normalized_weights, quantile, resample, std, var)
 from .sampler import (SamplerBusyError, current_proposal, deterministic_allocation_plan, importance_sample,
                       importance_sample_, prepare_sampler, reweigh_amis, share_normal_stream)
 from .targets import (GaussianMixtureTarget, LinearRegressionTarget, LogisticRegressionTarget, LogTarget,

@@ -488,6 +488,74 @@ int issm_fit_factor(const double *mean, const double *cov, int32_t d, const void
                               out_lognormalizer, nullptr, failures, failure_index, stream);
 }
 
+size_t issm_weighted_sum_workspace_bytes(int64_t n, int32_t d) {
+    if (n < 1 || d < 1) return 0;
+    return weighted_sum_workspace_bytes(n, d);
+}
+
+int issm_weighted_sum(const void *x, int32_t d, int64_t n, const void *logweights, int32_t dtype,
+                      const double *summary, double *out, void *workspace, size_t workspace_bytes,
+                      issm_stream_t stream) {
+    if (n < 1 || d < 1) return ISSM_E_SIZE;
+    if (!x || !logweights || !summary || !out || !workspace) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    if (workspace_bytes < weighted_sum_workspace_bytes(n, d)) return ISSM_E_WORKSPACE;
+    return weighted_sum(x, d, n, logweights, dtype, summary, out, workspace, (cudaStream_t)stream);
+}
+
+size_t issm_weighted_quantile_workspace_bytes(int32_t d, int32_t nprob) {
+    if (d < 1 || nprob < 1) return 0;
+    return weighted_quantile_workspace_bytes(d, nprob);
+}
+
+int issm_weighted_quantile(const void *x, int32_t d, int64_t n, const void *logweights, int32_t dtype,
+                           const double *summary, const double *probabilities, int32_t nprob, double *out,
+                           void *workspace, size_t workspace_bytes, issm_stream_t stream) {
+    if (n < 1 || d < 1 || nprob < 1) return ISSM_E_SIZE;
+    if (!x || !logweights || !summary || !probabilities || !out || !workspace) return ISSM_E_NULL;
+    ISSM_TRY(check_dtype(dtype));
+    if (workspace_bytes < weighted_quantile_workspace_bytes(d, nprob)) return ISSM_E_WORKSPACE;
+    if (((uintptr_t)workspace & 15) != 0) return ISSM_E_UNSUPPORTED;
+    return weighted_quantile(x, d, n, logweights, dtype, summary, probabilities, nprob, out, workspace,
+                             (cudaStream_t)stream);
+}
+
+static int glm_check(const issm_target *t, int32_t precision) {
+    if (!t) return ISSM_E_NULL;
+    if (t->kind != ISSM_TARGET_LINREG && t->kind != ISSM_TARGET_LOGISTIC) return ISSM_E_KIND;
+    if (t->dtype != ISSM_F32) return ISSM_E_DTYPE;
+    if (t->dim < 1 || t->count < 1) return ISSM_E_SIZE;
+    if (t->dim > 64) return ISSM_E_UNSUPPORTED;
+    if (precision != ISSM_PREC_BF16 && precision != ISSM_PREC_TF32 && precision != ISSM_PREC_BF16X1)
+        return ISSM_E_KIND;
+    if (!t->a || !t->b) return ISSM_E_NULL;
+    return ISSM_OK;
+}
+
+size_t issm_glm_operand_bytes(int32_t nobs, int32_t d, int32_t precision) {
+    if (nobs < 1 || d < 1 || d > 64) return 0;
+    return glm_operand_bytes(nobs, d, precision);
+}
+
+int issm_glm_prepare(const issm_target *target, int32_t precision, void *operand, size_t operand_bytes,
+                     issm_stream_t stream) {
+    ISSM_TRY(glm_check(target, precision));
+    if (!operand) return ISSM_E_NULL;
+    if (operand_bytes < glm_operand_bytes(target->count, target->dim, precision)) return ISSM_E_WORKSPACE;
+    if (((uintptr_t)operand & 15) != 0) return ISSM_E_UNSUPPORTED;
+    return glm_prepare(target, precision, operand, (cudaStream_t)stream);
+}
+
+int issm_glm_logdensity(const issm_target *target, int32_t precision, const void *operand, const float *x,
+                        int64_t n, float *out, int32_t *error, issm_stream_t stream) {
+    ISSM_TRY(glm_check(target, precision));
+    if (n < 0) return ISSM_E_SIZE;
+    if (n == 0) return ISSM_OK;
+    if (!operand || !x || !out || !error) return ISSM_E_NULL;
+    if (((uintptr_t)operand & 15) != 0) return ISSM_E_UNSUPPORTED;
+    return glm_logdensity(target, precision, operand, x, n, out, error, (cudaStream_t)stream);
+}
+
 size_t issm_select_workspace_bytes(void) { return select_workspace_bytes(); }
 
 int issm_select_kth(const void *values, int64_t n, int64_t k, int32_t dtype, void *out, void *workspace,

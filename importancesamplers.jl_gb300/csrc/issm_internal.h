@@ -2,6 +2,7 @@
 // and the kernel translation units.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (types only; driver calls are resolved through the runtime)
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -68,6 +69,24 @@ int population_covariances(const void *x, int d, int dtype, const void *weights,
                            cudaStream_t stream);
 int population_factors(const void *covs, int d, int k, int dtype, const uint8_t *status, const void *dofs,
                        void *factors, int32_t *info, cudaStream_t stream);
+
+// tensor maps of n x d FP32 sample arrays, 32-float x 128-row boxes (tma.cu)
+bool row_tiles_supported(const void *x, int d, int64_t n);
+int encode_row_tiles(CUtensorMap *map, const void *x, int d, int64_t n);
+
+// result statistics (stats.cu)
+size_t weighted_sum_workspace_bytes(int64_t n, int d);
+int weighted_sum(const void *x, int d, int64_t n, const void *lw, int dtype, const double *summary, double *out,
+                 void *ws, cudaStream_t stream);
+size_t weighted_quantile_workspace_bytes(int d, int nprob);
+int weighted_quantile(const void *x, int d, int64_t n, const void *lw, int dtype, const double *summary,
+                      const double *probs, int nprob, double *out, void *ws, cudaStream_t stream);
+
+// regression likelihood on tensor cores (glm_tc.cu)
+size_t glm_operand_bytes(int nobs, int d, int precision);
+int glm_prepare(const issm_target *t, int precision, void *ops, cudaStream_t stream);
+int glm_logdensity(const issm_target *t, int precision, const void *ops, const float *x, int64_t n, float *out,
+                   int *error, cudaStream_t stream);
 
 // order statistic and N-PMC clipping (select.cu)
 size_t select_workspace_bytes();

@@ -32,6 +32,8 @@
 //       log-sum-exp states through shared memory when the tile completes.
 // Every wait is bounded; a timeout sets the sticky error word and the CTA
 // unwinds after draining its outstanding copies and MMAs.
+#include <cstring>
+
 #include "issm_device.cuh"
 #include "issm_internal.h"
 #include "tcgen05.cuh"
@@ -131,6 +133,7 @@ struct TcParams {
     uint64_t *failures;
     int64_t index_base;
     int *error;
+    int tma;  // staged tiles arrive by tensor copies (swizzled 32-float boxes) of `x`
 };
 
 // Warp roles of mixture_tc_kernel.
@@ -144,7 +147,7 @@ constexpr int kBRing = 3;      // operand buffers in flight when a tile needs se
 constexpr int kMaxRawStages = 4;
 
 template <int KIND, int SPLIT, int DP, bool DIRECT>
-__global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
+__global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, const __grid_constant__ CUtensorMap tmap) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
     constexpr int PER = 16 / EB;              // elements per 16-byte K group
     constexpr int KG = DP / PER;              // K groups of the sample coordinates
@@ -166,7 +169,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     const uint32_t LBO_B = (uint32_t)(chunk * DP * 16);
     const uint32_t CHUNK_BYTES = (uint32_t)(NPART * chunk * B_COMP);
 
-    extern __shared__ __align__(1024) unsigned char smem[];
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // stages start on 1024-byte boundaries (the swizzled boxes need them)
+    unsigned char *smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
     unsigned char *s_raw = smem;
     unsigned char *s_a = s_raw + (size_t)S * RAW_BYTES;
     unsigned char *s_b = s_a + (size_t)nbufA * NPART * A_PART;
@@ -178,7 +183,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     // staged tiles with rows of 16-byte multiples at 16-byte aligned
     // addresses arrive by one bulk copy per row from the stager warp
     const bool vec = (p.d % 4 == 0) && ((reinterpret_cast<uintptr_t>(p.x) & 15) == 0);
-    const bool bulk = !DIRECT && S > 0 && vec;
+    const bool bulk = !DIRECT && S > 0 && p.tma != 0;
+    const int nbox = p.d > 32 ? 2 : 1;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int NW = chunk * DP;  // TMEM columns of one accumulator
@@ -385,14 +391,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
                             v[m + 2] = (active && c + 2 < p.d) ? f.z - cc.z : 0.f;
                             v[m + 3] = (active && c + 3 < p.d) ? f.w - cc.w : 0.f;
                         } else if (full) {
-                            const float4 f = *reinterpret_cast<const float4 *>(raw + row * RS + c);
+                            const float4 f = *reinterpret_cast<const float4 *>(
+                                bulk ? tc::swizzled_row_chunk(reinterpret_cast<const unsigned char *>(raw), row, c)
+                                     : raw + row * RS + c);
                             v[m] = f.x - cc.x;
                             v[m + 1] = f.y - cc.y;
                             v[m + 2] = f.z - cc.z;
                             v[m + 3] = f.w - cc.w;
                         } else {
                             float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-                            if (active) f = *reinterpret_cast<const float4 *>(raw + row * RS + c);
+                            if (active)
+                                f = *reinterpret_cast<const float4 *>(
+                                    bulk ? tc::swizzled_row_chunk(reinterpret_cast<const unsigned char *>(raw), row, c)
+                                         : raw + row * RS + c);
                             v[m] = (active && c < p.d) ? f.x - cc.x : 0.f;
                             v[m + 1] = (active && c + 1 < p.d) ? f.y - cc.y : 0.f;
                             v[m + 2] = (active && c + 2 < p.d) ? f.z - cc.z : 0.f;
@@ -417,10 +428,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
         }
         tc::cp_async_wait_all();
     } else if (warp == kStagerWarp) {
-        // ================= stager: one bulk copy per sample row into the padded ring =================
+        // ================= stager: a tile's swizzled boxes by tensor copies =================
         if (bulk) {
             int issued = 0;
-            const uint32_t rb = (uint32_t)p.d * 4u;
             for (int it = 0; it < my_tiles; ++it) {
                 const int s = it % S;
                 if (it >= S) {
@@ -429,12 +439,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
                     if (!__shfl_sync(0xffffffffu, fine, 0)) break;
                 }
                 const int64_t row0 = tile_of(it) * kTcTile;
-                const int rows = (int)min((int64_t)kTcTile, p.n - row0);
-                float *dst = reinterpret_cast<float *>(s_raw + (size_t)s * RAW_BYTES);
-                if (lane == 0) tc::mbar_arrive_expect_tx(&raw_full[s], (uint32_t)rows * rb);
+                unsigned char *dst = s_raw + (size_t)s * RAW_BYTES;
+                if (lane == 0) {
+                    // a box counts all its bytes (rows past n arrive as zeros)
+                    tc::mbar_arrive_expect_tx(&raw_full[s], (uint32_t)nbox * 16384u);
+                    for (int b = 0; b < nbox; ++b)
+                        tc::tma_load_2d(dst + (size_t)b * 16384, &tmap, 32 * b, (int)row0, &raw_full[s]);
+                }
                 __syncwarp();
-                for (int r = lane; r < rows; r += 32)
-                    tc::bulk_copy_g2s(dst + r * RS, p.x + (row0 + r) * p.d, rb, &raw_full[s]);
                 issued = it + 1;
             }
             // every copy lands before the CTA can exit (the converters consume
@@ -598,13 +610,13 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
         nch = (nslots + chunk - 1) / chunk;
         if (nch == 1) {
             stages = 3;
-            smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)NPART * chunk * B_COMP + (size_t)DP * 4;
+            smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)NPART * chunk * B_COMP + (size_t)DP * 4 + 1024;
         } else {
             // a staged tile if it fits beside a kBRing-deep operand ring; else
             // the converters read their rows from global memory (no staged
             // tile), with a kBRing- or 2-deep ring, which leaves room for
             // larger chunks (fewer, wider MMA items per tile)
-            const size_t base = NPART * A_PART + (size_t)DP * 4, cb = (size_t)NPART * chunk * B_COMP;
+            const size_t base = NPART * A_PART + (size_t)DP * 4 + 1024, cb = (size_t)NPART * chunk * B_COMP;
             bring = kBRing;
             stages = RAW_BYTES + base + kBRing * cb <= kTcMaxSmem ? 1 : 0;
             if (stages == 0 && base + kBRing * cb > kTcMaxSmem) bring = 2;
@@ -634,7 +646,13 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     p.ntiles = (int)((p.n + kTcTile - 1) / kTcTile);
     const int blocks = min(p.ntiles, device_sms() * occ);
     if (blocks < 1) return 0;
-    { kern<<<blocks, kTcThreads, smem, stream>>>(p); note_launch(); }
+    // staged tiles by tensor copies when the rows are whole 32-float boxes
+    CUtensorMap tmap;
+    memset(&tmap, 0, sizeof(tmap));
+    p.tma = 0;
+    if (stages > 0 && DP == p.d && row_tiles_supported(p.x, p.d, p.n))
+        p.tma = encode_row_tiles(&tmap, p.x, p.d, p.n) == ISSM_OK ? 1 : 0;
+    { kern<<<blocks, kTcThreads, smem, stream>>>(p, tmap); note_launch(); }
     return (int)cudaGetLastError();
 }
 

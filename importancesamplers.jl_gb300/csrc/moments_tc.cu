@@ -25,14 +25,19 @@
 // A is stored MN-major: each sample's 8-coordinate groups are 16-byte chunks,
 // so two threads convert a sample row straight from the staged tile. Warp
 // roles: warp 0 issues the MMAs; warps 1..8 build A (double-buffered) from
-// the staged tiles; warp 9 stages the tiles. When rows are 16-byte multiples
-// (d % 4 == 0, aligned arrays) the stager keeps a four-deep ring of padded
-// stages filled with one bulk copy per sample row (cp.async.bulk, completion
-// counted in bytes on the stage's mbarrier); converters wait on that
-// mbarrier and release the stage with one arrival per warp, so no role ever
-// waits on a CTA-wide barrier. Other shapes stage with 4-byte cp.async from
-// the converters. Per-CTA partials are summed across CTAs (compensated FP32)
-// and mean = c + S1/S0, cov = S2/S0 - (S1/S0)(S1/S0)^T in FP64.
+// the staged tiles; warp 9 stages the tiles. For d = 32 or 64 (aligned
+// arrays) the stager keeps a four-deep ring of stages filled by tensor copies
+// (cp.async.bulk.tensor through a tensor map of the samples: one or two
+// 32-float x 128-row boxes per tile, 128-byte swizzle, so converters read
+// rows without bank conflicts, plus one bulk copy of the tile's log weights;
+// completion counted in bytes on the stage's mbarrier); converters wait on
+// that mbarrier and release the stage with one arrival per warp, so no role
+// ever waits on a CTA-wide barrier. Other shapes stage padded rows with
+// 4-byte cp.async from the converters. Per-CTA partials are summed across
+// CTAs (compensated FP32) and mean = c + S1/S0, cov = S2/S0 - (S1/S0)(S1/S0)^T
+// in FP64.
+#include <cstring>
+
 #include "issm_device.cuh"
 #include "issm_internal.h"
 #include "tcgen05.cuh"
@@ -50,16 +55,21 @@ constexpr int kMtCtasPerSm = 1;  // CTAs per SM (two 64-sample pipelines measure
 constexpr int kMtCols = 80;    // MMA N (64 coordinates + sqrt(w) + padding)
 constexpr int kMtStages = 4;   // staged sample tiles in flight
 constexpr int kMtRS = 68;      // padded row of a staged tile (floats): conflict-free row reads
-constexpr int kMtRawBytes = kMtTile * kMtRS * 4 + kMtTile * 4;  // rows, then the tile's log weights
+constexpr int kMtWOff = kMtTile * kMtRS * 4;  // byte offset of the tile's log weights in a stage
+// rows (padded, or two swizzled boxes), then the log weights; a 1024-byte multiple
+constexpr int kMtRawBytes = (kMtWOff + kMtTile * 4 + 1023) / 1024 * 1024;
 // Rows 0..71 (9 row groups: 64 coordinates, sqrt(w), zeros) are stored; the
 // MMA's M = 128 also reads row groups 9..15, which land in the next buffer or
 // the staged tiles after A: those D rows and the matching columns >= 72 are
 // never read, so their content does not matter.
 constexpr int kMtGroups = 9;
 constexpr int kMtPart = kMtGroups * kMtTile * 16;
-constexpr size_t kMtSmem = (size_t)2 * 2 * kMtPart + (size_t)kMtStages * kMtRawBytes + 256;
+// A buffers, stages (1024-byte multiples: the swizzled boxes need 1024-byte
+// aligned destinations), centre; plus 1024 bytes to align the base
+constexpr size_t kMtSmem = (size_t)2 * 2 * kMtPart + (size_t)kMtStages * kMtRawBytes + 256 + 1024;
 static_assert((size_t)3 * kMtPart + (size_t)16 * kMtTile * 16 <= kMtSmem, "M = 128 reads stay inside the CTA's shared memory");
 static_assert(kMtSmem <= 232448 - 1024, "dynamic shared memory per CTA");
+static_assert((2 * 2 * kMtPart) % 1024 == 0 && kMtRawBytes % 1024 == 0, "stages start on 1024-byte boundaries");
 constexpr int kMtPartial = 65 * kMtCols;  // P = H / 2 + X of one CTA (S = P + P^T: H is symmetric)
 
 __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(const float *__restrict__ x, int d, int64_t n,
@@ -67,9 +77,13 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                                                                     const double *__restrict__ summary,
                                                                     const double *__restrict__ center,
                                                                     float *__restrict__ partial, int *error,
-                                                                    const int *__restrict__ gate) {
+                                                                    const int *__restrict__ gate,
+                                                                    const __grid_constant__ CUtensorMap tmap,
+                                                                    int tma) {
     if (gate != nullptr && *gate == 0) return;  // refinement pass not needed
-    extern __shared__ __align__(1024) unsigned char smem[];
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    // the swizzled boxes need 1024-byte aligned stages
+    unsigned char *smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
     unsigned char *s_a = smem;                                    // [buf][part] x kMtPart
     unsigned char *s_raw = smem + (size_t)2 * 2 * kMtPart;
     float *s_c = reinterpret_cast<float *>(s_raw + (size_t)kMtStages * kMtRawBytes);
@@ -108,9 +122,10 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
         abort_flag = 1;
         return false;
     };
-    // rows of 16-byte multiples at 16-byte aligned addresses: bulk copies
-    const bool bulk = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0) &&
-                      ((reinterpret_cast<uintptr_t>(lw) & 15) == 0);
+    // tensor copies of the tiles (d = 32 or 64, aligned arrays; the host
+    // encoded the tensor map); else padded rows by cp.async
+    const bool bulk = tma != 0;
+    const int nbox = d > 32 ? 2 : 1;
 
     if (warp == 0) {
         // ---- issuer: H += Ah Ah^T + Al Al^T, X += Al Ah^T per K slice ----
@@ -137,8 +152,8 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
             __syncwarp();
         }
     } else if (warp == kMtStagerWarp) {
-        // ---- stager: one bulk copy per sample row into the padded ring, the
-        // tile's log weights (whole 16-byte groups) in one more ----
+        // ---- stager: the tile's one or two swizzled boxes by tensor copies,
+        // its log weights (whole 16-byte groups) by one bulk copy ----
         if (bulk) {
             int issued = 0;
             for (int it = 0; it < my_tiles; ++it) {
@@ -150,13 +165,16 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                 }
                 const int64_t row0 = tile_of(it) * kMtTile;
                 const int rows = tile_rows(it);
-                const uint32_t rb = (uint32_t)d * 4u, wb = (uint32_t)(rows & ~3) * 4u;
-                float *dst = reinterpret_cast<float *>(s_raw + (size_t)s * kMtRawBytes);
-                if (lane == 0) tc::mbar_arrive_expect_tx(&raw_full[s], (uint32_t)rows * rb + wb);
+                const uint32_t wb = (uint32_t)(rows & ~3) * 4u;
+                unsigned char *dst = s_raw + (size_t)s * kMtRawBytes;
+                if (lane == 0) {
+                    // a box counts all its bytes (rows past n arrive as zeros)
+                    tc::mbar_arrive_expect_tx(&raw_full[s], (uint32_t)nbox * 16384u + wb);
+                    for (int b = 0; b < nbox; ++b)
+                        tc::tma_load_2d(dst + (size_t)b * 16384, &tmap, 32 * b, (int)row0, &raw_full[s]);
+                    if (wb > 0) tc::bulk_copy_g2s(dst + kMtWOff, lw + row0, wb, &raw_full[s]);
+                }
                 __syncwarp();
-                for (int r = lane; r < rows; r += 32)
-                    tc::bulk_copy_g2s(dst + r * kMtRS, x + (row0 + r) * d, rb, &raw_full[s]);
-                if (lane == 0 && wb > 0) tc::bulk_copy_g2s(dst + kMtTile * kMtRS, lw + row0, wb, &raw_full[s]);
                 issued = it + 1;
             }
             // every copy lands before the CTA can exit (the converters consume
@@ -201,7 +219,13 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                 ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
             }
             if (ok) {
-                const float *raw = reinterpret_cast<const float *>(s_raw + (size_t)stage * kMtRawBytes);
+                const unsigned char *stage_p = s_raw + (size_t)stage * kMtRawBytes;
+                const float *raw = reinterpret_cast<const float *>(stage_p);
+                // coordinates c .. c + 3 of this thread's row: swizzled box or padded row
+                auto row_at = [&](int c) -> const float4 * {
+                    return reinterpret_cast<const float4 *>(bulk ? tc::swizzled_row_chunk(stage_p, k, c)
+                                                                 : raw + k * kMtRS + c);
+                };
                 unsigned char *ah = s_a + (size_t)buf * 2 * kMtPart;
                 unsigned char *al = ah + kMtPart;
                 const int64_t i = tile_of(it) * kMtTile + k;
@@ -209,7 +233,7 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                 // the bulk copy carries whole 16-byte groups of weights; the
                 // (at most three) beyond them come from global memory
                 const int staged_w = bulk ? (tile_rows(it) & ~3) : kMtTile;
-                const float l = !active ? -INFINITY : (k < staged_w ? raw[kMtTile * kMtRS + k] : lw[i]);
+                const float l = !active ? -INFINITY : (k < staged_w ? raw[kMtWOff / 4 + k] : lw[i]);
                 const float sw = l == -INFINITY ? 0.f : expf(0.5f * (l - m)) * inv_sqrt_s;
                 const bool full = active && d == 64;
 #pragma unroll
@@ -219,8 +243,8 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                     const float4 c0 = *reinterpret_cast<const float4 *>(s_c + c),
                                  c1 = *reinterpret_cast<const float4 *>(s_c + c + 4);
                     if (full) {
-                        const float4 f0 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c);
-                        const float4 f1 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c + 4);
+                        const float4 f0 = *row_at(c);
+                        const float4 f1 = *row_at(c + 4);
                         v[0] = sw * (f0.x - c0.x);
                         v[1] = sw * (f0.y - c0.y);
                         v[2] = sw * (f0.z - c0.z);
@@ -232,8 +256,8 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                     } else {
                         float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f), f1 = f0;
                         if (active) {
-                            f0 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c);
-                            f1 = *reinterpret_cast<const float4 *>(raw + k * kMtRS + c + 4);
+                            f0 = *row_at(c);
+                            f1 = *row_at(c + 4);
                         }
                         v[0] = (active && c < d) ? sw * (f0.x - c0.x) : 0.f;
                         v[1] = (active && c + 1 < d) ? sw * (f0.y - c0.y) : 0.f;
@@ -437,15 +461,23 @@ int moments_tc(const void *x, int d, int64_t n, const void *lw, const double *su
     unsigned *counter = reinterpret_cast<unsigned *>(error + 1);  // zero with the workspace; reset by each use
     const int rblocks = (kMtPartial + 31) / 32;
     // pass 1 about `shift`
+    // tensor copies of the tiles when the shape allows (one map per call; both passes read it)
+    CUtensorMap tmap;
+    memset(&tmap, 0, sizeof(tmap));
+    int tma = 0;
+    if (row_tiles_supported(x, d, n) && ((reinterpret_cast<uintptr_t>(lw) & 15) == 0))
+        tma = encode_row_tiles(&tmap, x, d, n) == ISSM_OK ? 1 : 0;
     { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw,
-                                                                       summary, shift, partial, error, nullptr);
+                                                                       summary, shift, partial, error, nullptr,
+                                                                       tmap, tma);
       note_launch(); }
     { moments_tc_reduce_kernel<<<rblocks, kMtReduceThreads, 0, stream>>>(partial, blocks, sums, d, shift, mean, cov,
                                                                          nullptr, refine, prev_factor, counter);
       note_launch(); }
     // pass 2 about the new mean (kernels return at once unless pass 1 set `refine`)
     { moments_tc_kernel<<<blocks, kMtThreads, kMtSmem, stream>>>((const float *)x, d, n, (const float *)lw,
-                                                                      summary, mean, partial, error, refine);
+                                                                      summary, mean, partial, error, refine, tmap,
+                                                                      tma);
       note_launch(); }
     { moments_tc_reduce_kernel<<<rblocks, kMtReduceThreads, 0, stream>>>(partial, blocks, sums, d, mean, mean, cov,
                                                                          refine, nullptr, nullptr, counter);

@@ -192,6 +192,26 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst_smem, const void *src, u
         : "memory");
 }
 
+// Tiled 2-D tensor copy global -> shared through a tensor map (this GPU's own
+// memory, no multicast); completion counted on the mbarrier in bytes. x is the
+// inner (element) coordinate and must be a multiple of 16 bytes; y the row.
+__device__ __forceinline__ void tma_load_2d(void *dst_smem, const void *tmap, int x, int y, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst_smem)), "l"(reinterpret_cast<uint64_t>(tmap)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Shared-memory address of the 16-byte chunk holding coordinates c .. c + 3
+// (c a multiple of 4) of `row` in a tile staged by 128-byte-swizzled tensor
+// copies of 32-float boxes: box c / 32 of 128 rows x 128 bytes, chunk
+// (c / 4) % 8 of the row XOR (row % 8).
+__device__ __forceinline__ const float *swizzled_row_chunk(const unsigned char *stage, int row, int c) {
+    const int c4 = c >> 2;
+    return reinterpret_cast<const float *>(stage + (size_t)(c4 >> 3) * 16384 + (size_t)row * 128 +
+                                           ((((c4 & 7) ^ (row & 7))) << 4));
+}
+
 // Two FP32 values rounded to nearest-even bf16 and packed: a in the low half,
 // b in the high half (cvt.rn.bf16x2 puts its first source in the high half).
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {

@@ -20,6 +20,7 @@ GAUSSIAN, STUDENT_T = 0, 1
 SCALE_FACTOR, SCALE_DIAGONAL, SCALE_SPHERICAL = 0, 1, 2
 DENOM_FULL, DENOM_GENERATING, DENOM_PARTIAL, DENOM_PREFIX = 0, 1, 2, 3
 PREC_NATIVE, PREC_TF32, PREC_BF16 = 0, 1, 2
+PREC_BF16X1 = 3  # regression likelihood only: one bf16 product per K slice
 
 REASON_TARGET_NAN = 0x0100
 REASON_TARGET_POS_INF = 0x0200
@@ -114,6 +115,13 @@ SIGNATURES = [
     ("issm_fit_factor", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _p, _p, _p, _p, _i64, _p]),
     ("issm_fit_factor_ex", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _p, _p, _p, _p, _p, _i64, _p]),
     ("issm_fit_factor_reg", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _d, _p, _p, _p, _p, _p, _i64, _p]),
+    ("issm_weighted_sum_workspace_bytes", _sz, [_i64, _i32]),
+    ("issm_weighted_sum", C.c_int, [_p, _i32, _i64, _p, _i32, _p, _p, _p, _sz, _p]),
+    ("issm_weighted_quantile_workspace_bytes", _sz, [_i32, _i32]),
+    ("issm_weighted_quantile", C.c_int, [_p, _i32, _i64, _p, _i32, _p, _p, _i32, _p, _p, _sz, _p]),
+    ("issm_glm_operand_bytes", _sz, [_i32, _i32, _i32]),
+    ("issm_glm_prepare", C.c_int, [C.POINTER(Target), _i32, _p, _sz, _p]),
+    ("issm_glm_logdensity", C.c_int, [C.POINTER(Target), _i32, _p, _p, _i64, _p, _p, _p]),
     ("issm_select_workspace_bytes", _sz, []),
     ("issm_select_kth", C.c_int, [_p, _i64, _i64, _i32, _p, _p, _sz, _p]),
     ("issm_npmc_clip", C.c_int, [_p, _i64, _i32, _p, _p, _p, _sz, _p]),

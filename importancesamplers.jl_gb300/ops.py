@@ -283,6 +283,53 @@ def fit_factor(mean, cov, previous_factor, out_location, out_factor, out_lognorm
                 native.ptr(out_lognorm), native.ptr(out_inverse), native.ptr(failures), int(failure_index), _s())
 
 
+def weighted_sum(x, logweights, summary, out=None):
+    """sum_i w_i x_i per column (FP64) with the self-normalised weights of
+    the summary; x is (n,) or (n, d)."""
+    n = x.shape[0]
+    d = x.shape[1] if x.dim() == 2 else 1
+    out = torch.empty(d, dtype=torch.float64, device=x.device) if out is None else out
+    nb = native.lib().issm_weighted_sum_workspace_bytes(n, d)
+    ws = native.workspace(nb, x.device, "wsum")
+    native.call("issm_weighted_sum", native.ptr(x), d, n, native.ptr(logweights), _dt(x), native.ptr(summary),
+                native.ptr(out), native.ptr(ws), ws.numel(), _s())
+    return out
+
+
+def weighted_quantile(x, logweights, summary, probabilities):
+    """Component-wise weighted quantiles: (len(probabilities), d) FP64."""
+    n = x.shape[0]
+    d = x.shape[1] if x.dim() == 2 else 1
+    probs = torch.tensor([float(p) for p in probabilities], dtype=torch.float64, device=x.device)
+    out = torch.empty(probs.numel(), d, dtype=torch.float64, device=x.device)
+    nb = native.lib().issm_weighted_quantile_workspace_bytes(d, probs.numel())
+    ws = native.workspace(nb, x.device, "quantile")
+    native.call("issm_weighted_quantile", native.ptr(x), d, n, native.ptr(logweights), _dt(x), native.ptr(summary),
+                native.ptr(probs), probs.numel(), native.ptr(out), native.ptr(ws), ws.numel(), _s())
+    return out
+
+
+def glm_operand(target_struct, precision, device):
+    """The observations' tensor-core operand form of a LINREG / LOGISTIC
+    target (built once per target and precision)."""
+    nb = native.lib().issm_glm_operand_bytes(target_struct.count, target_struct.dim, int(precision))
+    ops_buf = torch.empty(max(int(nb), 16), dtype=torch.uint8, device=device)
+    native.call("issm_glm_prepare", ctypes.byref(target_struct), int(precision), native.ptr(ops_buf),
+                ops_buf.numel(), _s())
+    return ops_buf
+
+
+def glm_logdensity(target_struct, precision, operand, x, out=None):
+    """Regression log target of n FP32 samples: X beta on the tensor cores
+    with the likelihood reduced in the epilogue."""
+    n = x.shape[0]
+    out = torch.empty(n, dtype=torch.float32, device=x.device) if out is None else out
+    err = native.workspace(64, x.device, "glm", zero=True)
+    native.call("issm_glm_logdensity", ctypes.byref(target_struct), int(precision), native.ptr(operand),
+                native.ptr(x), n, native.ptr(out), native.ptr(err), _s())
+    return out
+
+
 def select_kth(values, k, out=None):
     """The k-th smallest (1-based) of `values` into a device scalar (NaN last)."""
     out = torch.empty(1, dtype=values.dtype, device=values.device) if out is None else out

@@ -62,10 +62,12 @@ def phase_of(reason_bits):
 
 class WeightedSamples:
     """samples: (n, d) device tensor (the reference's d x n column-major
-    layout), logweights: (n,), provenance / diagnostics: dicts."""
+    layout), or a dict of named (n, ...) device tensors (the reference's
+    NamedTuple samples); logweights: (n,); provenance / diagnostics: dicts."""
 
     def __init__(self, samples, logweights, provenance=None, diagnostics=None):
-        if samples.shape[0] != logweights.shape[0]:
+        counts = [t.shape[0] for t in samples.values()] if isinstance(samples, dict) else [samples.shape[0]]
+        if any(c != logweights.shape[0] for c in counts):
             raise ValueError("sample and weight counts must match")
         self.samples = samples
         self.logweights = logweights
@@ -110,19 +112,90 @@ def normalized_weights(result):
     return ops.normalize(result.logweights, sm)
 
 
-def mean(result):
-    w = normalized_weights(result)
+def _checked_summary(result):
+    sm = result.summary()
+    if float(sm[1]) == 0.0:
+        raise AllZeroWeightsError()
+    return sm
+
+
+def _functional_values(f, result):
+    """f's value for every sample, on the device: f maps the (n, d) sample
+    tensor (or a dict of named (n, ...) tensors) to one number per sample
+    (_device_functional_values, src/statistics.jl:15-34)."""
+    v = f(result.samples)
+    if not isinstance(v, torch.Tensor) or v.shape != (len(result),):
+        raise ValueError("device functionals must return one concrete number per sample")
+    if not v.dtype.is_floating_point:
+        v = v.double()
+    return v.contiguous()
+
+
+def mean(result, f=None):
+    """Self-normalised weighted mean (Statistics.mean(result),
+    src/statistics.jl:11-16), or the weighted expectation of the scalar
+    function f (mean(f, result), :18-33): one device pass, FP64 sums. Named
+    (dict) samples give a dict of means."""
+    sm = _checked_summary(result)
+    if f is not None:
+        v = _functional_values(f, result)
+        return float(ops.weighted_sum(v, result.logweights, sm).item())
     x = result.samples
+    if isinstance(x, dict):
+        return {k: _mean_of(t, result.logweights, sm) for k, t in x.items()}
+    return _mean_of(x, result.logweights, sm)
+
+
+def _mean_of(x, lw, sm):
     if x.dim() == 1:
-        return float(torch.dot(w.double(), x.double()))
-    return (w.double()[None, :] @ x.double()).reshape(-1)
+        return float(ops.weighted_sum(x, lw, sm).item())
+    return ops.weighted_sum(x.reshape(x.shape[0], -1).contiguous(), lw, sm).reshape(x.shape[1:])
 
 
-def var(result):
-    w = normalized_weights(result).double()
-    x = result.samples.double()
-    mu = mean(result)
-    return ((x - mu) ** 2 * (w[:, None] if x.dim() == 2 else w)).sum(0)
+def var(result, f=None, corrected=False):
+    """Uncorrected weighted variance (Statistics.var(result),
+    src/statistics.jl:35-63), of the samples or of f's values;
+    corrected=True is unsupported, as in the reference."""
+    if corrected:
+        raise ValueError("corrected moments are undefined for importance weights")
+    sm = _checked_summary(result)
+    x = _functional_values(f, result) if f is not None else result.samples
+    mu = ops.weighted_sum(x, result.logweights, sm)
+    dev = (x.double() - (mu if x.dim() == 2 else mu[0])) ** 2
+    v = ops.weighted_sum(dev.contiguous(), result.logweights, sm)
+    return float(v.item()) if x.dim() == 1 else v
+
+
+def std(result, f=None, corrected=False):
+    v = var(result, f, corrected)
+    return float(np.sqrt(v)) if isinstance(v, float) else torch.sqrt(v)
+
+
+def quantile(result, probabilities):
+    """Component-wise weighted quantiles with the StatsBase generic-weight
+    interpolation rule (Statistics.quantile, src/statistics.jl:106-154), on
+    the device: a scalar probability gives (d,), a list gives (len, d); 1-D
+    samples give floats. The reference requires a host result for this; here
+    the device result is used as it is."""
+    scalar = np.ndim(probabilities) == 0
+    probs = [float(probabilities)] if scalar else [float(p) for p in probabilities]
+    if not probs:
+        raise ValueError("quantile probabilities cannot be empty")
+    if not all(0.0 <= p <= 1.0 for p in probs):
+        raise ValueError("quantile probabilities must lie in [0, 1]")
+    sm = _checked_summary(result)
+    x = result.samples
+    if isinstance(x, dict):
+        return {k: quantile(WeightedSamples(t, result.logweights), probabilities) for k, t in x.items()}
+    q = ops.weighted_quantile(x.contiguous(), result.logweights, sm, probs)
+    if x.dim() == 1:
+        vals = q[:, 0].cpu().numpy()
+        return float(vals[0]) if scalar else vals
+    return q[0] if scalar else q
+
+
+def median(result):
+    return quantile(result, 0.5)
 
 
 def cov(result):
@@ -144,6 +217,8 @@ class UnweightedSamples:
         self.ancestors = ancestors
 
     def __len__(self):
+        if isinstance(self.samples, dict):
+            return next(iter(self.samples.values())).shape[0]
         return self.samples.shape[0]
 
 
@@ -188,7 +263,15 @@ def resample(seed, result, count=None, method=None, cdf="exact"):
     else:
         raise TypeError("unknown resampling method")
     x = result.samples
-    out = ops.gather(x if x.dim() == 2 else x.reshape(-1, 1), anc)
-    if x.dim() == 1:
-        out = out.reshape(-1)
-    return UnweightedSamples(out, anc)
+    if isinstance(x, dict):  # named samples: every field gathered by the same ancestors
+        return UnweightedSamples({k: _gather_rows(t, anc) for k, t in x.items()}, anc)
+    return UnweightedSamples(_gather_rows(x, anc), anc)
+
+
+def _gather_rows(x, anc):
+    """Rows anc - 1 of an (n, ...) device tensor (_gather_resampled_samples!,
+    src/resampling.jl:120-164): trailing dimensions flattened into one row of
+    the gather kernel."""
+    flat = x.reshape(x.shape[0], -1).contiguous()
+    out = ops.gather(flat, anc)
+    return out.reshape((anc.numel(),) + tuple(x.shape[1:]))

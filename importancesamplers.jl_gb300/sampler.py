@@ -127,9 +127,11 @@ class _Span:
 
 
 class PreparedSampler:
-    def __init__(self, seed, target, algorithm, device, precision, graphs=True, regularization=None):
+    def __init__(self, seed, target, algorithm, device, precision, graphs=True, regularization=None,
+                 target_precision=None):
         self.profile = None  # list of (name, start, end, algorithmic bytes) when profiling
         self.regularization = regularization
+        self.target_precision = precision if target_precision is None else target_precision
         self.seed = int(seed) & (2 ** 64 - 1)
         self.offset = 0
         self.target = target
@@ -174,7 +176,7 @@ class PreparedSampler:
 
 
 def prepare_sampler(seed, target, algorithm, device="cuda", precision=native.PREC_NATIVE, graphs=True,
-                    regularization=None):
+                    regularization=None, target_precision=None):
     """prepare_sampler(rng, logtarget, alg) with the device applied: packs the
     proposal(s) and allocates every buffer on the device.
 
@@ -185,10 +187,17 @@ def prepare_sampler(seed, target, algorithm, device="cuda", precision=native.PRE
     regularization: the moment fit's ridge coefficient. None keeps the
     reference's sqrt(eps(T)) of the sample type; an FP64 sampler given
     sqrt(eps(Float32)) fits exactly as an FP32 one would, which is how an FP64
-    run is compared with a reduced-precision run on the same draws."""
+    run is compared with a reduced-precision run on the same draws.
+
+    precision: PREC_NATIVE (the SIMT drop-in), PREC_TF32 or PREC_BF16 for
+    the AMIS / N-PMC density, moment and target kernels. Static MIS and
+    DM-PMC rounds (draw + every slot's density fused) run the SIMT kernel in
+    every form. target_precision (default: precision) is the form of the
+    built-in regression targets' X beta likelihood: PREC_BF16 (bf16 x3),
+    PREC_TF32, PREC_BF16X1 (one bf16 product) or PREC_NATIVE (SIMT)."""
     native.require()
     device = torch.device(device)
-    s = PreparedSampler(seed, target, algorithm, device, precision, graphs, regularization)
+    s = PreparedSampler(seed, target, algorithm, device, precision, graphs, regularization, target_precision)
     if isinstance(algorithm, ImportanceSampling):
         _prepare_static(s)
     elif isinstance(algorithm, (AMIS, NPMC)):
@@ -267,9 +276,11 @@ def _run_static(s):
     slots = ops.static_assign(db.cdf, u, s.stratified)
     normals = s.normals(n * d, dt)
     rn, ru = _radial_buffers(s, n, dt)
+    # the fused round (draw + every slot's density + log weight) is the SIMT
+    # kernel; the target runs in the sampler's target precision
     samples, lw, pid = ops.mis_round(db, s.den, slots, normals, None, rn, s.rn_stride, ru, s.ru_stride, fail,
-                                     s.precision)
-    values = s.bound_target.evaluate(samples, precision=s.precision)
+                                     native.PREC_NATIVE)
+    values = s.bound_target.evaluate(samples, precision=s.target_precision)
     ops.add_target_values(lw, values, fail)
     _raise_failures(fail.cpu().numpy())
     scheme = type(alg.mis_scheme).__name__
@@ -397,7 +408,7 @@ def _moment_body(s, is_npmc):
                                 rn_stride=s.rn_stride, radial_uniforms=ru, ru_stride=s.ru_stride, failures=fail,
                                 out=x_new, bank_ref=view)
         with _Span(s, "target", n_new * (d + 1) * es):
-            s.bound_target.evaluate(x_new, out=s.logtargets[n_old:n_tot], precision=s.precision)
+            s.bound_target.evaluate(x_new, out=s.logtargets[n_old:n_tot], precision=s.target_precision)
             ops.check_target_values(s.logtargets[n_old:n_tot], s.round_ids[n_old:n_tot], fail)
         if is_npmc:
             den = ops.denominator(native.DENOM_GENERATING)
@@ -695,9 +706,9 @@ def _run_dmpmc(s):
         rn, ru = _radial_buffers(s, n, dt)
         den = ops.denominator(native.DENOM_FULL, s.coefs[r])
         x, lw, pid = ops.mis_round(db, den, s.slots[r], normals, None, rn, s.rn_stride, ru, s.ru_stride, fail,
-                                   s.precision, samples=s.samples[lo:hi], logweights=s.logweights[lo:hi],
+                                   native.PREC_NATIVE, samples=s.samples[lo:hi], logweights=s.logweights[lo:hi],
                                    proposal_ids_out=s.proposal_ids[lo:hi])
-        s.bound_target.evaluate(x, out=_scratch(s, n, dt), precision=s.precision)
+        s.bound_target.evaluate(x, out=_scratch(s, n, dt), precision=s.target_precision)
         ops.add_target_values(lw, s._scratch[:n], fail)
         ops.logweight_summary(lw, out=s.summaries[r])
         if local:

@@ -55,9 +55,20 @@ class _NativeTarget:
 class _Bound:
     def __init__(self, target, struct, ta, tb):
         self.target, self.struct, self.keep = target, struct, (ta, tb)
+        self.operands = {}  # tensor-core operand form of a regression target, per precision
 
     def evaluate(self, samples, out=None, precision=None):
-        return ops.target_logdensity(self.struct, samples, out)
+        """The regression targets run their X beta on the tensor cores in the
+        reduced-precision forms (FP32 samples, d <= 64); every other case is
+        the SIMT kernel in the target's type."""
+        prec = native.PREC_NATIVE if precision is None else int(precision)
+        s = self.struct
+        if (prec != native.PREC_NATIVE and s.kind in (native.TARGET_LINREG, native.TARGET_LOGISTIC)
+                and samples.dtype == torch.float32 and s.dtype == native.F32 and s.dim <= 64):
+            if prec not in self.operands:
+                self.operands[prec] = ops.glm_operand(s, prec, samples.device)
+            return ops.glm_logdensity(s, prec, self.operands[prec], samples, out)
+        return ops.target_logdensity(s, samples, out)
 
 
 class _BoundBank:

@@ -72,6 +72,7 @@ typedef struct CUstream_st *issm_stream_t;
 #define ISSM_PREC_NATIVE 0  /* SIMT in the bank dtype: the drop-in FP32/FP64 path */
 #define ISSM_PREC_TF32   1  /* tcgen05 kind::tf32, FP32 accumulate, centred inputs */
 #define ISSM_PREC_BF16   2  /* tcgen05 kind::f16 (bf16), FP32 accumulate, centred inputs */
+#define ISSM_PREC_BF16X1 3  /* regression likelihood only: one bf16 product per K slice (no split) */
 
 /* Failure reason bits (src/execution.jl:758-767, adaptive_gaussian_execution.jl:9) */
 #define ISSM_REASON_TARGET_NAN          0x0100u
@@ -434,6 +435,31 @@ int issm_fit_factor_reg(const double *mean, const double *cov, int32_t d,
                         float *out_inverse, uint64_t *failures,
                         int64_t failure_index, issm_stream_t stream);
 
+/* ---- result statistics ------------------------------------------------------
+ * Statistics.mean(result) / mean(f, result) (src/statistics.jl:11-33): the
+ * self-normalised weighted sum out[c] = sum_i w_i x[i, c] (FP64, d >= 1),
+ * with w_i = e^{l_i - m} / S from the 3-word summary of the log weights;
+ * bitwise reproducible (per-block partials reduced in a fixed order). For
+ * the functional mean pass f's values as x with d = 1. */
+size_t issm_weighted_sum_workspace_bytes(int64_t n, int32_t d);
+int issm_weighted_sum(const void *x, int32_t d, int64_t n, const void *logweights,
+                      int32_t dtype, const double *summary, double *out,
+                      void *workspace, size_t workspace_bytes, issm_stream_t stream);
+/* Statistics.quantile(result, probabilities) (src/statistics.jl:106-154):
+ * component-wise weighted quantiles with the StatsBase generic-weight rule
+ * (threshold p (W - w_first) + w_first over the value-sorted positive-weight
+ * samples, linear interpolation between the neighbours), on the device with
+ * no sort (a weighted radix select); out[q * d + c] for probability q and
+ * coordinate c, in FP64 holding the sample type's value; NaN for a
+ * coordinate with a NaN sample. probabilities: device FP64, each in [0, 1]
+ * (the caller checks). The reference evaluates it on the host only. */
+size_t issm_weighted_quantile_workspace_bytes(int32_t d, int32_t nprob);
+int issm_weighted_quantile(const void *x, int32_t d, int64_t n, const void *logweights,
+                           int32_t dtype, const double *summary,
+                           const double *probabilities, int32_t nprob, double *out,
+                           void *workspace, size_t workspace_bytes,
+                           issm_stream_t stream);
+
 /* ---- N-PMC weight clipping ---------------------------------------------------
  * _moment_adaptation_workspace!(::NPMC, ...) (src/npmc_execution.jl:22-33):
  * the isqrt(n) largest of a round's n log weights are clipped to the
@@ -523,6 +549,26 @@ typedef struct issm_target {
 /* out[i] = log target(x_i) for n samples (d x n, target dtype). */
 int issm_target_logdensity(const issm_target *target, const void *x, int64_t n,
                            void *out, issm_stream_t stream);
+
+/* The LINREG / LOGISTIC targets' likelihood as a tensor-core GEMM: X beta
+ * for every (sample, observation) pair on tcgen05 with the Gaussian or
+ * Bernoulli-logit log-likelihood reduced in the epilogue, plus the prior
+ * (the batch callbacks of src/batched_targets.jl:54-214 and
+ * examples/batched_linear_regression.jl:18-37, whose X beta is a GEMM).
+ * FP32 target, d <= 64. precision: ISSM_PREC_BF16 (bf16 x3 split),
+ * ISSM_PREC_TF32, or ISSM_PREC_BF16X1 (one bf16 product: the plain BF16
+ * GEMM form, about 8 bits per product). issm_glm_prepare writes the
+ * observations' operand form (issm_glm_operand_bytes) once per target and
+ * precision; issm_glm_logdensity then evaluates n samples (d x n). `error`
+ * is a device int the caller zeroes; it becomes 1 if a completion wait
+ * timed out. Results stay within the form's log-density tolerance of
+ * issm_target_logdensity. */
+size_t issm_glm_operand_bytes(int32_t nobs, int32_t d, int32_t precision);
+int issm_glm_prepare(const issm_target *target, int32_t precision, void *operand,
+                     size_t operand_bytes, issm_stream_t stream);
+int issm_glm_logdensity(const issm_target *target, int32_t precision,
+                        const void *operand, const float *x, int64_t n,
+                        float *out, int32_t *error, issm_stream_t stream);
 
 /* ---- one AMIS run in one call --------------------------------------------
  * Every launch of an AMIS run with a Gaussian factor proposal (draws with

@@ -838,6 +838,66 @@ int orc_amis_run(const orc_target *target, int d, int family, double dof,
     return status;
 }
 
+/* ---- weighted quantile (src/statistics.jl:114-154) ---------------------------- */
+typedef struct { double v; int64_t i; } orc_vi;
+static int cmp_vi(const void *a, const void *b) {  /* value, then index: a stable sort */
+    const orc_vi *x = (const orc_vi *)a, *y = (const orc_vi *)b;
+    if (x->v < y->v) return -1;
+    if (x->v > y->v) return 1;
+    /* -0.0 sorts before 0.0 (Julia's isless) */
+    if (signbit(x->v) != signbit(y->v)) return signbit(x->v) ? -1 : 1;
+    return (x->i > y->i) - (x->i < y->i);
+}
+
+/* Component-wise weighted quantiles of x (n x d row-major) under normalised
+ * weights w: positive-weight samples sorted by value (stable), cumulative
+ * weights, threshold p (W - w_first) + w_first, upper = first index whose
+ * cumulative weight exceeds it (searchsortedlast + 1), linear interpolation
+ * with lower = upper - 1; NaN for a coordinate holding a NaN.
+ * out[q * d + c]. */
+void orc_weighted_quantile(const double *x, int d, int64_t n, const double *w, const double *probs, int nprob,
+                           double *out) {
+    orc_vi *buf = (orc_vi *)malloc(sizeof(orc_vi) * (size_t)n);
+    double *cum = (double *)malloc(sizeof(double) * (size_t)n);
+    for (int c = 0; c < d; ++c) {
+        int nan = 0;
+        int64_t m = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            const double v = x[(size_t)i * d + c];
+            if (isnan(v)) nan = 1;
+            if (w[i] != 0.0) { buf[m].v = v; buf[m].i = i; ++m; }
+        }
+        if (nan || m == 0) {
+            for (int q = 0; q < nprob; ++q) out[(size_t)q * d + c] = NAN;
+            continue;
+        }
+        qsort(buf, (size_t)m, sizeof(orc_vi), cmp_vi);
+        double s = 0.0;
+        for (int64_t j = 0; j < m; ++j) { s += w[buf[j].i]; cum[j] = s; }
+        const double total = cum[m - 1], first = w[buf[0].i];
+        for (int q = 0; q < nprob; ++q) {
+            const double thr = probs[q] * (total - first) + first;
+            int64_t upper = 0;  /* 0-based: first j with cum[j] > thr */
+            while (upper < m && !(cum[upper] > thr)) ++upper;
+            double v;
+            if (upper >= m) {
+                v = buf[m - 1].v;
+            } else {
+                const int64_t lower = upper - 1;
+                const double f = (thr - cum[lower]) / (cum[upper] - cum[lower]);
+                if (f == 0.0) v = buf[lower].v;
+                else {
+                    const double diff = buf[upper].v - buf[lower].v;
+                    v = isfinite(diff) ? buf[lower].v + f * diff : (1.0 - f) * buf[lower].v + f * buf[upper].v;
+                }
+            }
+            out[(size_t)q * d + c] = v;
+        }
+    }
+    free(buf);
+    free(cum);
+}
+
 static int cmp_double_nan_last(const void *a, const void *b) {
     const double x = *(const double *)a, y = *(const double *)b;
     if (isnan(x)) return isnan(y) ? 0 : 1;

@@ -105,6 +105,8 @@ int orc_fit_factor(const double *mean, const double *cov, int d,
                    const double *prev_factor, double dof, double logconstant,
                    double regularization, double *out_factor,
                    double *out_lognorm);
+void orc_weighted_quantile(const double *x, int d, int64_t n, const double *w, const double *probs, int nprob,
+                           double *out);
 int orc_npmc_run(const orc_target *target, int d, int family, double dof, const double *loc0,
                  const double *factor0, int rounds, const int64_t *schedule, const double *normals,
                  const double *rn, int rn_stride, const double *ru, int ru_stride, double regularization,

@@ -94,6 +94,7 @@ def _declare(L):
                                p, p, p, p, p, p, p, p, p, p]
     L.orc_set_threads.argtypes = [i32]
     L.orc_num_threads.restype = i32
+    L.orc_weighted_quantile.argtypes = [p, i32, i64, p, p, i32, p]
     L.orc_npmc_run.restype = i32
     L.orc_npmc_run.argtypes = [C.POINTER(Target), i32, i32, d, p, p, i32, p, p, p, i32, p, i32, d,
                                p, p, p, p, p, p, p, p]
@@ -299,6 +300,15 @@ def fit_factor(mean, cov, prev_factor, dof=0.0, logconstant=0.0, regularization=
     st = lib().orc_fit_factor(mean.ctypes.data, cov.ctypes.data, d, prev.ctypes.data, float(dof),
                               float(logconstant), float(reg), L.ctypes.data, C.addressof(ln))
     return st, L.reshape(d, d, order="F"), ln.value
+
+
+def weighted_quantile(x, d, w, probs):
+    """(len(probs), d) weighted quantiles of x (n x d) under weights w."""
+    x, w, pr = _f64(x), _f64(w), _f64(probs)
+    n = w.size
+    out = np.empty(pr.size * d)
+    lib().orc_weighted_quantile(x.ctypes.data, int(d), n, w.ctypes.data, pr.ctypes.data, pr.size, out.ctypes.data)
+    return out.reshape(pr.size, d)
 
 
 def npmc_run(target, d, loc0, factor0, schedule, normals, family=GAUSSIAN, dof=0.0, regularization=None):
