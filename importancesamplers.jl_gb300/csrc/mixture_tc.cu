@@ -145,6 +145,7 @@ constexpr int kStagerWarp = kFirstEpiWarp + kEpiWarps;  // bulk copies of the st
 constexpr int kTcThreads = 32 * (2 + kConvWarps + kEpiWarps);
 constexpr int kBRing = 3;      // operand buffers in flight when a tile needs several chunks
 constexpr int kMaxRawStages = 4;
+constexpr bool kTcTensorStaging = false;  // see launch_tc
 
 template <int KIND, int SPLIT, int DP, bool DIRECT>
 __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, const __grid_constant__ CUtensorMap tmap) {
@@ -314,16 +315,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, c
     } else if (warp < kFirstEpiWarp) {
         // ================= converters: sample tiles -> A operand =================
         const int ctid = tid - 32;
-        auto issue_raw = [&](int it) {  // 4-byte cp.async staging (rows without bulk copies)
+        auto issue_raw = [&](int it) {  // cp.async staging into padded rows
             if (it < my_tiles) {
                 const int64_t row0 = tile_of(it) * kTcTile;
                 const int rows = (int)min((int64_t)kTcTile, p.n - row0);
                 float *dst = reinterpret_cast<float *>(s_raw + (size_t)(it % S) * RAW_BYTES);
                 const float *src = p.x + row0 * p.d;
-                const int total = rows * p.d;
-                for (int e = ctid; e < total; e += kConvThreads) {
-                    const int r = e / p.d, c = e - r * p.d;
-                    tc::cp_async4(dst + r * RS + c, src + (size_t)r * p.d + c);
+                if (vec && p.d == DP) {
+                    constexpr int Q4 = DP / 4;
+                    const int total = rows * Q4;
+                    for (int e = ctid; e < total; e += kConvThreads) {
+                        const int r = e / Q4, c4 = e % Q4;
+                        tc::cp_async16(dst + r * RS + c4 * 4, src + (size_t)e * 4);
+                    }
+                } else if (vec) {
+                    const int q4 = p.d >> 2, total = rows * q4;
+                    for (int e = ctid; e < total; e += kConvThreads) {
+                        const int r = e / q4, c4 = e - r * q4;
+                        tc::cp_async16(dst + r * RS + c4 * 4, src + (size_t)r * p.d + c4 * 4);
+                    }
+                } else {
+                    const int total = rows * p.d;
+                    for (int e = ctid; e < total; e += kConvThreads) {
+                        const int r = e / p.d, c = e - r * p.d;
+                        tc::cp_async4(dst + r * RS + c, src + (size_t)r * p.d + c);
+                    }
                 }
             }
             tc::cp_async_commit();
@@ -646,11 +662,14 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     p.ntiles = (int)((p.n + kTcTile - 1) / kTcTile);
     const int blocks = min(p.ntiles, device_sms() * occ);
     if (blocks < 1) return 0;
-    // staged tiles by tensor copies when the rows are whole 32-float boxes
+    // Staged tiles by tensor copies (kTcTensorStaging) measured slower than
+    // the converters' own 16-byte cp.async for this kernel (append pass at
+    // d = 64: 5.2 ms against 3.8 ms per 40-round run), so the copies stay
+    // with the converters; the tensor-copy path is kept for shapes that gain.
     CUtensorMap tmap;
     memset(&tmap, 0, sizeof(tmap));
     p.tma = 0;
-    if (stages > 0 && DP == p.d && row_tiles_supported(p.x, p.d, p.n))
+    if (kTcTensorStaging && stages > 0 && DP == p.d && row_tiles_supported(p.x, p.d, p.n))
         p.tma = encode_row_tiles(&tmap, p.x, p.d, p.n) == ISSM_OK ? 1 : 0;
     { kern<<<blocks, kTcThreads, smem, stream>>>(p, tmap); note_launch(); }
     return (int)cudaGetLastError();

@@ -24,8 +24,8 @@
 //
 // A is stored MN-major: each sample's 8-coordinate groups are 16-byte chunks,
 // so two threads convert a sample row straight from the staged tile. Warp
-// roles: warp 0 issues the MMAs; warps 1..8 build A (double-buffered) from
-// the staged tiles; warp 9 stages the tiles. For d = 32 or 64 (aligned
+// roles: warp 0 issues the MMAs; warps 1..16 build A (double-buffered) from
+// the staged tiles; warp 17 stages the tiles. For d = 32 or 64 (aligned
 // arrays) the stager keeps a four-deep ring of stages filled by tensor copies
 // (cp.async.bulk.tensor through a tensor map of the samples: one or two
 // 32-float x 128-row boxes per tile, 128-byte swizzle, so converters read
@@ -44,7 +44,10 @@
 
 namespace issm {
 
-constexpr int kMtConvWarps = 8;
+// 16 converter warps (four threads per sample row, two coordinate groups
+// each): the conversion is latency-bound, and with one CTA per SM (shared
+// memory) only more warps hide its dependency chains
+constexpr int kMtConvWarps = 16;
 constexpr int kMtConvThreads = 32 * kMtConvWarps;
 constexpr int kMtStagerWarp = 1 + kMtConvWarps;
 constexpr int kMtThreads = 32 * (2 + kMtConvWarps);  // issuer, converters, stager
@@ -193,9 +196,18 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                 float *dst = reinterpret_cast<float *>(s_raw + (size_t)(it % kMtStages) * kMtRawBytes);
                 float *dlw = dst + kMtTile * kMtRS;
                 const float *src = x + row0 * d;
-                for (int e = ctid; e < rows * d; e += kMtConvThreads) {
-                    const int r = e / d, c = e - r * d;
-                    tc::cp_async4(dst + r * kMtRS + c, src + (size_t)r * d + c);
+                const bool vec = (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(x) & 15) == 0);
+                if (vec) {
+                    const int q4 = d >> 2, total = rows * q4;
+                    for (int e = ctid; e < total; e += kMtConvThreads) {
+                        const int r = e / q4, c4 = e - r * q4;
+                        tc::cp_async16(dst + r * kMtRS + c4 * 4, src + (size_t)r * d + c4 * 4);
+                    }
+                } else {
+                    for (int e = ctid; e < rows * d; e += kMtConvThreads) {
+                        const int r = e / d, c = e - r * d;
+                        tc::cp_async4(dst + r * kMtRS + c, src + (size_t)r * d + c);
+                    }
                 }
                 for (int r = ctid; r < rows; r += kMtConvThreads) tc::cp_async4(dlw + r, lw + row0 + r);
             }

@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 
 # largest |error| / max(1, |log target|) per form: bf16 x3 keeps about 16
 # bits per product, tf32 11, one bf16 product 8
-TOL = {"bf16": 5e-6, "tf32": 3e-4, "bf16x1": 3e-3}
+TOL = {"bf16": 5e-6, "tf32": 1e-3, "bf16x1": 3e-3}
 
 
 def _fp64_logtarget(kind, X, y, B, sigma, prior_var):
