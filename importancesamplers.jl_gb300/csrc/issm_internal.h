@@ -74,6 +74,10 @@ int population_factors(const void *covs, int d, int k, int dtype, const uint8_t 
 bool row_tiles_supported(const void *x, int d, int64_t n);
 int encode_row_tiles(CUtensorMap *map, const void *x, int d, int64_t n);
 
+// one launch per phase across the in-flight runs of a serving loop (group.cu)
+int group_step(const void *runs, int nruns, int64_t blocks_new, int64_t blocks_all, int64_t blocks_mom,
+               cudaStream_t stream);
+
 // result statistics (stats.cu)
 size_t weighted_sum_workspace_bytes(int64_t n, int d);
 int weighted_sum(const void *x, int d, int64_t n, const void *lw, int dtype, const double *summary, double *out,

@@ -32,8 +32,6 @@
 //       log-sum-exp states through shared memory when the tile completes.
 // Every wait is bounded; a timeout sets the sticky error word and the CTA
 // unwinds after draining its outstanding copies and MMAs.
-#include <cstring>
-
 #include "issm_device.cuh"
 #include "issm_internal.h"
 #include "tcgen05.cuh"
@@ -133,7 +131,6 @@ struct TcParams {
     uint64_t *failures;
     int64_t index_base;
     int *error;
-    int tma;  // staged tiles arrive by tensor copies (swizzled 32-float boxes) of `x`
 };
 
 // Warp roles of mixture_tc_kernel.
@@ -141,14 +138,11 @@ constexpr int kConvWarps = 8;  // stage sample tiles and build the A operand
 constexpr int kEpiWarps = 4;   // one per TMEM lane quadrant
 constexpr int kConvThreads = 32 * kConvWarps;
 constexpr int kFirstEpiWarp = 1 + kConvWarps;
-constexpr int kStagerWarp = kFirstEpiWarp + kEpiWarps;  // bulk copies of the staged sample tiles
-constexpr int kTcThreads = 32 * (2 + kConvWarps + kEpiWarps);
+constexpr int kTcThreads = 32 * (1 + kConvWarps + kEpiWarps);
 constexpr int kBRing = 3;      // operand buffers in flight when a tile needs several chunks
-constexpr int kMaxRawStages = 4;
-constexpr bool kTcTensorStaging = false;  // see launch_tc
 
 template <int KIND, int SPLIT, int DP, bool DIRECT>
-__global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, const __grid_constant__ CUtensorMap tmap) {
+__global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
     constexpr int PER = 16 / EB;              // elements per 16-byte K group
     constexpr int KG = DP / PER;              // K groups of the sample coordinates
@@ -170,22 +164,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, c
     const uint32_t LBO_B = (uint32_t)(chunk * DP * 16);
     const uint32_t CHUNK_BYTES = (uint32_t)(NPART * chunk * B_COMP);
 
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    // stages start on 1024-byte boundaries (the swizzled boxes need them)
-    unsigned char *smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
+    extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *s_raw = smem;
     unsigned char *s_a = s_raw + (size_t)S * RAW_BYTES;
     unsigned char *s_b = s_a + (size_t)nbufA * NPART * A_PART;
     float *s_c = reinterpret_cast<float *>(s_b + (size_t)nbufB * CHUNK_BYTES);
     __shared__ __align__(8) uint64_t a_full[2], a_empty[2], b_full[kBRing], b_empty[kBRing], d_full[2], d_empty[2];
-    __shared__ __align__(8) uint64_t raw_full[kMaxRawStages], raw_empty[kMaxRawStages];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_flag;
-    // staged tiles with rows of 16-byte multiples at 16-byte aligned
-    // addresses arrive by one bulk copy per row from the stager warp
-    const bool vec = (p.d % 4 == 0) && ((reinterpret_cast<uintptr_t>(p.x) & 15) == 0);
-    const bool bulk = !DIRECT && S > 0 && p.tma != 0;
-    const int nbox = p.d > 32 ? 2 : 1;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int NW = chunk * DP;  // TMEM columns of one accumulator
@@ -201,10 +187,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, c
         for (int b = 0; b < kBRing; ++b) {
             tc::mbar_init(&b_full[b], 1);
             tc::mbar_init(&b_empty[b], 1);
-        }
-        for (int s = 0; s < kMaxRawStages; ++s) {
-            tc::mbar_init(&raw_full[s], 1);
-            tc::mbar_init(&raw_empty[s], kConvWarps);
         }
         tc::fence_mbar_init();
         abort_flag = 0;
@@ -315,7 +297,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, c
     } else if (warp < kFirstEpiWarp) {
         // ================= converters: sample tiles -> A operand =================
         const int ctid = tid - 32;
-        auto issue_raw = [&](int it) {  // cp.async staging into padded rows
+        const bool vec = (p.d % 4 == 0) && ((reinterpret_cast<uintptr_t>(p.x) & 15) == 0);
+        auto issue_raw = [&](int it) {
             if (it < my_tiles) {
                 const int64_t row0 = tile_of(it) * kTcTile;
                 const int rows = (int)min((int64_t)kTcTile, p.n - row0);
@@ -344,8 +327,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, c
             }
             tc::cp_async_commit();
         };
-        if (!DIRECT && !bulk)
-            for (int s = 0; s < S; ++s) issue_raw(s);
+        for (int s = 0; s < S; ++s) issue_raw(s);
         const int row = ctid & (kTcTile - 1), half = ctid >> 7;
         constexpr int HV = DP / 8;  // float4s of this thread's half row
         for (int it = 0; it < my_tiles; ++it) {
@@ -368,21 +350,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, c
                                             active && c + 3 < p.d ? xr[c + 3] : 0.f);
                     }
                 }
+            } else {
+                if (S == 1) tc::cp_async_wait<0>();
+                else if (S == 2) tc::cp_async_wait<1>();
+                else tc::cp_async_wait<2>();
+                tc::named_sync(1, kConvThreads);
             }
             bool ok = true;
-            if (!DIRECT) {
-                if (bulk) {
-                    // every lane acquires the stage's bytes itself; the outcome is made warp-uniform
-                    ok = __all_sync(0xffffffffu, wait(&raw_full[it % S], (uint32_t)((it / S) & 1)));
-                } else {
-                    if (S == 1) tc::cp_async_wait<0>();
-                    else if (S == 2) tc::cp_async_wait<1>();
-                    else tc::cp_async_wait<2>();
-                    tc::named_sync(1, kConvThreads);
-                }
-            }
             const int abuf = it % nbufA;
-            if (it >= nbufA && ok) {
+            if (it >= nbufA) {
                 if (lane == 0) ok = wait(&a_empty[abuf], (uint32_t)(((it - nbufA) / nbufA) & 1));
                 ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
             }
@@ -407,19 +383,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, c
                             v[m + 2] = (active && c + 2 < p.d) ? f.z - cc.z : 0.f;
                             v[m + 3] = (active && c + 3 < p.d) ? f.w - cc.w : 0.f;
                         } else if (full) {
-                            const float4 f = *reinterpret_cast<const float4 *>(
-                                bulk ? tc::swizzled_row_chunk(reinterpret_cast<const unsigned char *>(raw), row, c)
-                                     : raw + row * RS + c);
+                            const float4 f = *reinterpret_cast<const float4 *>(raw + row * RS + c);
                             v[m] = f.x - cc.x;
                             v[m + 1] = f.y - cc.y;
                             v[m + 2] = f.z - cc.z;
                             v[m + 3] = f.w - cc.w;
                         } else {
                             float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
-                            if (active)
-                                f = *reinterpret_cast<const float4 *>(
-                                    bulk ? tc::swizzled_row_chunk(reinterpret_cast<const unsigned char *>(raw), row, c)
-                                         : raw + row * RS + c);
+                            if (active) f = *reinterpret_cast<const float4 *>(raw + row * RS + c);
                             v[m] = (active && c < p.d) ? f.x - cc.x : 0.f;
                             v[m + 1] = (active && c + 1 < p.d) ? f.y - cc.y : 0.f;
                             v[m + 2] = (active && c + 2 < p.d) ? f.z - cc.z : 0.f;
@@ -435,42 +406,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p, c
             tc::fence_proxy_async();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&a_full[it % nbufA]);
-            if (bulk) {
-                if (lane == 0) tc::mbar_arrive(&raw_empty[it % S]);  // this warp is done with the stage
-            } else if (!DIRECT) {
+            if (!DIRECT) {
                 tc::named_sync(1, kConvThreads);  // the stage is consumed: refill it
                 issue_raw(it + S);
             }
         }
         tc::cp_async_wait_all();
-    } else if (warp == kStagerWarp) {
-        // ================= stager: a tile's swizzled boxes by tensor copies =================
-        if (bulk) {
-            int issued = 0;
-            for (int it = 0; it < my_tiles; ++it) {
-                const int s = it % S;
-                if (it >= S) {
-                    int fine = 1;
-                    if (lane == 0) fine = wait(&raw_empty[s], (uint32_t)(((it / S) - 1) & 1));
-                    if (!__shfl_sync(0xffffffffu, fine, 0)) break;
-                }
-                const int64_t row0 = tile_of(it) * kTcTile;
-                unsigned char *dst = s_raw + (size_t)s * RAW_BYTES;
-                if (lane == 0) {
-                    // a box counts all its bytes (rows past n arrive as zeros)
-                    tc::mbar_arrive_expect_tx(&raw_full[s], (uint32_t)nbox * 16384u);
-                    for (int b = 0; b < nbox; ++b)
-                        tc::tma_load_2d(dst + (size_t)b * 16384, &tmap, 32 * b, (int)row0, &raw_full[s]);
-                }
-                __syncwarp();
-                issued = it + 1;
-            }
-            // every copy lands before the CTA can exit (the converters consume
-            // them all unless a wait timed out)
-            if (lane == 0)
-                for (int it = max(0, issued - S); it < issued; ++it)
-                    tc::mbar_wait(&raw_full[it % S], (uint32_t)((it / S) & 1));
-        }
     } else {
         // ================= epilogue: radial densities and the log-sum-exp =================
         const int qd = warp & 3;
@@ -626,13 +567,13 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
         nch = (nslots + chunk - 1) / chunk;
         if (nch == 1) {
             stages = 3;
-            smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)NPART * chunk * B_COMP + (size_t)DP * 4 + 1024;
+            smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)NPART * chunk * B_COMP + (size_t)DP * 4;
         } else {
             // a staged tile if it fits beside a kBRing-deep operand ring; else
             // the converters read their rows from global memory (no staged
             // tile), with a kBRing- or 2-deep ring, which leaves room for
             // larger chunks (fewer, wider MMA items per tile)
-            const size_t base = NPART * A_PART + (size_t)DP * 4 + 1024, cb = (size_t)NPART * chunk * B_COMP;
+            const size_t base = NPART * A_PART + (size_t)DP * 4, cb = (size_t)NPART * chunk * B_COMP;
             bring = kBRing;
             stages = RAW_BYTES + base + kBRing * cb <= kTcMaxSmem ? 1 : 0;
             if (stages == 0 && base + kBRing * cb > kTcMaxSmem) bring = 2;
@@ -662,16 +603,7 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     p.ntiles = (int)((p.n + kTcTile - 1) / kTcTile);
     const int blocks = min(p.ntiles, device_sms() * occ);
     if (blocks < 1) return 0;
-    // Staged tiles by tensor copies (kTcTensorStaging) measured slower than
-    // the converters' own 16-byte cp.async for this kernel (append pass at
-    // d = 64: 5.2 ms against 3.8 ms per 40-round run), so the copies stay
-    // with the converters; the tensor-copy path is kept for shapes that gain.
-    CUtensorMap tmap;
-    memset(&tmap, 0, sizeof(tmap));
-    p.tma = 0;
-    if (kTcTensorStaging && stages > 0 && DP == p.d && row_tiles_supported(p.x, p.d, p.n))
-        p.tma = encode_row_tiles(&tmap, p.x, p.d, p.n) == ISSM_OK ? 1 : 0;
-    { kern<<<blocks, kTcThreads, smem, stream>>>(p, tmap); note_launch(); }
+    { kern<<<blocks, kTcThreads, smem, stream>>>(p); note_launch(); }
     return (int)cudaGetLastError();
 }
 

@@ -115,6 +115,8 @@ SIGNATURES = [
     ("issm_fit_factor", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _p, _p, _p, _p, _i64, _p]),
     ("issm_fit_factor_ex", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _p, _p, _p, _p, _p, _i64, _p]),
     ("issm_fit_factor_reg", C.c_int, [_p, _p, _i32, _p, _d, _d, _i32, _d, _p, _p, _p, _p, _p, _i64, _p]),
+    ("issm_group_run_bytes", _sz, []),
+    ("issm_group_step", C.c_int, [_p, _i32, _i64, _i64, _i64, _p]),
     ("issm_weighted_sum_workspace_bytes", _sz, [_i64, _i32]),
     ("issm_weighted_sum", C.c_int, [_p, _i32, _i64, _p, _i32, _p, _p, _p, _sz, _p]),
     ("issm_weighted_quantile_workspace_bytes", _sz, [_i32, _i32]),

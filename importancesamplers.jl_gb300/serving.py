@@ -25,7 +25,7 @@ import torch
 
 from . import native
 from .methods import AMIS
-from .results import RoundError, SamplerExecutionError
+from .results import AMISRoundError, RoundError, SamplerExecutionError
 from .sampler import (SamplerBusyError, _finish_moment_summary, _moment_body, _native_body, native_body_eligible,
                       prepare_sampler)
 
@@ -181,6 +181,233 @@ class ServeLoop:
             elif running:
                 time.sleep(0.0002)
         return results
+
+
+GROUP_TILE, GROUP_MOMENT_SAMPLES, GROUP_MOMENT_WORDS = 128, 2048, 2145
+_RUN_FIELDS = ["d", "rounds", "round", "n_round", "n_old", "seed", "normal_offset", "blk_new0", "blk_all0",
+               "blk_mom0", "nmom", "samples", "logtargets", "lognum", "logweights", "loc", "fac", "lognorm",
+               "cand_loc", "cand_fac", "cand_lognorm", "t_mode", "t_chol", "summaries", "mean", "cov", "failures",
+               "partial", "mpartial", "t_const", "logcount"]
+_COL = {name: k for k, name in enumerate(_RUN_FIELDS)}
+
+
+def _cdiv(a, b):
+    return -(-a // b)
+
+
+class _GroupedRun:
+    """The device state of one admitted run: three allocations (FP32, FP64,
+    failure words) carved into the issm_group_run arrays."""
+
+    def __init__(self, request, device, start):
+        p, tgt = request.proposal, request.target
+        d, R, n = p.dimension, request.rounds, request.round_size
+        self.request, self.start, self.round = request, start, 0
+        self.d, self.R, self.n = d, R, n
+        # the target's exact mode-centred form from its sufficient statistics
+        X, y, s2, pv = tgt.X, tgt.y, tgt.sigma ** 2, tgt.prior_var
+        A = X.T @ X / s2 + np.eye(d) / pv
+        mode = np.linalg.solve(A, X.T @ y / s2)
+        r = y - X @ mode
+        c0 = (-0.5 * len(y) * np.log(2 * np.pi * s2) - 0.5 * float(r @ r) / s2
+              - 0.5 * d * np.log(2 * np.pi * pv) - 0.5 * float(mode @ mode) / pv)
+        U = np.linalg.cholesky(A).T  # A = U^T U, U upper
+        # FP32 block: history, candidate, target, samples and per-sample arrays
+        sizes = {"loc": R * d, "fac": R * d * d, "lognorm": R, "cand_loc": d, "cand_fac": d * d, "cand_lognorm": 1,
+                 "t_mode": d, "t_chol": d * d, "samples": R * n * d, "logtargets": R * n, "lognum": R * n,
+                 "logweights": R * n}
+        off, o = {}, 0
+        for k, v in sizes.items():
+            off[k] = o
+            o += _cdiv(v, 64) * 64  # 256-byte aligned slices
+        self.f32 = torch.empty(o, dtype=torch.float32, device=device)
+        host = np.concatenate([np.asarray(p.location, dtype=np.float32),
+                               np.ascontiguousarray(p.factor_matrix().T, dtype=np.float32).reshape(-1),
+                               np.array([p.lognormalizer], dtype=np.float32), mode.astype(np.float32),
+                               np.ascontiguousarray(U.T, dtype=np.float32).reshape(-1)])
+        # pinned (cached host allocator) and asynchronous: admission never waits for the device
+        staged = torch.from_numpy(host).pin_memory().to(device, non_blocking=True)
+        f = self.f32
+        f[off["loc"]:off["loc"] + d].copy_(staged[:d])
+        f[off["fac"]:off["fac"] + d * d].copy_(staged[d:d + d * d])
+        f[off["lognorm"]:off["lognorm"] + 1].copy_(staged[d + d * d:d + d * d + 1])
+        f[off["t_mode"]:off["t_mode"] + d].copy_(staged[d + d * d + 1:2 * d + d * d + 1])
+        f[off["t_chol"]:off["t_chol"] + d * d].copy_(staged[2 * d + d * d + 1:])
+        # FP64 block: summaries, mean, covariance, summary and moment partials
+        self.blk_all_max = _cdiv(R * n, GROUP_TILE)
+        self.nmom_max = _cdiv(R * n, GROUP_MOMENT_SAMPLES)
+        d64 = {"summaries": 3 * R, "mean": d, "cov": d * d, "partial": 3 * self.blk_all_max,
+               "mpartial": GROUP_MOMENT_WORDS * self.nmom_max}
+        off64, o = {}, 0
+        for k, v in d64.items():
+            off64[k] = o
+            o += _cdiv(v, 32) * 32
+        self.f64 = torch.zeros(o, dtype=torch.float64, device=device)
+        self.fail = torch.zeros(3 * R, dtype=torch.int64, device=device)
+        self.ptr = {k: self.f32.data_ptr() + 4 * v for k, v in off.items()}
+        self.ptr.update({k: self.f64.data_ptr() + 8 * v for k, v in off64.items()})
+        self.ptr["failures"] = self.fail.data_ptr()
+        self.off64 = off64
+        self.t_const = float(c0)
+        self.normal_offset = 0
+
+    def nbytes(self):
+        return self.f32.numel() * 4 + self.f64.numel() * 8 + self.fail.numel() * 8
+
+
+class GroupedServeLoop:
+    """Continuous batching of AMIS linear-regression posterior runs (Gaussian
+    factor proposals, FP32, d <= 64) with one launch per phase per step for
+    every in-flight run (issm_group_step).
+
+    Each step advances every in-flight run by one round: the host writes one
+    descriptor row per run (its arrays, round, random-stream position and
+    block offsets), copies the table to the device and issues seven kernels;
+    runs of any dimension, budget and round share the launches. A request
+    joins at the next step once it has arrived and the memory budget allows;
+    a run that finished its last round is read back (its final summary,
+    posterior mean and failure words, one copy for every run that finished
+    at that step) and its memory returned. At most `lookahead` steps are in
+    flight, so admissions follow the device. A run's numbers depend only on
+    its own inputs and seed: alone and in any mix they are bitwise the same."""
+
+    def __init__(self, device="cuda", memory_budget=16 << 30, max_inflight=4096, lookahead=2):
+        native.require()
+        self.device = torch.device(device)
+        self.memory_budget = int(memory_budget)
+        self.max_inflight = int(max_inflight)
+        self.lookahead = int(lookahead)
+        self.stream = torch.cuda.current_stream(self.device)
+
+    @staticmethod
+    def eligible(request):
+        from .proposals import FACTOR, GAUSSIAN
+        from .targets import LinearRegressionTarget
+
+        p = request.proposal
+        return (isinstance(request.target, LinearRegressionTarget) and p.family == GAUSSIAN and
+                p.scale_kind == FACTOR and p.dtype == np.float32 and p.dimension <= 64)
+
+    def _table(self, runs):
+        t = np.zeros((len(runs), len(_RUN_FIELDS)), dtype=np.int64)
+        f = t.view(np.float64)
+        bn = ba = bm = 0
+        for k, g in enumerate(runs):
+            n_old = g.round * g.n
+            nall = n_old + g.n
+            row = t[k]
+            row[_COL["d"]], row[_COL["rounds"]], row[_COL["round"]] = g.d, g.R, g.round
+            row[_COL["n_round"]], row[_COL["n_old"]] = g.n, n_old
+            row[_COL["seed"]] = np.int64(np.uint64(g.request.seed & (2 ** 64 - 1)).view(np.int64))
+            row[_COL["normal_offset"]] = g.normal_offset
+            row[_COL["blk_new0"]], row[_COL["blk_all0"]], row[_COL["blk_mom0"]] = bn, ba, bm
+            nmom = _cdiv(nall, GROUP_MOMENT_SAMPLES)
+            row[_COL["nmom"]] = nmom
+            for name in ("samples", "logtargets", "lognum", "logweights", "loc", "fac", "lognorm", "cand_loc",
+                         "cand_fac", "cand_lognorm", "t_mode", "t_chol", "summaries", "mean", "cov", "failures",
+                         "partial", "mpartial"):
+                row[_COL[name]] = g.ptr[name]
+            f[k, _COL["t_const"]] = g.t_const
+            f[k, _COL["logcount"]] = float(np.float32(np.log(g.n)))
+            bn += _cdiv(g.n, GROUP_TILE)
+            ba += _cdiv(nall, GROUP_TILE)
+            bm += nmom
+        return t, bn, ba, bm
+
+    def run(self, requests, clock=time.perf_counter):
+        pending = sorted(requests, key=lambda r: r.arrival)
+        for r in pending:
+            if not self.eligible(r):
+                raise ValueError(f"request {r.rid}: the grouped loop serves linear-regression targets with FP32 "
+                                 "Gaussian factor proposals of d <= 64")
+        lib = native.lib()
+        t0 = clock()
+        queue, active, finishing, results = [], [], [], []
+        steps = []  # (event, host table, device table) of steps in flight
+        used, i = 0, 0
+        while i < len(pending) or queue or active or finishing:
+            now = clock() - t0
+            while i < len(pending) and pending[i].arrival <= now:
+                queue.append(pending[i])
+                i += 1
+            # retire runs whose last step has completed
+            if finishing:
+                done = [(g, ev) for g, ev in finishing if ev.query()]
+                if done:
+                    finishing = [(g, ev) for g, ev in finishing if not ev.query() or all(g is not h for h, _ in done)]
+                    results.extend(self._retire([g for g, _ in done], clock() - t0))
+                    used -= sum(g.nbytes() for g, _ in done)
+            # admit in arrival order while the in-flight cap and the memory budget allow
+            while queue and len(active) < self.max_inflight:
+                g = _GroupedRun(queue[0], self.device, clock() - t0)
+                if used + g.nbytes() > self.memory_budget and active:
+                    del g
+                    break
+                queue.pop(0)
+                active.append(g)
+                used += g.nbytes()
+            if active:
+                # at most `lookahead` steps in flight
+                while len(steps) >= self.lookahead:
+                    steps.pop(0)[0].synchronize()
+                table, bn, ba, bm = self._table(active)
+                host = torch.from_numpy(table).pin_memory()
+                dev = torch.empty_like(host, device=self.device)
+                dev.copy_(host, non_blocking=True)
+                native.call("issm_group_step", dev.data_ptr(), len(active), bn, ba, bm,
+                            self.stream.cuda_stream)
+                ev = torch.cuda.Event()
+                ev.record(self.stream)
+                steps.append((ev, host, dev))
+                still = []
+                for g in active:
+                    g.normal_offset += g.n * g.d + 8
+                    g.round += 1
+                    if g.round == g.R:
+                        finishing.append((g, ev))
+                    else:
+                        still.append(g)
+                active = still
+            elif not queue and i < len(pending):
+                time.sleep(max(0.0, min(pending[i].arrival - (clock() - t0), 0.001)))
+            elif finishing:
+                time.sleep(0.0002)
+        return results
+
+    def _retire(self, runs, now):
+        """One copy for every run that finished at a step: its failure words,
+        last summary and posterior mean (the last fit's moments over every
+        retained sample with the final weights)."""
+        parts = []
+        for g in runs:
+            s = g.off64["summaries"] + 3 * (g.R - 1)
+            parts += [g.fail.view(torch.float64), g.f64[s:s + 3], g.f64[g.off64["mean"]:g.off64["mean"] + g.d]]
+        packed = torch.cat(parts).cpu().numpy()
+        out, o = [], 0
+        for g in runs:
+            words = packed[o:o + 3 * g.R].view(np.int64).reshape(g.R, 3)
+            o += 3 * g.R
+            m, s, s2 = packed[o:o + 3]
+            o += 3
+            mean = packed[o:o + g.d].copy()
+            o += g.d
+            error = None
+            for t in range(g.R):
+                if words[t][0] != 0:
+                    from .sampler import _raise_failures
+
+                    try:
+                        _raise_failures(words[t], AMISRoundError, t + 1)
+                    except AMISRoundError as e:
+                        error = e
+                    break
+            total = g.R * g.n
+            logz = float(m + np.log(s) - np.log(total)) if s > 0 else float("-inf")
+            ess = float(s * s / s2) if s > 0 else 0.0
+            if error is not None:
+                mean, logz, ess = np.full(g.d, np.nan), float("nan"), 0.0
+            out.append(ServeResult(g.request, mean, logz, ess, g.start, now, error))
+        return out
 
 
 def serve_latency_summary(results):

@@ -616,6 +616,47 @@ int issm_amis_run(const issm_amis_run_desc *run, issm_stream_t stream);
 size_t issm_amis_run_desc_bytes(void);
 size_t issm_amis_run_desc_workspace_offset(void);
 
+/* ---- many runs per launch (serving) -----------------------------------------
+ * No one-call counterpart in the reference, which runs each sampler's rounds
+ * on its own (the per-run sequence is _launch_prefilled_amis_round!,
+ * src/amis_execution.jl:261-357, then _fit_moment_proposal!,
+ * src/adaptive_gaussian_execution.jl:348-425). issm_group_step advances every
+ * run of a device table of issm_group_run rows by one AMIS round with seven
+ * launches in all, however many runs: draws from the counter-based normal
+ * stream, the linear-regression target in its mode-centred quadratic form,
+ * the retrospective mixture, weights and their summary, FP64 moment sums
+ * about the previous location, and the FP64 fit of the next proposal. Gaussian
+ * factor proposals, FP32 samples, d <= 64, one sample count per round per
+ * run. Rows are ordered by their block offsets: blk_new0 (ceil(n_round /
+ * ISSM_GROUP_TILE) blocks per run), blk_all0 (ceil((n_old + n_round) /
+ * ISSM_GROUP_TILE)) and blk_mom0 (ceil((n_old + n_round) /
+ * ISSM_GROUP_MOMENT_SAMPLES), = nmom) are each run's cumulative starts and
+ * blocks_new / blocks_all / blocks_mom the totals. `partial` holds 3 doubles
+ * per blk_all block and `mpartial` ISSM_GROUP_MOMENT_WORDS per moment block.
+ * A run only touches its own arrays and every per-run reduction has a fixed
+ * order, so its results do not depend on the other runs in the table. */
+#define ISSM_GROUP_TILE 128
+#define ISSM_GROUP_MOMENT_SAMPLES 2048
+#define ISSM_GROUP_MOMENT_WORDS 2145
+typedef struct issm_group_run {
+    int64_t d, rounds, round, n_round, n_old;   /* round: 0-based round of this step */
+    uint64_t seed, normal_offset;               /* normal stream position of this round */
+    int64_t blk_new0, blk_all0, blk_mom0, nmom;
+    float *samples, *logtargets, *lognum, *logweights;   /* rounds * n_round (x d) */
+    float *loc, *fac, *lognorm;                 /* history: rounds slots, factors column-major */
+    float *cand_loc, *cand_fac, *cand_lognorm;  /* the last round's fit */
+    const float *t_mode, *t_chol;               /* target: mode (d), U (d x d column-major, upper) */
+    double *summaries;                          /* rounds x 3: (max, S, S2) of each round's weights */
+    double *mean, *cov;                         /* FP64 d, d x d: the last fit's moments */
+    uint64_t *failures;                         /* rounds x 3 failure records */
+    double *partial, *mpartial;                 /* scratch of this step */
+    double t_const;                             /* target: log p(y, mode) */
+    double logcount;                            /* log n_round */
+} issm_group_run;
+size_t issm_group_run_bytes(void);
+int issm_group_step(const issm_group_run *runs, int32_t nruns, int64_t blocks_new,
+                    int64_t blocks_all, int64_t blocks_mom, issm_stream_t stream);
+
 /* ---- tensor-core self-test ------------------------------------------------
  * No counterpart in the reference: a one-CTA tcgen05 GEMM
  * C[128 x n] = A[128 x k] B[n x k]^T (row-major FP32 in and out; inputs rounded

@@ -11,8 +11,11 @@ import torch
 pytestmark = pytest.mark.gpu
 
 # largest |error| / max(1, |log target|) per form: bf16 x3 keeps about 16
-# bits per product, tf32 11, one bf16 product 8
-TOL = {"bf16": 5e-6, "tf32": 1e-3, "bf16x1": 3e-3}
+# bits per product, tf32 11, one bf16 product 8. The Gaussian likelihood
+# squares the residual y - x'beta, which doubles the relative error of a
+# small residual, and the FP32 sum over observations adds about 1e-6
+# (the SIMT FP32 path is held to 1e-5 for the same reason)
+TOL = {"bf16": 1e-5, "tf32": 2e-3, "bf16x1": 1e-2}
 
 
 def _fp64_logtarget(kind, X, y, B, sigma, prior_var):

@@ -205,3 +205,44 @@ def test_launch_failure_is_reported_and_the_loop_continues(issm, cuda):
         alone = issm.serving.ServeLoop(cuda, max_inflight=1).run([r])[0]
         assert out[r.rid].error is None
         assert np.array_equal(out[r.rid].posterior_mean, alone.posterior_mean) and out[r.rid].logz == alone.logz
+
+
+def test_grouped_serving_matches_alone_and_analytic(issm, cuda):
+    """One launch per phase per step for every in-flight run
+    (issm_group_step): each run gives bitwise the same numbers alone and in
+    the mix (runs of d = 2..64 and budgets 4k..40k share every launch), and
+    matches the conjugate analytic posterior."""
+    reqs, truth = _requests(issm, SPEC)
+    alone = {}
+    for r in reqs:
+        alone[r.rid] = issm.serving.GroupedServeLoop(cuda).run([r])[0]
+    reqs2, _ = _requests(issm, SPEC)
+    mixed = {res.rid: res for res in issm.serving.GroupedServeLoop(cuda).run(reqs2)}
+    assert sorted(mixed) == sorted(alone)
+    for rid, a in alone.items():
+        m = mixed[rid]
+        assert m.error is None and a.error is None
+        assert np.array_equal(a.posterior_mean, m.posterior_mean)
+        assert a.logz == m.logz and a.ess == m.ess
+        mean, sd, logz = truth[rid]
+        assert np.max(np.abs(m.posterior_mean - mean) / sd) < 0.25, rid
+        assert abs(m.logz - logz) < 0.1, (rid, m.logz, logz)
+
+
+def test_grouped_serving_staggered_arrivals(issm, cuda):
+    """Requests arriving while others are mid-run join at the next step (the
+    table holds runs in different rounds) and still give their alone
+    numbers; the memory budget caps the admitted footprint."""
+    reqs, truth = _requests(issm, SPEC * 3, seed=5)
+    for k, r in enumerate(reqs):
+        r.arrival = 0.002 * k
+    loop = issm.serving.GroupedServeLoop(cuda, max_inflight=5)
+    out = {res.rid: res for res in loop.run(reqs)}
+    assert len(out) == len(reqs)
+    reqs2, _ = _requests(issm, SPEC * 3, seed=5)
+    for r in reqs2[::4]:
+        a = issm.serving.GroupedServeLoop(cuda).run([r])[0]
+        assert np.array_equal(a.posterior_mean, out[r.rid].posterior_mean) and a.logz == out[r.rid].logz
+    for rid, res in out.items():
+        mean, sd, logz = truth[rid]
+        assert np.max(np.abs(res.posterior_mean - mean) / sd) < 0.25, rid

@@ -66,18 +66,21 @@ def test_weighted_mean_var_and_functional_mean(issm, cuda, dtype):
     tx, tl = torch.tensor(x, dtype=dtype, device=cuda), torch.tensor(lw, dtype=dtype, device=cuda)
     res = issm.WeightedSamples(tx, tl)
     xs, ws = tx.double().cpu().numpy(), _weights(tl.double().cpu().numpy())
+    # FP32 log weights are summarised in FP32 (max, sum of expf), as the
+    # reference sums FP32 weights; the weighted sums themselves are FP64
+    tol = 1e-10 if dtype == torch.float64 else 2e-6
     m = issm.mean(res).cpu().numpy()
-    assert np.allclose(m, ws @ xs, rtol=1e-10, atol=1e-10)
+    assert np.allclose(m, ws @ xs, rtol=tol, atol=tol)
     # bitwise reproducible: the same reduction order every call
     assert np.array_equal(m, issm.mean(res).cpu().numpy())
     v = issm.var(res).cpu().numpy()
-    assert np.allclose(v, ws @ (xs - ws @ xs) ** 2, rtol=1e-9)
+    assert np.allclose(v, ws @ (xs - ws @ xs) ** 2, rtol=10 * tol)
     f = lambda s: (s[:, 0] * s[:, 1]).double()  # noqa: E731
     fm = issm.mean(res, f)
-    assert fm == pytest.approx(float(ws @ (xs[:, 0] * xs[:, 1])), rel=1e-9)
+    assert fm == pytest.approx(float(ws @ (xs[:, 0] * xs[:, 1])), rel=10 * tol, abs=tol)
     fv = issm.var(res, f)
     vals = xs[:, 0] * xs[:, 1]
-    assert fv == pytest.approx(float(ws @ (vals - ws @ vals) ** 2), rel=1e-8)
+    assert fv == pytest.approx(float(ws @ (vals - ws @ vals) ** 2), rel=100 * tol)
     assert issm.std(res, f) == pytest.approx(np.sqrt(fv))
 
 
