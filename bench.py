@@ -642,8 +642,15 @@ def run_serve(args):
 
     # warm-up: compile-free, but first launches and allocations
     prec = {"fp32": issm.native.PREC_NATIVE, "tf32": issm.native.PREC_TF32, "bf16": issm.native.PREC_BF16}[args.precision]
-    warm, _ = make(8)
-    issm.serving.ServeLoop(dev, max_inflight=args.inflight, precision=prec).run(warm)
+    grouped = args.serve_loop == "grouped"
+
+    def loop():
+        if grouped:
+            return issm.serving.GroupedServeLoop(dev, max_inflight=args.inflight)
+        return issm.serving.ServeLoop(dev, max_inflight=args.inflight, precision=prec)
+
+    warm, _ = make(64)
+    loop().run(warm)
     sweep = []
     for rate in args.rates:
         reqs, truth = make(args.requests)
@@ -651,14 +658,19 @@ def run_serve(args):
         for r in reqs:
             t += rng.exponential(1.0 / rate)
             r.arrival = t
+        launches0 = issm.native.launches()
         t0 = time.perf_counter()
-        out = issm.serving.ServeLoop(dev, max_inflight=args.inflight, precision=prec).run(reqs)
+        out = loop().run(reqs)
         wall = time.perf_counter() - t0
+        launches = issm.native.launches() - launches0
+        errors = sum(r.error is not None for r in out)
+        out = [r for r in out if r.error is None]
         lat = np.array([r.latency for r in out])
         samples = sum(r.samples for r in reqs)
         lz = np.array([abs(r.logz - truth[r.rid][2]) for r in out])
         me = np.array([float(np.max(np.abs(r.posterior_mean - truth[r.rid][0]) / truth[r.rid][1])) for r in out])
-        sweep.append({"rate_per_s": rate, "requests": len(out), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+        sweep.append({"rate_per_s": rate, "requests": len(reqs), "failed_runs": errors, "gpu_launches": launches,
+                      "p50_ms": 1e3 * float(np.percentile(lat, 50)),
                       "p99_ms": 1e3 * float(np.percentile(lat, 99)), "samples_per_s": samples / wall,
                       "runs_per_s": len(out) / wall, "wall_s": wall,
                       "abs_logz_error": {"p50": float(np.median(lz)), "p90": float(np.percentile(lz, 90)),
@@ -669,7 +681,9 @@ def run_serve(args):
             "workload": "Bayesian linear regression posteriors, d~U{2..64}, n_obs log-uniform 50-5000, "
                         "budget log-uniform 1k-100k, AMIS 4 rounds, Poisson arrivals; initial proposal the "
                         "posterior's Laplace form displaced and widened by 0.5/sqrt(d) of its scale",
-            "precision": {"bf16": "bf16 (bf16 x3 split)", "tf32": "tf32", "fp32": "fp32"}[args.precision],
+            "serve_loop": args.serve_loop,
+            "precision": ("fp32 (grouped SIMT kernels; FP64 moments and fit)" if grouped else
+                          {"bf16": "bf16 (bf16 x3 split)", "tf32": "tf32", "fp32": "fp32"}[args.precision]),
             "max_inflight": args.inflight, "sweep": sweep}
     print(json.dumps(line), flush=True)
 
@@ -688,10 +702,17 @@ def main():
     ap.add_argument("--workload", default="amis", choices=["amis", "serve", "static-mis"],
                     help="amis: the headline AMIS d=64 run; serve: the serving-mix latency sweep; "
                          "static-mis: the N=4,194,304, d=16, K=64 static MIS microbench")
-    ap.add_argument("--requests", type=int, default=200, help="serve: requests per arrival rate")
-    ap.add_argument("--rates", type=float, nargs="+", default=[50.0, 200.0, 1000.0], help="serve: arrivals per second")
-    ap.add_argument("--inflight", type=int, default=8, help="serve: concurrent runs (streams)")
+    ap.add_argument("--requests", type=int, default=10_000, help="serve: requests per arrival rate")
+    ap.add_argument("--rates", type=float, nargs="+", default=[1000.0, 5000.0, 20000.0],
+                    help="serve: arrivals per second")
+    ap.add_argument("--serve-loop", default="grouped", choices=["grouped", "streams"],
+                    help="serve: grouped (one launch per phase per step for every in-flight run) or streams "
+                         "(one issm_amis_run per run on its own stream)")
+    ap.add_argument("--inflight", type=int, default=None,
+                    help="serve: concurrent runs (default 4096 grouped, 8 streams)")
     args = ap.parse_args()
+    if args.inflight is None:
+        args.inflight = 4096 if args.serve_loop == "grouped" else 8
     if args.workload == "serve":
         run_serve(args)
         return

@@ -56,6 +56,7 @@ int issm_amis_run(const issm_amis_run_desc *r, issm_stream_t stream) {
     if (!h.locations || !h.scales || !h.lognormalizers) return ISSM_E_NULL;
     const bool tc = r->precision != ISSM_PREC_NATIVE;
     if (tc && (h.dtype != ISSM_F32 || !h.inverse_factors)) return ISSM_E_UNSUPPORTED;
+    if (r->target_operand && h.dtype != ISSM_F32) return ISSM_E_DTYPE;  // the tensor-core likelihood reads FP32
     if (!r->samples || !r->logtargets || !r->lognum || !r->logweights || !r->round_ids || !r->round_ids_init ||
         !r->summaries || !r->round_failures || !r->mean || !r->cov || !r->shift || !r->cand_location ||
         !r->cand_factor || !r->cand_lognormalizer || !r->initial_location || !r->initial_factor ||
@@ -99,7 +100,12 @@ int issm_amis_run(const issm_amis_run_desc *r, issm_stream_t stream) {
         ISSM_TRY(issm_draw_philox(&view, t, r->seed, r->counter, offset, nullptr, 0, nullptr, 0, n_new, x_new, fail, 0,
                                   stream));
         offset += (uint64_t)n_new * d + 8;
-        ISSM_TRY(issm_target_logdensity(r->target, x_new, n_new, logtargets + (size_t)n_old * es, stream));
+        if (r->target_operand)  // X beta on the tensor cores, the likelihood in the epilogue
+            ISSM_TRY(issm_glm_logdensity(r->target, r->target_precision, r->target_operand, (const float *)x_new, n_new,
+                                         (float *)(logtargets + (size_t)n_old * es),
+                                         (int32_t *)(ws_tc + tc_bytes - 64), stream));
+        else
+            ISSM_TRY(issm_target_logdensity(r->target, x_new, n_new, logtargets + (size_t)n_old * es, stream));
         ISSM_TRY(issm_check_target_values(logtargets + (size_t)n_old * es, n_new, h.dtype, r->round_ids + n_old, fail,
                                           0, stream));
         // retrospective append over the retained samples, then the prefix mixture of the new ones

@@ -490,6 +490,10 @@ def _native_body(s):
                               native.ptr(s.round_ids), native.ptr(s.summaries), native.ptr(s.round_failures),
                               native.ptr(s.mean), native.ptr(s.cov), native.ptr(s.shift), native.ptr(s.cand_loc),
                               native.ptr(s.cand_factor), native.ptr(s.cand_lognorm), native.ptr(ws), ws.numel())
+    # the same target form as the host round loop's evaluate()
+    operand = s.bound_target.tensor_operand(s.target_precision, h.dtype, s.device)
+    if operand is not None:
+        desc.target_operand, desc.target_precision = native.ptr(operand), int(s.target_precision)
     native.call("issm_amis_run", ctypes.byref(desc), native.stream_ptr())
     s.offset = sum(int(v) * d + 8 for v in s.schedule)
 

@@ -197,7 +197,14 @@ def _cdiv(a, b):
 
 class _GroupedRun:
     """The device state of one admitted run: three allocations (FP32, FP64,
-    failure words) carved into the issm_group_run arrays."""
+    failure words) carved into the issm_group_run arrays, the initial
+    proposal and the target's constants written by one host-to-device copy,
+    and the run's fixed descriptor fields as one table row."""
+
+    # the FP32 block: what admission writes comes first (one contiguous copy
+    # covers the target's mode and factor and the history's slot 0)
+    _F32 = ("t_mode", "t_chol", "lognorm", "loc", "fac", "cand_loc", "cand_fac", "cand_lognorm", "samples",
+            "logtargets", "lognum", "logweights")
 
     def __init__(self, request, device, start):
         p, tgt = request.proposal, request.target
@@ -212,44 +219,44 @@ class _GroupedRun:
         c0 = (-0.5 * len(y) * np.log(2 * np.pi * s2) - 0.5 * float(r @ r) / s2
               - 0.5 * d * np.log(2 * np.pi * pv) - 0.5 * float(mode @ mode) / pv)
         U = np.linalg.cholesky(A).T  # A = U^T U, U upper
-        # FP32 block: history, candidate, target, samples and per-sample arrays
-        sizes = {"loc": R * d, "fac": R * d * d, "lognorm": R, "cand_loc": d, "cand_fac": d * d, "cand_lognorm": 1,
-                 "t_mode": d, "t_chol": d * d, "samples": R * n * d, "logtargets": R * n, "lognum": R * n,
+        sizes = {"t_mode": d, "t_chol": d * d, "lognorm": R, "loc": R * d, "fac": R * d * d, "cand_loc": d,
+                 "cand_fac": d * d, "cand_lognorm": 1, "samples": R * n * d, "logtargets": R * n, "lognum": R * n,
                  "logweights": R * n}
         off, o = {}, 0
-        for k, v in sizes.items():
+        for k in self._F32:
             off[k] = o
-            o += _cdiv(v, 64) * 64  # 256-byte aligned slices
+            o += _cdiv(sizes[k], 64) * 64  # 256-byte aligned slices
         self.f32 = torch.empty(o, dtype=torch.float32, device=device)
-        host = np.concatenate([np.asarray(p.location, dtype=np.float32),
-                               np.ascontiguousarray(p.factor_matrix().T, dtype=np.float32).reshape(-1),
-                               np.array([p.lognormalizer], dtype=np.float32), mode.astype(np.float32),
-                               np.ascontiguousarray(U.T, dtype=np.float32).reshape(-1)])
+        head = np.zeros(off["fac"] + d * d, dtype=np.float32)
+        head[off["t_mode"]:off["t_mode"] + d] = mode
+        head[off["t_chol"]:off["t_chol"] + d * d] = U.T.reshape(-1)  # U column-major
+        head[off["lognorm"]] = p.lognormalizer
+        head[off["loc"]:off["loc"] + d] = p.location
+        head[off["fac"]:off["fac"] + d * d] = p.factor_matrix().T.reshape(-1)  # L column-major
         # pinned (cached host allocator) and asynchronous: admission never waits for the device
-        staged = torch.from_numpy(host).pin_memory().to(device, non_blocking=True)
-        f = self.f32
-        f[off["loc"]:off["loc"] + d].copy_(staged[:d])
-        f[off["fac"]:off["fac"] + d * d].copy_(staged[d:d + d * d])
-        f[off["lognorm"]:off["lognorm"] + 1].copy_(staged[d + d * d:d + d * d + 1])
-        f[off["t_mode"]:off["t_mode"] + d].copy_(staged[d + d * d + 1:2 * d + d * d + 1])
-        f[off["t_chol"]:off["t_chol"] + d * d].copy_(staged[2 * d + d * d + 1:])
+        self.f32[:head.size].copy_(torch.from_numpy(head).pin_memory(), non_blocking=True)
         # FP64 block: summaries, mean, covariance, summary and moment partials
-        self.blk_all_max = _cdiv(R * n, GROUP_TILE)
-        self.nmom_max = _cdiv(R * n, GROUP_MOMENT_SAMPLES)
-        d64 = {"summaries": 3 * R, "mean": d, "cov": d * d, "partial": 3 * self.blk_all_max,
-               "mpartial": GROUP_MOMENT_WORDS * self.nmom_max}
+        d64 = {"summaries": 3 * R, "mean": d, "cov": d * d, "partial": 3 * _cdiv(R * n, GROUP_TILE),
+               "mpartial": GROUP_MOMENT_WORDS * _cdiv(R * n, GROUP_MOMENT_SAMPLES)}
         off64, o = {}, 0
         for k, v in d64.items():
             off64[k] = o
             o += _cdiv(v, 32) * 32
         self.f64 = torch.zeros(o, dtype=torch.float64, device=device)
         self.fail = torch.zeros(3 * R, dtype=torch.int64, device=device)
-        self.ptr = {k: self.f32.data_ptr() + 4 * v for k, v in off.items()}
-        self.ptr.update({k: self.f64.data_ptr() + 8 * v for k, v in off64.items()})
-        self.ptr["failures"] = self.fail.data_ptr()
         self.off64 = off64
-        self.t_const = float(c0)
-        self.normal_offset = 0
+        # the descriptor fields that never change
+        row = np.zeros(len(_RUN_FIELDS), dtype=np.int64)
+        row[_COL["d"]], row[_COL["rounds"]], row[_COL["n_round"]] = d, R, n
+        row[_COL["seed"]] = np.uint64(request.seed & (2 ** 64 - 1)).view(np.int64)
+        for k, v in off.items():
+            row[_COL[k]] = self.f32.data_ptr() + 4 * v
+        for k, v in off64.items():
+            row[_COL[k]] = self.f64.data_ptr() + 8 * v
+        row[_COL["failures"]] = self.fail.data_ptr()
+        row.view(np.float64)[_COL["t_const"]] = float(c0)
+        row.view(np.float64)[_COL["logcount"]] = float(np.float32(np.log(n)))
+        self.row = row
 
     def nbytes(self):
         return self.f32.numel() * 4 + self.f64.numel() * 8 + self.fail.numel() * 8
@@ -288,31 +295,27 @@ class GroupedServeLoop:
         return (isinstance(request.target, LinearRegressionTarget) and p.family == GAUSSIAN and
                 p.scale_kind == FACTOR and p.dtype == np.float32 and p.dimension <= 64)
 
-    def _table(self, runs):
-        t = np.zeros((len(runs), len(_RUN_FIELDS)), dtype=np.int64)
-        f = t.view(np.float64)
-        bn = ba = bm = 0
-        for k, g in enumerate(runs):
-            n_old = g.round * g.n
-            nall = n_old + g.n
-            row = t[k]
-            row[_COL["d"]], row[_COL["rounds"]], row[_COL["round"]] = g.d, g.R, g.round
-            row[_COL["n_round"]], row[_COL["n_old"]] = g.n, n_old
-            row[_COL["seed"]] = np.int64(np.uint64(g.request.seed & (2 ** 64 - 1)).view(np.int64))
-            row[_COL["normal_offset"]] = g.normal_offset
-            row[_COL["blk_new0"]], row[_COL["blk_all0"]], row[_COL["blk_mom0"]] = bn, ba, bm
-            nmom = _cdiv(nall, GROUP_MOMENT_SAMPLES)
-            row[_COL["nmom"]] = nmom
-            for name in ("samples", "logtargets", "lognum", "logweights", "loc", "fac", "lognorm", "cand_loc",
-                         "cand_fac", "cand_lognorm", "t_mode", "t_chol", "summaries", "mean", "cov", "failures",
-                         "partial", "mpartial"):
-                row[_COL[name]] = g.ptr[name]
-            f[k, _COL["t_const"]] = g.t_const
-            f[k, _COL["logcount"]] = float(np.float32(np.log(g.n)))
-            bn += _cdiv(g.n, GROUP_TILE)
-            ba += _cdiv(nall, GROUP_TILE)
-            bm += nmom
-        return t, bn, ba, bm
+    @staticmethod
+    def _table(runs):
+        """The step's descriptor table: the runs' fixed rows and, per run,
+        its round, retained count, normal-stream position and block offsets
+        (exclusive prefix sums of its block counts)."""
+        t = np.stack([g.row for g in runs])
+        rnd = np.array([g.round for g in runs], dtype=np.int64)
+        n = t[:, _COL["n_round"]]
+        d = t[:, _COL["d"]]
+        nall = (rnd + 1) * n
+        bn = -(-n // GROUP_TILE)
+        ba = -(-nall // GROUP_TILE)
+        bm = -(-nall // GROUP_MOMENT_SAMPLES)
+        t[:, _COL["round"]] = rnd
+        t[:, _COL["n_old"]] = rnd * n
+        # each round takes n d + 8 elements of the run's normal stream
+        t[:, _COL["normal_offset"]] = rnd * (n * d + 8)
+        for col, cnt in (("blk_new0", bn), ("blk_all0", ba), ("blk_mom0", bm)):
+            t[:, _COL[col]] = np.cumsum(cnt) - cnt
+        t[:, _COL["nmom"]] = bm
+        return t, int(bn.sum()), int(ba.sum()), int(bm.sum())
 
     def run(self, requests, clock=time.perf_counter):
         pending = sorted(requests, key=lambda r: r.arrival)
@@ -361,7 +364,6 @@ class GroupedServeLoop:
                 steps.append((ev, host, dev))
                 still = []
                 for g in active:
-                    g.normal_offset += g.n * g.d + 8
                     g.round += 1
                     if g.round == g.R:
                         finishing.append((g, ev))

@@ -57,18 +57,28 @@ class _Bound:
         self.target, self.struct, self.keep = target, struct, (ta, tb)
         self.operands = {}  # tensor-core operand form of a regression target, per precision
 
+    def tensor_operand(self, precision, dtype, device):
+        """The observations' tensor-core operand form when this target runs
+        its X beta on the tensor cores at `precision` for samples of `dtype`
+        (a regression target, a reduced-precision form, FP32, d <= 64), built
+        once per precision; else None (the SIMT kernel)."""
+        prec = native.PREC_NATIVE if precision is None else int(precision)
+        s = self.struct
+        if not (prec != native.PREC_NATIVE and s.kind in (native.TARGET_LINREG, native.TARGET_LOGISTIC)
+                and dtype == torch.float32 and s.dtype == native.F32 and s.dim <= 64):
+            return None
+        if prec not in self.operands:
+            self.operands[prec] = ops.glm_operand(s, prec, device)
+        return self.operands[prec]
+
     def evaluate(self, samples, out=None, precision=None):
         """The regression targets run their X beta on the tensor cores in the
         reduced-precision forms (FP32 samples, d <= 64); every other case is
         the SIMT kernel in the target's type."""
-        prec = native.PREC_NATIVE if precision is None else int(precision)
-        s = self.struct
-        if (prec != native.PREC_NATIVE and s.kind in (native.TARGET_LINREG, native.TARGET_LOGISTIC)
-                and samples.dtype == torch.float32 and s.dtype == native.F32 and s.dim <= 64):
-            if prec not in self.operands:
-                self.operands[prec] = ops.glm_operand(s, prec, samples.device)
-            return ops.glm_logdensity(s, prec, self.operands[prec], samples, out)
-        return ops.target_logdensity(s, samples, out)
+        operand = self.tensor_operand(precision, samples.dtype, samples.device)
+        if operand is not None:
+            return ops.glm_logdensity(self.struct, int(precision), operand, samples, out)
+        return ops.target_logdensity(self.struct, samples, out)
 
 
 class _BoundBank:

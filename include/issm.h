@@ -588,6 +588,10 @@ int issm_glm_logdensity(const issm_target *target, int32_t precision,
  * (issm_tc_workspace_bytes(rounds, d), rounded up to 256 bytes), the moments
  * scratch (issm_moments_workspace_bytes(total, d), rounded up) and the
  * reduction scratch; the first two end in their sticky timeout words.
+ * target_operand, when not NULL, is the regression target's operand form
+ * (issm_glm_prepare for target_precision) and the target runs through
+ * issm_glm_logdensity, its timeout word shared with the tensor-core
+ * scratch's; NULL runs issm_target_logdensity (SIMT, the target's type).
  * ISSM_E_UNSUPPORTED for Student-t or non-factor histories. */
 typedef struct issm_amis_run_desc {
     issm_bank history;
@@ -608,11 +612,13 @@ typedef struct issm_amis_run_desc {
     void *cand_location, *cand_factor, *cand_lognormalizer;  /* the last round's fit */
     void *workspace;
     size_t workspace_bytes;
+    const void *target_operand;      /* issm_glm_prepare output, or NULL */
+    int32_t target_precision, reserved;
 } issm_amis_run_desc;
 size_t issm_amis_run_workspace_bytes(int32_t d, int64_t total, int32_t rounds);
 int issm_amis_run(const issm_amis_run_desc *run, issm_stream_t stream);
-/* sizeof(issm_amis_run_desc) and the offset of its last field, for bindings
- * that mirror the struct (checked by the CPU tests). */
+/* sizeof(issm_amis_run_desc) and the offset of its workspace_bytes field,
+ * for bindings that mirror the struct (checked by the CPU tests). */
 size_t issm_amis_run_desc_bytes(void);
 size_t issm_amis_run_desc_workspace_offset(void);
 

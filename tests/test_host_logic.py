@@ -156,3 +156,40 @@ def test_serve_footprint_grows_with_the_run(issm):
     assert req(16, 4, 1000).footprint() > a
     assert req(8, 8, 1000).footprint() > a
     assert req(8, 4, 1000).footprint() >= 4 * 1000 * 8 * 4  # at least the retained samples
+
+
+def test_grouped_table_offsets_and_layout(issm):
+    """The grouped serving step's descriptor table: 31 eight-byte fields in
+    issm_group_run order (the library's own size), each run's block ranges
+    the exclusive prefix sums of its block counts, its retained count and
+    normal-stream position set by its round, and the fixed fields left as
+    admitted."""
+    sv = issm.serving
+    assert len(sv._RUN_FIELDS) * 8 == issm.native.lib().issm_group_run_bytes()
+
+    class Fake:
+        def __init__(self, d, n, rnd):
+            self.row = np.zeros(len(sv._RUN_FIELDS), dtype=np.int64)
+            self.row[sv._COL["d"]], self.row[sv._COL["n_round"]], self.row[sv._COL["rounds"]] = d, n, 4
+            self.row[sv._COL["samples"]] = 1000 + d
+            self.row.view(np.float64)[sv._COL["t_const"]] = -1.5
+            self.round = rnd
+
+    runs = [Fake(5, 300, 0), Fake(64, 128, 2), Fake(2, 5000, 3)]
+    t, bn, ba, bm = sv.GroupedServeLoop._table(runs)
+    col = sv._COL
+    assert t.shape == (3, len(sv._RUN_FIELDS))
+    assert list(t[:, col["round"]]) == [0, 2, 3]
+    assert list(t[:, col["n_old"]]) == [0, 256, 15000]
+    assert list(t[:, col["normal_offset"]]) == [0, 2 * (128 * 64 + 8), 3 * (5000 * 2 + 8)]
+    new = [3, 1, 40]
+    alln = [3, 3, 157]          # ceil(300 / 128), ceil(384 / 128), ceil(20000 / 128)
+    mom = [1, 1, 10]            # ceil(n_all / 2048)
+    assert list(t[:, col["blk_new0"]]) == [0, 3, 4] and bn == sum(new)
+    assert list(t[:, col["blk_all0"]]) == [0, 3, 6] and ba == sum(alln)
+    assert list(t[:, col["blk_mom0"]]) == [0, 1, 2] and bm == sum(mom)
+    assert list(t[:, col["nmom"]]) == mom
+    assert list(t[:, col["samples"]]) == [1005, 1064, 1002]
+    assert np.all(t.view(np.float64)[:, col["t_const"]] == -1.5)
+    # the fixed rows are not modified by building a table
+    assert runs[1].row[col["round"]] == 0
