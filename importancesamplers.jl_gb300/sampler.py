@@ -359,20 +359,28 @@ def _graph_eligible(s):
 
 def _run_moment(s):
     is_npmc = isinstance(s.algorithm, NPMC)
+    # an eligible AMIS run is issued by one issm_amis_run call (the same
+    # library calls as the round loop, bitwise the same results)
+    if not is_npmc and native_body_eligible(s):
+        def body():
+            _native_body(s)
+    else:
+        def body():
+            _moment_body(s, is_npmc)
     if _graph_eligible(s) and s.calls >= 1:
         if s.graph is None:
             g = torch.cuda.CUDAGraph()
             torch.cuda.synchronize(s.device)
             l0 = native.lib().issm_kernel_launches()
             with torch.cuda.graph(g):
-                _moment_body(s, is_npmc)
+                body()
             s.graph_launches = int(native.lib().issm_kernel_launches() - l0)
             native.note_replay(-s.graph_launches)  # captured, not run
             s.graph = g
         s.graph.replay()
         native.note_replay(s.graph_launches)
     else:
-        _moment_body(s, is_npmc)
+        body()
     return _finish_moment(s, is_npmc)
 
 
