@@ -283,9 +283,18 @@ def fit_factor(mean, cov, previous_factor, out_location, out_factor, out_lognorm
                 native.ptr(out_lognorm), native.ptr(out_inverse), native.ptr(failures), int(failure_index), _s())
 
 
+def _same_dtype(x, logweights):
+    """The statistics kernels read the values and the log weights in one
+    type: when they differ, both are read in FP64."""
+    if x.dtype != logweights.dtype:
+        x, logweights = x.double(), logweights.double()
+    return x.contiguous(), logweights.contiguous()
+
+
 def weighted_sum(x, logweights, summary, out=None):
     """sum_i w_i x_i per column (FP64) with the self-normalised weights of
     the summary; x is (n,) or (n, d)."""
+    x, logweights = _same_dtype(x, logweights)
     n = x.shape[0]
     d = x.shape[1] if x.dim() == 2 else 1
     out = torch.empty(d, dtype=torch.float64, device=x.device) if out is None else out
@@ -298,6 +307,7 @@ def weighted_sum(x, logweights, summary, out=None):
 
 def weighted_quantile(x, logweights, summary, probabilities):
     """Component-wise weighted quantiles: (len(probabilities), d) FP64."""
+    x, logweights = _same_dtype(x, logweights)
     n = x.shape[0]
     d = x.shape[1] if x.dim() == 2 else 1
     probs = torch.tensor([float(p) for p in probabilities], dtype=torch.float64, device=x.device)
