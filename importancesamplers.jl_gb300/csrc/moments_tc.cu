@@ -1,19 +1,19 @@
 // moments_tc.cu — tensor-core form of the weighted moments that drive AMIS /
 // N-PMC adaptation (_weighted_moments!, src/adaptive_gaussian_execution.jl:268-273).
 //
-// One streaming pass over the retained samples. For a tile of 128 samples the
-// operand A is 128 rows x 128 samples: rows 0..d-1 hold sqrt(w) (x - c)
-// (c = previous proposal mean), row 64 holds sqrt(w), with the samples along
-// K; A A^T then holds S2 = sum w z z^T (rows/cols 0..63), S1 = sum w z
-// (row 64) and S0 = sum w (D[64][64]). A is split A = Ah + Al in bf16 and
-// two accumulators in tensor memory, H += Ah Ah^T + Al Al^T and X += Al Ah^T,
-// give S = H + X + X^T = (Ah + Al)(Ah + Al)^T (each CTA stores P = H / 2 + X,
-// and S = P + P^T since H is symmetric):
-// the Gram matrix of the split operand (about 16 significant bits per
-// element), so the covariance (its Schur complement) is positive semidefinite
-// up to FP32 accumulation however few samples carry the weight, and the
-// regularising ridge keeps the fit positive definite. The third MMA per K
-// slice costs nothing measurable: the pass is bound by HBM.
+// One streaming pass over the retained samples. For a tile of 128 samples,
+// v = sqrt(w) (x - c) (c = previous proposal mean) is split v = vh + vl into
+// bf16 parts, and so is sqrt(w) = sh + sl. One MMA per 16-sample K slice
+// accumulates, in tensor memory, D = A B^T with A = [vh; vl] (M = 128 rows:
+// 64 hi, 64 lo) and B = [vh; vl; sh; sl] (N = 144): all four hi/lo blocks of
+// (vh + vl)(vh + vl)^T and the products with sh, sl. The epilogue adds them:
+// S2 = sum w z z^T, S1 = sum w z of the split operand, and the converters sum
+// S0 = sum (sh + sl)^2 the same way, so [S2 S1; S1^T S0] is the Gram matrix
+// of the split operand (about 16 significant bits per element): the
+// covariance, its Schur complement, is positive semidefinite up to FP32
+// accumulation however few samples carry the weight, and the regularising
+// ridge keeps the fit positive definite. Each CTA stores P = S / 2; the
+// reduce kernel forms S = P + P^T.
 //
 // When the new mean lies far from c relative to the spread, S2/S0 and the
 // mean's outer product nearly cancel. A second pass centred at the first
@@ -23,19 +23,20 @@
 // return at once when the flag is clear.
 //
 // A is stored MN-major: each sample's 8-coordinate groups are 16-byte chunks,
-// so two threads convert a sample row straight from the staged tile. Warp
-// roles: warp 0 issues the MMAs; warps 1..16 build A (double-buffered) from
-// the staged tiles; warp 17 stages the tiles. For d = 32 or 64 (aligned
-// arrays) the stager keeps a four-deep ring of stages filled by tensor copies
+// so four threads convert a sample row straight from the staged tile. Warp
+// roles: warp 0 issues the MMAs; warps 1..16 build the operand (three
+// buffers, so conversion runs up to two tiles ahead of the MMAs) from the
+// staged tiles; warp 17 stages the tiles. For d = 32 or 64 (aligned arrays)
+// the stager keeps a three-deep ring of stages filled by tensor copies
 // (cp.async.bulk.tensor through a tensor map of the samples: one or two
 // 32-float x 128-row boxes per tile, 128-byte swizzle, so converters read
 // rows without bank conflicts, plus one bulk copy of the tile's log weights;
 // completion counted in bytes on the stage's mbarrier); converters wait on
 // that mbarrier and release the stage with one arrival per warp, so no role
 // ever waits on a CTA-wide barrier. Other shapes stage padded rows with
-// 4-byte cp.async from the converters. Per-CTA partials are summed across
-// CTAs (compensated FP32) and mean = c + S1/S0, cov = S2/S0 - (S1/S0)(S1/S0)^T
-// in FP64.
+// cp.async from the converters. Per-CTA partials are summed across CTAs
+// (compensated FP32) and mean = c + S1/S0, cov = S2/S0 - (S1/S0)(S1/S0)^T in
+// FP64.
 #include <cstring>
 
 #include "issm_device.cuh"
@@ -55,25 +56,27 @@ constexpr int kMtTile = 128;   // samples per tile = MMA K extent per tile
 constexpr int kMtTPR = kMtConvThreads / kMtTile;  // converter threads per sample row
 constexpr int kMtGPT = 8 / kMtTPR;                // coordinate groups (of 8) per converter thread
 constexpr int kMtCtasPerSm = 1;  // CTAs per SM (two 64-sample pipelines measured the same)
-constexpr int kMtCols = 80;    // MMA N (64 coordinates + sqrt(w) + padding)
-constexpr int kMtStages = 4;   // staged sample tiles in flight
+constexpr int kMtCols = 80;    // columns of a CTA's partial (64 coordinates, sqrt(w), padding)
+constexpr int kMtN = 144;      // MMA N: hi rows, lo rows, sqrt(w) hi and lo, padding
+constexpr int kMtStages = 3;   // staged sample tiles in flight
+constexpr int kMtABufs = 3;    // operand buffers: conversion runs up to two tiles ahead of the MMAs
 constexpr int kMtRS = 68;      // padded row of a staged tile (floats): conflict-free row reads
 constexpr int kMtWOff = kMtTile * kMtRS * 4;  // byte offset of the tile's log weights in a stage
 // rows (padded, or two swizzled boxes), then the log weights; a 1024-byte multiple
 constexpr int kMtRawBytes = (kMtWOff + kMtTile * 4 + 1023) / 1024 * 1024;
-// Rows 0..71 (9 row groups: 64 coordinates, sqrt(w), zeros) are stored; the
-// MMA's M = 128 also reads row groups 9..15, which land in the next buffer or
-// the staged tiles after A: those D rows and the matching columns >= 72 are
-// never read, so their content does not matter.
-constexpr int kMtGroups = 9;
-constexpr int kMtPart = kMtGroups * kMtTile * 16;
-// A buffers, stages (1024-byte multiples: the swizzled boxes need 1024-byte
+// One operand buffer holds 18 row groups of 128 samples x 16 bytes, MN-major:
+// groups 0..7 the bf16 hi parts of the 64 coordinates, groups 8..15 their lo
+// parts, group 16 (sqrt(w) hi, sqrt(w) lo, zeros) and group 17 zeros. A is
+// its first 16 groups (M = 128), B all 18 (N = 144).
+constexpr int kMtGroups = 18;
+constexpr int kMtBuf = kMtGroups * kMtTile * 16;
+// operand buffers, stages (1024-byte multiples: the swizzled boxes need 1024-byte
 // aligned destinations), centre; plus 1024 bytes to align the base
-constexpr size_t kMtSmem = (size_t)2 * 2 * kMtPart + (size_t)kMtStages * kMtRawBytes + 256 + 1024;
-static_assert((size_t)3 * kMtPart + (size_t)16 * kMtTile * 16 <= kMtSmem, "M = 128 reads stay inside the CTA's shared memory");
-static_assert(kMtSmem <= 232448 - 1024, "dynamic shared memory per CTA");
-static_assert((2 * 2 * kMtPart) % 1024 == 0 && kMtRawBytes % 1024 == 0, "stages start on 1024-byte boundaries");
-constexpr int kMtPartial = 65 * kMtCols;  // P = H / 2 + X of one CTA (S = P + P^T: H is symmetric)
+constexpr size_t kMtSmem = (size_t)kMtABufs * kMtBuf + (size_t)kMtStages * kMtRawBytes + 256 + 1024;
+static_assert(kMtSmem <= 232448 - 2048, "dynamic shared memory per CTA");
+static_assert(kMtBuf % 1024 == 0 && kMtRawBytes % 1024 == 0, "stages start on 1024-byte boundaries");
+static_assert(128 * 65 * 4 <= kMtRawBytes, "the epilogue's row sums fit in one stage");
+constexpr int kMtPartial = 65 * kMtCols;  // P = S / 2 of one CTA (the reduce forms S = P + P^T)
 
 __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(const float *__restrict__ x, int d, int64_t n,
                                                                     const float *__restrict__ lw,
@@ -87,16 +90,17 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     // the swizzled boxes need 1024-byte aligned stages
     unsigned char *smem = smem_raw + ((1024 - (tc::smem_u32(smem_raw) & 1023)) & 1023);
-    unsigned char *s_a = smem;                                    // [buf][part] x kMtPart
-    unsigned char *s_raw = smem + (size_t)2 * 2 * kMtPart;
+    unsigned char *s_a = smem;                                    // [buf] x kMtBuf
+    unsigned char *s_raw = smem + (size_t)kMtABufs * kMtBuf;
     float *s_c = reinterpret_cast<float *>(s_raw + (size_t)kMtStages * kMtRawBytes);
-    __shared__ __align__(8) uint64_t a_full[2], a_empty[2], raw_full[kMtStages], raw_empty[kMtStages];
+    __shared__ __align__(8) uint64_t a_full[kMtABufs], a_empty[kMtABufs], raw_full[kMtStages], raw_empty[kMtStages];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_flag;
+    __shared__ float s_s0[kMtConvWarps];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) tc::tmem_alloc(&tmem_base, 256);
     if (tid == 0) {
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < kMtABufs; ++b) {
             tc::mbar_init(&a_full[b], kMtConvWarps);
             tc::mbar_init(&a_empty[b], 1);
         }
@@ -108,12 +112,18 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
         abort_flag = 0;
     }
     for (int c = tid; c < 64; c += kMtThreads) s_c[c] = c < d ? (float)center[c] : 0.f;
+    // group 17 of every buffer: zeros (B rows 136..143, never read back)
+    for (int e = tid; e < kMtABufs * kMtTile; e += kMtThreads)
+        *reinterpret_cast<uint4 *>(s_a + (size_t)(e / kMtTile) * kMtBuf + 17 * kMtTile * 16 + (e % kMtTile) * 16) =
+            make_uint4(0u, 0u, 0u, 0u);
+    if (tid < kMtConvWarps) s_s0[tid] = 0.f;
     const float m = (float)summary[0];
     const float inv_sqrt_s = (float)(1.0 / sqrt(summary[1]));
+    tc::fence_proxy_async();
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tbase = tmem_base;  // H at columns 0..79, X at 128..207
+    const uint32_t tbase = tmem_base;  // D: 128 lanes x 144 columns
     const int64_t ntiles = (n + kMtTile - 1) / kMtTile;
     const int my_tiles = (int)((ntiles - (int64_t)blockIdx.x + gridDim.x - 1) / gridDim.x);
     auto tile_of = [&](int it) -> int64_t { return (int64_t)blockIdx.x + (int64_t)it * gridDim.x; };
@@ -131,23 +141,20 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
     const int nbox = d > 32 ? 2 : 1;
 
     if (warp == 0) {
-        // ---- issuer: H += Ah Ah^T + Al Al^T, X += Al Ah^T per K slice ----
-        const uint32_t idesc = tc::instr_desc(tc::kBF16, 128, kMtCols) | tc::kMajorMN;
+        // ---- issuer: D += [Ah; Al] [Ah; Al; sqrt(w)]^T, one MMA per K slice ----
+        const uint32_t idesc = tc::instr_desc(tc::kBF16, 128, kMtN) | tc::kMajorMN;
         constexpr uint32_t LBO = 128, SBO = kMtTile * 16;  // K-group stride, row-group stride
         for (int it = 0; it < my_tiles; ++it) {
-            const int buf = it & 1;
+            const int buf = it % kMtABufs;
             if (lane == 0) {
-                const bool ok = wait(&a_full[buf], (uint32_t)((it >> 1) & 1));
+                const bool ok = wait(&a_full[buf], (uint32_t)((it / kMtABufs) & 1));
                 tc::fence_after_sync();
                 if (ok) {
-                    const uint32_t a0 = tc::smem_u32(s_a + (size_t)buf * 2 * kMtPart), a1 = a0 + kMtPart;
+                    const uint32_t a0 = tc::smem_u32(s_a + (size_t)buf * kMtBuf);
 #pragma unroll
                     for (int s = 0; s < kMtTile / 16; ++s) {
-                        const uint64_t dh = tc::smem_desc(a0 + s * 256, LBO, SBO);
-                        const uint64_t dl = tc::smem_desc(a1 + s * 256, LBO, SBO);
-                        tc::mma(tbase, dh, dh, idesc, it > 0 || s > 0);
-                        tc::mma(tbase + 128, dl, dh, idesc, it > 0 || s > 0);
-                        tc::mma(tbase, dl, dl, idesc, true);
+                        const uint64_t da = tc::smem_desc(a0 + s * 256, LBO, SBO);
+                        tc::mma(tbase, da, da, idesc, it > 0 || s > 0);
                     }
                 }
                 tc::commit(&a_empty[buf]);
@@ -187,9 +194,9 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                     tc::mbar_wait(&raw_full[it % kMtStages], (uint32_t)((it / kMtStages) & 1));
         }
     } else {
-        // ---- converters: build A = sqrt(w) (x - c) from the staged tiles ----
+        // ---- converters: build [Ah; Al; sqrt(w)] from the staged tiles ----
         const int ctid = tid - 32;
-        auto issue_raw = [&](int it) {  // 4-byte cp.async staging (shapes without bulk copies)
+        auto issue_raw = [&](int it) {  // cp.async staging (shapes without tensor copies)
             if (it < my_tiles) {
                 const int64_t row0 = tile_of(it) * kMtTile;
                 const int rows = tile_rows(it);
@@ -216,8 +223,9 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
         if (!bulk)
             for (int s = 0; s < kMtStages; ++s) issue_raw(s);
         const int k = ctid % kMtTile, part = ctid / kMtTile;
+        float s0 = 0.f;  // sum of (sqrt(w) hi + lo)^2 over this thread's samples: S0 of the split operand
         for (int it = 0; it < my_tiles; ++it) {
-            const int buf = it & 1, stage = it % kMtStages;
+            const int buf = it % kMtABufs, stage = it % kMtStages;
             bool ok = true;
             if (bulk) {
                 // every lane acquires the stage's bytes itself; the outcome is made warp-uniform
@@ -226,8 +234,8 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                 tc::cp_async_wait<kMtStages - 1>();
                 tc::named_sync(1, kMtConvThreads);
             }
-            if (it >= 2 && ok) {
-                if (lane == 0) ok = wait(&a_empty[buf], (uint32_t)(((it - 2) >> 1) & 1));
+            if (it >= kMtABufs && ok) {
+                if (lane == 0) ok = wait(&a_empty[buf], (uint32_t)(((it / kMtABufs) - 1) & 1));
                 ok = __shfl_sync(0xffffffffu, (int)ok, 0) != 0;
             }
             if (ok) {
@@ -238,8 +246,7 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                     return reinterpret_cast<const float4 *>(bulk ? tc::swizzled_row_chunk(stage_p, k, c)
                                                                  : raw + k * kMtRS + c);
                 };
-                unsigned char *ah = s_a + (size_t)buf * 2 * kMtPart;
-                unsigned char *al = ah + kMtPart;
+                unsigned char *ab = s_a + (size_t)buf * kMtBuf;
                 const int64_t i = tile_of(it) * kMtTile + k;
                 const bool active = i < n;
                 // the bulk copy carries whole 16-byte groups of weights; the
@@ -287,15 +294,18 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
                     };
                     const uint4 lo = make_uint4(lo2(v[0], v[1], hi.x), lo2(v[2], v[3], hi.y), lo2(v[4], v[5], hi.z),
                                                 lo2(v[6], v[7], hi.w));
-                    *reinterpret_cast<uint4 *>(ah + (size_t)g * kMtTile * 16 + k * 16) = hi;
-                    *reinterpret_cast<uint4 *>(al + (size_t)g * kMtTile * 16 + k * 16) = lo;
+                    *reinterpret_cast<uint4 *>(ab + (size_t)g * kMtTile * 16 + k * 16) = hi;
+                    *reinterpret_cast<uint4 *>(ab + (size_t)(8 + g) * kMtTile * 16 + k * 16) = lo;
                 }
                 if (part == kMtTPR - 1) {
-                    // row group 8: sqrt(w) in row 64
+                    // group 16: sqrt(w) hi in row 128, its lo part in row 129
                     const uint32_t h = tc::pack_bf16x2(sw, 0.f);
-                    const uint32_t lo = tc::pack_bf16x2(sw - __uint_as_float(h << 16), 0.f);
-                    *reinterpret_cast<uint4 *>(ah + (size_t)8 * kMtTile * 16 + k * 16) = make_uint4(h, 0u, 0u, 0u);
-                    *reinterpret_cast<uint4 *>(al + (size_t)8 * kMtTile * 16 + k * 16) = make_uint4(lo, 0u, 0u, 0u);
+                    const float swh = __uint_as_float(h << 16);
+                    const uint32_t hl = tc::pack_bf16x2(swh, sw - swh);
+                    const float swl = __uint_as_float(hl & 0xffff0000u);
+                    const float sws = swh + swl;  // exact: swl is a bf16 below swh's last bit
+                    s0 = fmaf(sws, sws, s0);
+                    *reinterpret_cast<uint4 *>(ab + (size_t)16 * kMtTile * 16 + k * 16) = make_uint4(hl, 0u, 0u, 0u);
                 }
             }
             tc::fence_proxy_async();
@@ -309,13 +319,16 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
             }
         }
         if (!bulk) tc::cp_async_wait_all();
+        // S0 per warp in a fixed order (lanes by xor tree, warps summed in order below)
+        for (int off = 16; off > 0; off >>= 1) s0 += __shfl_xor_sync(0xffffffffu, s0, off);
+        if (lane == 0) s_s0[warp - 1] = s0;
     }
     // ---- the last commit tracks every MMA of the CTA ----
     tc::fence_before_sync();
     __syncthreads();
     if (my_tiles > 0) {
         const int last = my_tiles - 1;
-        if (!tc::mbar_wait(&a_empty[last & 1], (uint32_t)((last >> 1) & 1)) && tid == 0) {
+        if (!tc::mbar_wait(&a_empty[last % kMtABufs], (uint32_t)((last / kMtABufs) & 1)) && tid == 0) {
             atomicExch(error, 1);
             abort_flag = 1;
         }
@@ -323,21 +336,41 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
     __syncthreads();
     tc::fence_after_sync();
     float *out = partial + (size_t)blockIdx.x * kMtPartial;
+    // row sums T[r][j] = D[r][j] + D[r][64 + j] (j < 64) and T[r][64] =
+    // D[r][128] + D[r][129] in the first stage's space (every copy has landed)
+    float *T = reinterpret_cast<float *>(s_raw);
     // warps 1..4 read TMEM lane quadrants 1, 2, 3, 0 (a warp reads quadrant warp % 4)
     if (!abort_flag && warp >= 1 && warp <= 4) {
         const int q = warp & 3, row = 32 * q + lane;
+        const uint32_t lane_base = tbase + ((uint32_t)(32 * q) << 16);
 #pragma unroll
-        for (int c0 = 0; c0 < kMtCols; c0 += 16) {
-            float h[16], xv[16];
+        for (int c0 = 0; c0 < 64; c0 += 16) {
+            float a[16], b[16];
             if (my_tiles > 0) {
-                tc::tmem_ld16(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, h);
-                tc::tmem_ld16(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(128 + c0), xv);
+                tc::tmem_ld16(lane_base + (uint32_t)c0, a);
+                tc::tmem_ld16(lane_base + (uint32_t)(64 + c0), b);
             } else {
-                for (int j = 0; j < 16; ++j) h[j] = xv[j] = 0.f;
+                for (int j = 0; j < 16; ++j) a[j] = b[j] = 0.f;
             }
-            if (row <= 64) {
-                for (int j = 0; j < 16; ++j) out[row * kMtCols + c0 + j] = fmaf(0.5f, h[j], xv[j]);
-            }
+            for (int j = 0; j < 16; ++j) T[row * 65 + c0 + j] = a[j] + b[j];
+        }
+        float a[16];
+        if (my_tiles > 0) tc::tmem_ld16(lane_base + 128u, a);
+        else for (int j = 0; j < 16; ++j) a[j] = 0.f;
+        T[row * 65 + 64] = a[0] + a[1];
+    }
+    __syncthreads();
+    // P = S / 2 over 65 x 80: S2 = T[i] + T[64 + i], S1 the sqrt(w) column, S0 from the converters
+    if (!abort_flag) {
+        float s0_all = 0.f;
+        for (int w = 0; w < kMtConvWarps; ++w) s0_all += s_s0[w];
+        for (int e = tid; e < kMtPartial; e += kMtThreads) {
+            const int r = e / kMtCols, c = e - r * kMtCols;
+            float v = 0.f;
+            if (r < 64 && c < 65) v = T[r * 65 + c] + T[(64 + r) * 65 + c];
+            else if (r == 64 && c < 64) v = T[c * 65 + 64] + T[(64 + c) * 65 + 64];
+            else if (r == 64 && c == 64) v = s0_all;
+            out[e] = 0.5f * v;
         }
     }
     tc::fence_before_sync();
@@ -345,7 +378,7 @@ __global__ void __launch_bounds__(kMtThreads, kMtCtasPerSm) moments_tc_kernel(co
     if (warp == 0) tc::tmem_dealloc(tbase, 256);
 }
 
-// Partials are [block][65][80] FP32 (P = H / 2 + X). Every CTA sums 32 entries
+// Partials are [block][65][80] FP32 (P = S / 2). Every CTA sums 32 entries
 // over the blocks (32 block-strided lanes per entry, coalesced); the last CTA
 // to finish (a device-scope counter, reset by that CTA) forms S = P + P^T and
 // from it mean = c + S1/S0 and cov = S2/S0 - (S1/S0)(S1/S0)^T in FP64, with c
