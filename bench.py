@@ -677,6 +677,22 @@ def run_serve(args):
                                          "max": float(lz.max())},
                       "posterior_mean_error_sd": {"p50": float(np.median(me)), "p90": float(np.percentile(me, 90)),
                                                   "max": float(me.max())}})
+    # CPU baseline: the FP64 oracle AMIS (OpenMP over samples) on a bounded
+    # sample of the same mix, with fed normals
+    from oracle import oracle as orc
+
+    cpu_reqs, _ = make(args.cpu_requests)
+    cpu_s, cpu_samples = 0.0, 0
+    for r in cpu_reqs:
+        t = r.target
+        tv = orc.TargetView(orc.TARGET_LINREG, r.proposal.dimension, j=t.X.shape[0], a=t.X, b=t.y, p0=t.sigma,
+                            p1=t.prior_var)
+        normals = np.random.default_rng(r.rid).standard_normal(r.rounds * r.round_size * r.proposal.dimension)
+        t0 = time.perf_counter()
+        orc.amis_run(tv, r.proposal.dimension, r.proposal.location, r.proposal.factor_matrix(),
+                     [r.round_size] * r.rounds, normals, regularization=float(np.sqrt(np.finfo(np.float32).eps)))
+        cpu_s += time.perf_counter() - t0
+        cpu_samples += r.rounds * r.round_size
     line = {"metric": "serving mix p50/p99 latency and weighted samples/s", "impl": "gb300",
             "workload": "Bayesian linear regression posteriors, d~U{2..64}, n_obs log-uniform 50-5000, "
                         "budget log-uniform 1k-100k, AMIS 4 rounds, Poisson arrivals; initial proposal the "
@@ -684,7 +700,11 @@ def run_serve(args):
             "serve_loop": args.serve_loop,
             "precision": ("fp32 (grouped SIMT kernels; FP64 moments and fit)" if grouped else
                           {"bf16": "bf16 (bf16 x3 split)", "tf32": "tf32", "fp32": "fp32"}[args.precision]),
-            "max_inflight": args.inflight, "sweep": sweep}
+            "max_inflight": args.inflight, "sweep": sweep,
+            "cpu_baseline": {"runs_per_s": len(cpu_reqs) / cpu_s, "samples_per_s": cpu_samples / cpu_s,
+                             "unit": "runs/s and weighted samples/s, back to back (no arrivals)",
+                             "cores": orc.num_threads(), "kind": "port",
+                             "sample": f"{len(cpu_reqs)} requests of the same mix, FP64 oracle AMIS on fed normals"}}
     print(json.dumps(line), flush=True)
 
 
@@ -705,6 +725,7 @@ def main():
     ap.add_argument("--requests", type=int, default=10_000, help="serve: requests per arrival rate")
     ap.add_argument("--rates", type=float, nargs="+", default=[1000.0, 5000.0, 20000.0],
                     help="serve: arrivals per second")
+    ap.add_argument("--cpu-requests", type=int, default=16, help="serve: requests in the CPU-baseline sample")
     ap.add_argument("--serve-loop", default="grouped", choices=["grouped", "streams"],
                     help="serve: grouped (one launch per phase per step for every in-flight run) or streams "
                          "(one issm_amis_run per run on its own stream)")

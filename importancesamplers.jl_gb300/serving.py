@@ -195,71 +195,87 @@ def _cdiv(a, b):
     return -(-a // b)
 
 
-class _GroupedRun:
-    """The device state of one admitted run: three allocations (FP32, FP64,
-    failure words) carved into the issm_group_run arrays, the initial
-    proposal and the target's constants written by one host-to-device copy,
-    and the run's fixed descriptor fields as one table row."""
+class _Prep:
+    """Host side of one grouped run, computed off the serving thread: the
+    target's exact mode-centred form from its sufficient statistics, the byte
+    layout of the run's single device allocation, and the bytes admission
+    writes (zeroed failure words, the target's mode and factor, the history's
+    slot 0)."""
 
-    # the FP32 block: what admission writes comes first (one contiguous copy
-    # covers the target's mode and factor and the history's slot 0)
-    _F32 = ("t_mode", "t_chol", "lognorm", "loc", "fac", "cand_loc", "cand_fac", "cand_lognorm", "samples",
-            "logtargets", "lognum", "logweights")
+    # 256-byte aligned slices of one allocation; the head (up to the end of
+    # slot 0 of the factors) is written by one host-to-device copy
+    _HEAD = (("failures", 8), ("t_mode", 4), ("t_chol", 4), ("lognorm", 4), ("loc", 4), ("fac", 4))
+    _REST = (("cand_loc", 4), ("cand_fac", 4), ("cand_lognorm", 4), ("samples", 4), ("logtargets", 4),
+             ("lognum", 4), ("logweights", 4), ("summaries", 8), ("mean", 8), ("cov", 8), ("partial", 8),
+             ("mpartial", 8))
 
-    def __init__(self, request, device, start):
+    def __init__(self, request):
         p, tgt = request.proposal, request.target
         d, R, n = p.dimension, request.rounds, request.round_size
-        self.request, self.start, self.round = request, start, 0
-        self.d, self.R, self.n = d, R, n
-        # the target's exact mode-centred form from its sufficient statistics
+        self.request, self.d, self.R, self.n = request, d, R, n
         X, y, s2, pv = tgt.X, tgt.y, tgt.sigma ** 2, tgt.prior_var
         A = X.T @ X / s2 + np.eye(d) / pv
         mode = np.linalg.solve(A, X.T @ y / s2)
         r = y - X @ mode
-        c0 = (-0.5 * len(y) * np.log(2 * np.pi * s2) - 0.5 * float(r @ r) / s2
-              - 0.5 * d * np.log(2 * np.pi * pv) - 0.5 * float(mode @ mode) / pv)
+        self.t_const = float(-0.5 * len(y) * np.log(2 * np.pi * s2) - 0.5 * float(r @ r) / s2
+                             - 0.5 * d * np.log(2 * np.pi * pv) - 0.5 * float(mode @ mode) / pv)
         U = np.linalg.cholesky(A).T  # A = U^T U, U upper
-        sizes = {"t_mode": d, "t_chol": d * d, "lognorm": R, "loc": R * d, "fac": R * d * d, "cand_loc": d,
-                 "cand_fac": d * d, "cand_lognorm": 1, "samples": R * n * d, "logtargets": R * n, "lognum": R * n,
-                 "logweights": R * n}
-        off, o = {}, 0
-        for k in self._F32:
-            off[k] = o
-            o += _cdiv(sizes[k], 64) * 64  # 256-byte aligned slices
-        self.f32 = torch.empty(o, dtype=torch.float32, device=device)
-        head = np.zeros(off["fac"] + d * d, dtype=np.float32)
-        head[off["t_mode"]:off["t_mode"] + d] = mode
-        head[off["t_chol"]:off["t_chol"] + d * d] = U.T.reshape(-1)  # U column-major
-        head[off["lognorm"]] = p.lognormalizer
-        head[off["loc"]:off["loc"] + d] = p.location
-        head[off["fac"]:off["fac"] + d * d] = p.factor_matrix().T.reshape(-1)  # L column-major
+        count = {"failures": 3 * R, "t_mode": d, "t_chol": d * d, "lognorm": R, "loc": R * d, "fac": R * d * d,
+                 "cand_loc": d, "cand_fac": d * d, "cand_lognorm": 1, "samples": R * n * d, "logtargets": R * n,
+                 "lognum": R * n, "logweights": R * n, "summaries": 3 * R, "mean": d, "cov": d * d,
+                 "partial": 3 * _cdiv(R * n, GROUP_TILE),
+                 "mpartial": GROUP_MOMENT_WORDS * _cdiv(R * n, GROUP_MOMENT_SAMPLES)}
+        self.off, o = {}, 0
+        for name, es in self._HEAD + self._REST:
+            self.off[name] = o
+            o += _cdiv(count[name] * es, 256) * 256
+        self.nbytes = o
+        head = np.zeros(self.off["fac"] + 4 * d * d, dtype=np.uint8)
+        f32 = head.view(np.float32)
+
+        def put(name, values):
+            a = self.off[name] // 4
+            f32[a:a + values.size] = values
+
+        put("t_mode", mode.astype(np.float32))
+        put("t_chol", np.ascontiguousarray(U.T, dtype=np.float32).reshape(-1))  # U column-major
+        put("lognorm", np.array([p.lognormalizer], dtype=np.float32))
+        put("loc", np.asarray(p.location, dtype=np.float32))
+        put("fac", np.ascontiguousarray(p.factor_matrix().T, dtype=np.float32).reshape(-1))  # L column-major
+        self.head = head
+
+
+class _GroupedRun:
+    """The device state of one admitted run: one allocation carved into the
+    issm_group_run arrays, its head written by one asynchronous copy from
+    pinned memory, and the run's fixed descriptor fields as one table row."""
+
+    def __init__(self, prep, device, start):
+        self.prep, self.request, self.start, self.round = prep, prep.request, start, 0
+        self.d, self.R, self.n = prep.d, prep.R, prep.n
+        self.buf = torch.empty(prep.nbytes, dtype=torch.uint8, device=device)
         # pinned (cached host allocator) and asynchronous: admission never waits for the device
-        self.f32[:head.size].copy_(torch.from_numpy(head).pin_memory(), non_blocking=True)
-        # FP64 block: summaries, mean, covariance, summary and moment partials
-        d64 = {"summaries": 3 * R, "mean": d, "cov": d * d, "partial": 3 * _cdiv(R * n, GROUP_TILE),
-               "mpartial": GROUP_MOMENT_WORDS * _cdiv(R * n, GROUP_MOMENT_SAMPLES)}
-        off64, o = {}, 0
-        for k, v in d64.items():
-            off64[k] = o
-            o += _cdiv(v, 32) * 32
-        self.f64 = torch.zeros(o, dtype=torch.float64, device=device)
-        self.fail = torch.zeros(3 * R, dtype=torch.int64, device=device)
-        self.off64 = off64
-        # the descriptor fields that never change
+        self.buf[:prep.head.size].copy_(torch.from_numpy(prep.head).pin_memory(), non_blocking=True)
+        base = self.buf.data_ptr()
         row = np.zeros(len(_RUN_FIELDS), dtype=np.int64)
-        row[_COL["d"]], row[_COL["rounds"]], row[_COL["n_round"]] = d, R, n
-        row[_COL["seed"]] = np.uint64(request.seed & (2 ** 64 - 1)).view(np.int64)
-        for k, v in off.items():
-            row[_COL[k]] = self.f32.data_ptr() + 4 * v
-        for k, v in off64.items():
-            row[_COL[k]] = self.f64.data_ptr() + 8 * v
-        row[_COL["failures"]] = self.fail.data_ptr()
-        row.view(np.float64)[_COL["t_const"]] = float(c0)
-        row.view(np.float64)[_COL["logcount"]] = float(np.float32(np.log(n)))
+        row[_COL["d"]], row[_COL["rounds"]], row[_COL["n_round"]] = self.d, self.R, self.n
+        row[_COL["seed"]] = np.uint64(self.request.seed & (2 ** 64 - 1)).view(np.int64)
+        for name, o in prep.off.items():
+            row[_COL[name]] = base + o
+        row.view(np.float64)[_COL["t_const"]] = prep.t_const
+        row.view(np.float64)[_COL["logcount"]] = float(np.float32(np.log(self.n)))
         self.row = row
 
     def nbytes(self):
-        return self.f32.numel() * 4 + self.f64.numel() * 8 + self.fail.numel() * 8
+        return self.prep.nbytes
+
+    def result_views(self):
+        """The bytes read back when the run finishes: failure words, the last
+        round's summary, the posterior mean."""
+        o = self.prep.off
+        s = o["summaries"] + 24 * (self.R - 1)
+        return [self.buf[o["failures"]:o["failures"] + 24 * self.R], self.buf[s:s + 24],
+                self.buf[o["mean"]:o["mean"] + 8 * self.d]]
 
 
 class GroupedServeLoop:
@@ -271,12 +287,15 @@ class GroupedServeLoop:
     descriptor row per run (its arrays, round, random-stream position and
     block offsets), copies the table to the device and issues seven kernels;
     runs of any dimension, budget and round share the launches. A request
-    joins at the next step once it has arrived and the memory budget allows;
-    a run that finished its last round is read back (its final summary,
-    posterior mean and failure words, one copy for every run that finished
-    at that step) and its memory returned. At most `lookahead` steps are in
-    flight, so admissions follow the device. A run's numbers depend only on
-    its own inputs and seed: alone and in any mix they are bitwise the same."""
+    joins at the next step once it has arrived and the memory budget allows
+    (its host preparation, the target's sufficient statistics, mode and
+    factor, runs on the serving thread: BLAS calls from several threads at
+    once oversubscribe the host's cores). A run that finished its last round
+    is read back asynchronously (failure words, final summary and posterior
+    mean, one copy for every run that finished at that step) and its memory
+    returned. At most `lookahead` steps are in flight, so admissions follow
+    the device. A run's numbers depend only on its own inputs and seed: alone
+    and in any mix they are bitwise the same."""
 
     def __init__(self, device="cuda", memory_budget=16 << 30, max_inflight=4096, lookahead=2):
         native.require()
@@ -323,32 +342,43 @@ class GroupedServeLoop:
             if not self.eligible(r):
                 raise ValueError(f"request {r.rid}: the grouped loop serves linear-regression targets with FP32 "
                                  "Gaussian factor proposals of d <= 64")
-        lib = native.lib()
+        native.lib()
         t0 = clock()
-        queue, active, finishing, results = [], [], [], []
+        queue, active, reading, results = [], [], [], []
+        preps = {}  # request id -> _Prep of the queue head held back by the memory budget
         steps = []  # (event, host table, device table) of steps in flight
         used, i = 0, 0
-        while i < len(pending) or queue or active or finishing:
+        while i < len(pending) or queue or active or reading:
             now = clock() - t0
             while i < len(pending) and pending[i].arrival <= now:
                 queue.append(pending[i])
                 i += 1
-            # retire runs whose last step has completed
-            if finishing:
-                done = [(g, ev) for g, ev in finishing if ev.query()]
-                if done:
-                    finishing = [(g, ev) for g, ev in finishing if not ev.query() or all(g is not h for h, _ in done)]
-                    results.extend(self._retire([g for g, _ in done], clock() - t0))
-                    used -= sum(g.nbytes() for g, _ in done)
+            # decode the read-backs that have landed
+            if reading:
+                landed = [x for x in reading if x[2].query()]
+                if landed:
+                    reading = [x for x in reading if all(x is not y for y in landed)]
+                    for runs, host, _ in landed:
+                        results.extend(self._decode(runs, host.numpy(), clock() - t0))
+                        used -= sum(g.nbytes() for g in runs)
             # admit in arrival order while the in-flight cap and the memory budget allow
             while queue and len(active) < self.max_inflight:
-                g = _GroupedRun(queue[0], self.device, clock() - t0)
-                if used + g.nbytes() > self.memory_budget and active:
-                    del g
+                request = queue[0]
+                if request.rid not in preps:
+                    try:
+                        preps[request.rid] = _Prep(request)
+                    except Exception as e:  # a target the preparation rejects fails alone
+                        queue.pop(0)
+                        results.append(ServeResult(request, np.full(request.proposal.dimension, np.nan),
+                                                   float("nan"), 0.0, clock() - t0, clock() - t0, e))
+                        continue
+                prep = preps[request.rid]
+                if used + prep.nbytes > self.memory_budget and (active or reading):
                     break
                 queue.pop(0)
-                active.append(g)
-                used += g.nbytes()
+                del preps[request.rid]
+                active.append(_GroupedRun(prep, self.device, clock() - t0))
+                used += prep.nbytes
             if active:
                 # at most `lookahead` steps in flight
                 while len(steps) >= self.lookahead:
@@ -357,42 +387,42 @@ class GroupedServeLoop:
                 host = torch.from_numpy(table).pin_memory()
                 dev = torch.empty_like(host, device=self.device)
                 dev.copy_(host, non_blocking=True)
-                native.call("issm_group_step", dev.data_ptr(), len(active), bn, ba, bm,
-                            self.stream.cuda_stream)
+                native.call("issm_group_step", dev.data_ptr(), len(active), bn, ba, bm, self.stream.cuda_stream)
                 ev = torch.cuda.Event()
                 ev.record(self.stream)
                 steps.append((ev, host, dev))
-                still = []
+                still, done = [], []
                 for g in active:
                     g.round += 1
-                    if g.round == g.R:
-                        finishing.append((g, ev))
-                    else:
-                        still.append(g)
+                    (done if g.round == g.R else still).append(g)
                 active = still
+                if done:
+                    reading.append(self._read_back(done))
             elif not queue and i < len(pending):
                 time.sleep(max(0.0, min(pending[i].arrival - (clock() - t0), 0.001)))
-            elif finishing:
+            elif reading:
                 time.sleep(0.0002)
         return results
 
-    def _retire(self, runs, now):
-        """One copy for every run that finished at a step: its failure words,
-        last summary and posterior mean (the last fit's moments over every
-        retained sample with the final weights)."""
-        parts = []
-        for g in runs:
-            s = g.off64["summaries"] + 3 * (g.R - 1)
-            parts += [g.fail.view(torch.float64), g.f64[s:s + 3], g.f64[g.off64["mean"]:g.off64["mean"] + g.d]]
-        packed = torch.cat(parts).cpu().numpy()
+    def _read_back(self, runs):
+        """Stream-ordered after the runs' last step: one gather and one
+        asynchronous copy into pinned memory for every run that finished."""
+        packed = torch.cat([v for g in runs for v in g.result_views()])
+        host = torch.empty(packed.numel(), dtype=torch.uint8, pin_memory=True)
+        host.copy_(packed, non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(self.stream)
+        return runs, host, ev
+
+    def _decode(self, runs, packed, now):
         out, o = [], 0
         for g in runs:
-            words = packed[o:o + 3 * g.R].view(np.int64).reshape(g.R, 3)
-            o += 3 * g.R
-            m, s, s2 = packed[o:o + 3]
-            o += 3
-            mean = packed[o:o + g.d].copy()
-            o += g.d
+            words = packed[o:o + 24 * g.R].view(np.int64).reshape(g.R, 3)
+            o += 24 * g.R
+            m, s, s2 = packed[o:o + 24].view(np.float64)
+            o += 24
+            mean = packed[o:o + 8 * g.d].view(np.float64).copy()
+            o += 8 * g.d
             error = None
             for t in range(g.R):
                 if words[t][0] != 0:

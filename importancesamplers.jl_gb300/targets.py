@@ -199,9 +199,13 @@ class LinearRegressionTarget(_NativeTarget):
         A = X.T @ X / s2 + np.eye(d) / pv
         b = X.T @ y / s2
         mean = np.linalg.solve(A, b)
-        cov_y = s2 * np.eye(n) + pv * X @ X.T
-        sign, logdet = np.linalg.slogdet(cov_y)
-        logz = -0.5 * (n * np.log(2 * np.pi) + logdet + y @ np.linalg.solve(cov_y, y))
+        # y ~ N(0, C), C = s2 I_n + pv X X^T, in d x d form: det C = s2^n
+        # pv^d det A (determinant lemma) and y^T C^-1 y = (y^T y - y^T X
+        # A^-1 X^T y / s2) / s2 (Woodbury)
+        L = np.linalg.cholesky(A)
+        logdet = n * np.log(s2) + d * np.log(pv) + 2.0 * np.sum(np.log(np.diag(L)))
+        quad = (y @ y - b @ mean * s2) / s2
+        logz = -0.5 * (n * np.log(2 * np.pi) + logdet + quad)
         return mean, logz
 
 
