@@ -698,7 +698,7 @@ def run_serve(args):
                         "budget log-uniform 1k-100k, AMIS 4 rounds, Poisson arrivals; initial proposal the "
                         "posterior's Laplace form displaced and widened by 0.5/sqrt(d) of its scale",
             "serve_loop": args.serve_loop,
-            "precision": ("fp32 (grouped SIMT kernels; FP64 moments and fit)" if grouped else
+            "precision": ("fp32 (grouped SIMT kernels; compensated FP32 moment sums, FP64 merge and fit)" if grouped else
                           {"bf16": "bf16 (bf16 x3 split)", "tf32": "tf32", "fp32": "fp32"}[args.precision]),
             "max_inflight": args.inflight, "sweep": sweep,
             "cpu_baseline": {"runs_per_s": len(cpu_reqs) / cpu_s, "samples_per_s": cpu_samples / cpu_s,

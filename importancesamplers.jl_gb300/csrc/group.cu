@@ -27,8 +27,8 @@
 //   group_form       log weights log pi - log mixture + log N_t and per-block
 //                    (max, S, S2) partials;
 //   group_summary    one block per run: the partials merged in order;
-//   group_moments    per-block FP64 sums of w (x - c) and w (x - c)(x - c)^T
-//                    about the previous location c;
+//   group_moments    per-block sums of w (x - c) and w (x - c)(x - c)^T about
+//                    the previous location c (compensated FP32, stored FP64);
 //   group_fit        one block per run: the sums merged in order, mean and
 //                    covariance, the ridge sqrt(eps(Float32)) tr(L L^T) / d,
 //                    an FP64 Cholesky and the next slot (or the candidate).
@@ -203,7 +203,12 @@ __global__ void group_summary_kernel(const GroupRun *__restrict__ runs) {
     o[2] = s2;
 }
 
-// per block of up to kGMomTiles tiles: FP64 S0, S1 = sum w (x - c), lower S2
+// per block of up to kGMomTiles tiles: S0, S1 = sum w (x - c) and the lower
+// S2 = sum w (x - c)(x - c)^T, each summed in compensated FP32 (Kahan) and
+// stored as FP64 for the fixed-order FP64 merge of the fit. FP64 arithmetic
+// here would run on this GPU's narrow FP64 pipe (a warp-instruction holds it
+// for about 16 SM cycles whatever the active lanes): two FP64 operations per
+// (entry, sample) made this kernel most of a serving step.
 __global__ void __launch_bounds__(256) group_moments_kernel(const GroupRun *__restrict__ runs, int nruns) {
     const int j = find_run(runs, nruns, blockIdx.x, 2);
     const GroupRun &R = runs[j];
@@ -213,14 +218,14 @@ __global__ void __launch_bounds__(256) group_moments_kernel(const GroupRun *__re
     const double *sum = R.summaries + 3 * t;
     const double m = sum[0], inv = 1.0 / sum[1];
     const float *c = R.loc + (size_t)t * d;
-    __shared__ double zt[32][65];
-    __shared__ double wt[32];
+    __shared__ float zt[32][65];
+    __shared__ float wt[32];
     const int tri = d * (d + 1) / 2;
     constexpr int kPer = 9;  // lower-triangle entries per thread (d <= 64: 2080 / 256 < 9)
-    double acc[kPer], s1 = 0.0, s0 = 0.0;
+    float acc[kPer], cmp[kPer], s1 = 0.f, c1 = 0.f, s0 = 0.f, c0 = 0.f;
     int er[kPer], ec[kPer];
     for (int u = 0; u < kPer; ++u) {
-        acc[u] = 0.0;
+        acc[u] = cmp[u] = 0.f;
         const int q = threadIdx.x + u * 256;
         int r = 0, cc = 0;
         if (q < tri) {
@@ -232,35 +237,42 @@ __global__ void __launch_bounds__(256) group_moments_kernel(const GroupRun *__re
         er[u] = r;
         ec[u] = cc;
     }
+    // Kahan step: sum += v with the running compensation
+    auto kahan = [](float &s, float &k, float v) {
+        const float y = v - k;
+        const float tt = s + y;
+        k = (tt - s) - y;
+        s = tt;
+    };
     const int64_t i0 = mb * kGMomTiles * kGTile, i1 = min(ntot, i0 + (int64_t)kGMomTiles * kGTile);
     for (int64_t s0i = i0; s0i < i1; s0i += 32) {
         const int rows = (int)min((int64_t)32, i1 - s0i);
         __syncthreads();
         for (int e = threadIdx.x; e < rows * d; e += blockDim.x) {
             const int r = e / d, cc = e - r * d;
-            zt[r][cc] = (double)R.samples[(s0i + r) * d + cc] - (double)c[cc];
+            zt[r][cc] = R.samples[(s0i + r) * d + cc] - c[cc];
         }
         for (int r = threadIdx.x; r < rows; r += blockDim.x) {
             const double l = (double)R.logweights[s0i + r];
-            wt[r] = l == -INFINITY ? 0.0 : exp(l - m) * inv;
+            wt[r] = l == -INFINITY ? 0.f : (float)(exp(l - m) * inv);
         }
         __syncthreads();
         for (int r = 0; r < rows; ++r) {
-            const double w = wt[r];
-            if (w == 0.0) continue;
+            const float w = wt[r];
+            if (w == 0.f) continue;
 #pragma unroll
             for (int u = 0; u < kPer; ++u)
-                if (threadIdx.x + u * 256 < tri) acc[u] += w * zt[r][er[u]] * zt[r][ec[u]];
-            if (threadIdx.x < d) s1 += w * zt[r][threadIdx.x];
-            if (threadIdx.x == 0) s0 += w;
+                if (threadIdx.x + u * 256 < tri) kahan(acc[u], cmp[u], w * zt[r][er[u]] * zt[r][ec[u]]);
+            if (threadIdx.x < d) kahan(s1, c1, w * zt[r][threadIdx.x]);
+            if (threadIdx.x == 0) kahan(s0, c0, w);
         }
     }
     double *out = R.mpartial + (size_t)mb * kMomWords;
-    if (threadIdx.x == 0) out[0] = s0;
-    if (threadIdx.x < d) out[1 + threadIdx.x] = s1;
+    if (threadIdx.x == 0) out[0] = (double)s0 - (double)c0;
+    if (threadIdx.x < d) out[1 + threadIdx.x] = (double)s1 - (double)c1;
 #pragma unroll
     for (int u = 0; u < kPer; ++u)
-        if (threadIdx.x + u * 256 < tri) out[1 + 64 + threadIdx.x + u * 256] = acc[u];
+        if (threadIdx.x + u * 256 < tri) out[1 + 64 + threadIdx.x + u * 256] = (double)acc[u] - (double)cmp[u];
 }
 
 // one block per run: merge the moment partials, mean and covariance, ridge,

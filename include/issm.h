@@ -630,8 +630,9 @@ size_t issm_amis_run_desc_workspace_offset(void);
  * run of a device table of issm_group_run rows by one AMIS round with seven
  * launches in all, however many runs: draws from the counter-based normal
  * stream, the linear-regression target in its mode-centred quadratic form,
- * the retrospective mixture, weights and their summary, FP64 moment sums
- * about the previous location, and the FP64 fit of the next proposal. Gaussian
+ * the retrospective mixture, weights and their summary, moment sums about the
+ * previous location (compensated FP32 per block, merged in FP64), and the FP64
+ * fit of the next proposal. Gaussian
  * factor proposals, FP32 samples, d <= 64, one sample count per round per
  * run. Rows are ordered by their block offsets: blk_new0 (ceil(n_round /
  * ISSM_GROUP_TILE) blocks per run), blk_all0 (ceil((n_old + n_round) /
