@@ -141,25 +141,29 @@ constexpr int kFirstEpiWarp = 1 + kConvWarps;
 constexpr int kTcThreads = 32 * (1 + kConvWarps + kEpiWarps);
 constexpr int kBRing = 3;      // operand buffers in flight when a tile needs several chunks
 
-template <int KIND, int SPLIT, int DP, bool DIRECT>
+// NOB: one component centred at its own location, whose offset column
+// -W (mu - c) is therefore zero: the MMAs run over the coordinates' K groups
+// only (K = DP instead of DP + 16), and three A buffers fit.
+template <int KIND, int SPLIT, int DP, bool DIRECT, bool NOB>
 __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     constexpr int EB = KIND == tc::kBF16 ? 2 : 4;
     constexpr int PER = 16 / EB;              // elements per 16-byte K group
     constexpr int KG = DP / PER;              // K groups of the sample coordinates
-    constexpr int KGX = KG + 2;               // plus the constant-1 column and padding
+    constexpr int KGB = KG + 2;               // operand form: plus the offset column and padding
+    constexpr int KGX = NOB ? KG : KGB;       // K groups the MMAs read
     constexpr int QH = KG / 2;                // K groups converted per thread (two threads per row)
     constexpr int NPART = SPLIT == 3 ? 2 : 1;
     constexpr int RS = DP + 4;                // padded raw row (floats): conflict-free row reads
     constexpr int RAW_BYTES = kTcTile * RS * 4;
     constexpr int A_PART = kTcTile * KGX * 16;
-    constexpr int B_COMP = DP * KGX * 16;
+    constexpr int B_COMP = DP * KGB * 16;
     constexpr int KSTEPS = KGX / 2;           // MMA K slices of 32 bytes
     constexpr uint32_t LBO_A = kTcTile * 16;
     const int chunk = p.chunk, nchunks = p.nchunks, S = p.raw_stages;
     // one component chunk: A double-buffered, the chunk's operands loaded once;
     // several chunks: one A buffer (a tile is converted once per nchunks items)
     // and a ring of kBRing operand buffers filled kBRing - 1 items ahead
-    const int nbufA = nchunks > 1 ? 1 : 2;
+    const int nbufA = nchunks > 1 ? 1 : NOB ? 3 : 2;
     const int nbufB = nchunks > 1 ? p.bring : 1;
     const uint32_t LBO_B = (uint32_t)(chunk * DP * 16);
     const uint32_t CHUNK_BYTES = (uint32_t)(NPART * chunk * B_COMP);
@@ -169,7 +173,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     unsigned char *s_a = s_raw + (size_t)S * RAW_BYTES;
     unsigned char *s_b = s_a + (size_t)nbufA * NPART * A_PART;
     float *s_c = reinterpret_cast<float *>(s_b + (size_t)nbufB * CHUNK_BYTES);
-    __shared__ __align__(8) uint64_t a_full[2], a_empty[2], b_full[kBRing], b_empty[kBRing], d_full[2], d_empty[2];
+    __shared__ __align__(8) uint64_t a_full[3], a_empty[3], b_full[kBRing], b_empty[kBRing], d_full[2], d_empty[2];
     __shared__ uint32_t tmem_base;
     __shared__ volatile int abort_flag;
 
@@ -178,9 +182,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     const uint32_t ncols = 2 * NW <= 32 ? 32 : 2 * NW <= 64 ? 64 : 2 * NW <= 128 ? 128 : 2 * NW <= 256 ? 256 : 512;
     if (warp == 0) tc::tmem_alloc(&tmem_base, ncols);
     if (tid == 0) {
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < 3; ++b) {
             tc::mbar_init(&a_full[b], kConvWarps);
             tc::mbar_init(&a_empty[b], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&d_full[b], 1);
             tc::mbar_init(&d_empty[b], kEpiWarps);
         }
@@ -193,7 +199,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mixture_tc_kernel(TcParams p) {
     }
     for (int c = tid; c < DP; c += kTcThreads) s_c[c] = p.center[c];
     // constant K groups of the A buffers: a 1 in column DP (hi part), zeros elsewhere
-    for (int e = tid; e < nbufA * NPART * 2 * kTcTile; e += kTcThreads) {
+    for (int e = tid; e < (NOB ? 0 : nbufA * NPART * 2 * kTcTile); e += kTcThreads) {
         const int row = e % kTcTile, g = (e / kTcTile) & 1, part = (e / (2 * kTcTile)) % NPART,
                   buf = e / (2 * kTcTile * NPART);
         const uint32_t one = KIND == tc::kTF32 ? 0x3F800000u : 0x3F80u;
@@ -555,9 +561,12 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
     constexpr int NPART = SPLIT == 3 ? 2 : 1;
     constexpr size_t RAW_BYTES = (size_t)kTcTile * (DP + 4) * 4;
     constexpr size_t A_PART = (size_t)kTcTile * KGX * 16;
+    constexpr size_t A_PART_NOB = (size_t)kTcTile * (KGX - 2) * 16;
     constexpr size_t B_COMP = (size_t)DP * KGX * 16;
     static_assert(NPART * B_COMP <= (size_t)DP * (4 * DP + 64), "operand form exceeds its workspace slot");
     const int nslots = p.last_slot - p.first_slot + 1;
+    // one component centred at its own location: no offset column
+    const bool nob = nslots == 1 && cslot == p.first_slot;
     // largest chunk (<= 256 TMEM columns) whose buffers fit: one chunk keeps
     // three staged tiles and two A buffers; several chunks keep one A buffer
     // and a ring of kBRing chunk buffers, with one staged tile or none
@@ -567,7 +576,8 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
         nch = (nslots + chunk - 1) / chunk;
         if (nch == 1) {
             stages = 3;
-            smem = stages * RAW_BYTES + 2 * NPART * A_PART + (size_t)NPART * chunk * B_COMP + (size_t)DP * 4;
+            smem = stages * RAW_BYTES + (nob ? 3 * NPART * A_PART_NOB : 2 * NPART * A_PART) +
+                   (size_t)NPART * chunk * B_COMP + (size_t)DP * 4;
         } else {
             // a staged tile if it fits beside a kBRing-deep operand ring; else
             // the converters read their rows from global memory (no staged
@@ -591,7 +601,9 @@ static int launch_tc(TcParams p, const float *w, const float *loc, int cslot, un
       note_launch(); }
     // DIRECT (no staged tile; converters read rows from global memory) is a
     // separate instantiation so the staged form keeps its registers
-    auto kern = stages == 0 ? mixture_tc_kernel<KIND, SPLIT, DP, true> : mixture_tc_kernel<KIND, SPLIT, DP, false>;
+    auto kern = stages == 0 ? mixture_tc_kernel<KIND, SPLIT, DP, true, false>
+                : nob && nch == 1 ? mixture_tc_kernel<KIND, SPLIT, DP, false, true>
+                                  : mixture_tc_kernel<KIND, SPLIT, DP, false, false>;
     const int st = allow_dynamic_smem((const void *)kern);
     if (st) return st;
     int occ = 1;
