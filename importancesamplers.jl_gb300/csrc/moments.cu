@@ -149,16 +149,19 @@ int weighted_moments(const void *x, int d, int64_t n, const void *lw, int dtype,
 // (src/proposals.jl:73-80); zero upper triangle; lognormalizer and validity
 // (:493-528).
 // 1 / a in FP64 with few FP64 instructions: an FP32 reciprocal seed refined
-// by two Newton-Raphson steps r <- r + r (1 - a r) (about 24 -> 48 -> full
-// double bits). Each FP64 instruction occupies a warp's FP64 pipe for about
-// 64 cycles on this GPU (and takes as long to complete), so the factorisation's
+// by two Newton-Raphson steps r <- r + r (1 - a r) (about 23 -> 46 -> full
+// double bits; the seed is the hardware's approximate FP32 reciprocal). Each
+// FP64 instruction occupies a warp's FP64 pipe for about 64 cycles on this
+// GPU (and takes as long to complete), so the factorisation's
 // sequential chain is built from as few of them as possible. Values outside
 // the FP32 seed's range, zero, negative or non-finite values take the exact
 // division (and give its NaN / Inf).
 __device__ __forceinline__ double rcp_nr(double a) {
     const float af = (float)a;
     if (!(af > 1e-30f && af < 1e30f)) return 1.0 / a;
-    double r = (double)__frcp_rn(af);
+    float rf;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(af));  // one MUFU op; Newton makes up the bits
+    double r = (double)rf;
     double e = fma(-a, r, 1.0);
     r = fma(r, e, r);
     e = fma(-a, r, 1.0);
@@ -187,9 +190,11 @@ template <typename V> __device__ __forceinline__ V warp_sum_all(V v) {
 //  * one thread per row solves its panel row, l_ic = (a_ic - sum_q l_iq d_q
 //    l_cq) / d_c;
 //  * while warp 0 updates and factors the next diagonal block (lookahead),
-//    warps 1..7 apply the rank-8 update to the rest of the trailing lower
-//    triangle, each thread holding up to eight independent elements (column
-//    pairs (k, m-1-k) balance the work), so the pipe, not latency, bounds it.
+//    warps 1-3 and 5-7 apply the rank-8 update to the rest of the trailing
+//    lower triangle, each thread holding up to nine independent elements
+//    (column pairs (k, m-1-k) balance the work), so the pipe, not latency,
+//    bounds it; warp 4 stays out, since it would queue FP64 instructions on
+//    warp 0's sub-partition ahead of the pivot chain.
 // The pivots fail exactly when Cholesky's would (d_j <= 0 or not finite).
 template <typename T>
 __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restrict__ mean,
@@ -333,15 +338,20 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
             }
             __syncwarp();
             factor_diag(base, nbn, wn);
-        } else {
-            // rank-nb update of the trailing lower triangle outside the next diagonal block
-            const int wt = tid - 32, half = (m + 1) >> 1, total = half * (m + 1);
-            int ei[8], ek[8];
+        } else if (warp != 4) {
+            // rank-nb update of the trailing lower triangle outside the next
+            // diagonal block, by warps 1-3 and 5-7: warp 4 shares warp 0's
+            // sub-partition (warp id mod 4) and so its FP64 pipe, which the
+            // pivot chain needs free
+            const int wt = (warp < 4 ? warp - 1 : warp - 2) * 32 + lane, half = (m + 1) >> 1,
+                      total = half * (m + 1);
+            constexpr int kT = 9;  // elements per thread: 192 x 9 >= 28 x 57, the largest trailing triangle
+            int ei[kT], ek[kT];
 #pragma unroll
-            for (int t = 0; t < 8; ++t) {
+            for (int t = 0; t < kT; ++t) {
                 ei[t] = -1;
                 ek[t] = 0;
-                const int e = wt + t * 224;
+                const int e = wt + t * 192;
                 if (e < total) {
                     const int c = e / (m + 1), r = e - c * (m + 1);
                     int i = -1, k = 0;
@@ -361,16 +371,16 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
                     }
                 }
             }
-            double acc[8];
+            double acc[kT];
 #pragma unroll
-            for (int t = 0; t < 8; ++t) acc[t] = ei[t] >= 0 ? A[(base + ei[t]) + (base + ek[t]) * d] : 0.0;
+            for (int t = 0; t < kT; ++t) acc[t] = ei[t] >= 0 ? A[(base + ei[t]) + (base + ek[t]) * d] : 0.0;
             for (int c = 0; c < nb; ++c) {
 #pragma unroll
-                for (int t = 0; t < 8; ++t)
+                for (int t = 0; t < kT; ++t)
                     if (ei[t] >= 0) acc[t] = fma(-A[(base + ei[t]) + (kb + c) * d], wc[c][base + ek[t]], acc[t]);
             }
 #pragma unroll
-            for (int t = 0; t < 8; ++t)
+            for (int t = 0; t < kT; ++t)
                 if (ei[t] >= 0) A[(base + ei[t]) + (base + ek[t]) * d] = acc[t];
         }
         __syncthreads();
