@@ -186,7 +186,8 @@ template <typename V> __device__ __forceinline__ V warp_sum_all(V v) {
 // FP64 instruction holds a warp's FP64 pipe for about 64 cycles on this GPU
 // (and takes as long to complete), so:
 //  * the sequential chain per column is only 1/d_j (an FP32 seed and two
-//    Newton steps), run by warp 0 on the 8 x 8 diagonal block;
+//    Newton steps), run by warp 0 on the 8 x 8 diagonal block, which it
+//    holds in registers (one element per lane, shuffles between steps);
 //  * one thread per row solves its panel row, l_ic = (a_ic - sum_q l_iq d_q
 //    l_cq) / d_c;
 //  * while warp 0 updates and factors the next diagonal block (lookahead),
@@ -268,32 +269,52 @@ __global__ void __launch_bounds__(256) fit_factor_kernel(const double *__restric
     __syncthreads();
 
     // ---- blocked LDL^T ----
+    // warp 0: LDL^T of the nb x nb diagonal block at (kb, kb), in registers.
+    // Lane e < 28 holds the strictly-lower element (ei, ec) of the block
+    // (row-major lower order, e = ei (ei - 1) / 2 + ec) and lanes 0..nb-1 the
+    // diagonal; a column step is a pivot broadcast, the reciprocal chain, one
+    // scaling and one update per held element, with the operands exchanged by
+    // warp shuffles, so the chain holds no shared-memory round trip
     auto factor_diag = [&](int kb, int nb, double (*w)[64]) {  // warp 0
-        for (int j = kb; j < kb + nb; ++j) {
-            const double dj = A[j + j * d];
+        int ei = 1, ec = 0;
+        {
+            int t = lane;
+            while (ei < 8 && t >= ei) {
+                t -= ei;
+                ++ei;
+            }
+            ec = t;
+        }
+        const bool hasl = lane < 28 && ei < nb;
+        const bool hasd = lane < nb;
+        double vl = hasl ? A[(kb + ei) + (kb + ec) * d] : 0.0;
+        double vd = hasd ? A[(kb + lane) + (kb + lane) * d] : 0.0;
+        double ul = 0.0;  // u = l d of this lane's lower element, once its column is done
+        const int lane_d = lane * (lane - 1) / 2;  // lanes of row `lane`'s lower elements start here
+        for (int j = 0; j < nb; ++j) {
+            const double dj = __shfl_sync(0xffffffffu, vd, j);
             const double rj = rcp_nr(dj);
             if (lane == 0) {
-                s_dg[j] = dj;
-                s_rinv[j - kb] = rj;
+                s_dg[kb + j] = dj;
+                s_rinv[j] = rj;
             }
-            const int rows = kb + nb - 1 - j;
-            if (lane < rows) {
-                const double u = A[(j + 1 + lane) + j * d];
-                w[j - kb][j + 1 + lane] = u;
-                A[(j + 1 + lane) + j * d] = u * rj;
+            // column j: element (ei, j) becomes l = u / d_j
+            if (hasl && ec == j) {
+                ul = vl;
+                vl = vl * rj;
+                w[j][kb + ei] = ul;
             }
-            __syncwarp();
-            if (lane < rows * (rows + 1) / 2) {
-                int c = 0, t = lane;
-                while (t >= rows - c) {
-                    t -= rows - c;
-                    ++c;
-                }
-                const int i = c + t;
-                A[(j + 1 + i) + (j + 1 + c) * d] -= A[(j + 1 + i) + j * d] * w[j - kb][j + 1 + c];
-            }
-            __syncwarp();
+            // (ei, ec), ec > j: -= l(ei, j) u(ec, j); diagonal (c, c), c > j: -= l(c, j) u(c, j)
+            const double l_i = __shfl_sync(0xffffffffu, vl, (ei * (ei - 1) / 2 + j) & 31);
+            const double u_c = __shfl_sync(0xffffffffu, ul, (ec * (ec - 1) / 2 + j) & 31);
+            const double l_d = __shfl_sync(0xffffffffu, vl, (lane_d + j) & 31);
+            const double u_d = __shfl_sync(0xffffffffu, ul, (lane_d + j) & 31);
+            if (hasl && ec > j) vl = fma(-l_i, u_c, vl);
+            if (hasd && lane > j) vd = fma(-l_d, u_d, vd);
         }
+        if (hasl) A[(kb + ei) + (kb + ec) * d] = vl;
+        if (hasd) A[(kb + lane) + (kb + lane) * d] = vd;  // the pivot d_lane
+        __syncwarp();
     };
     if (warp == 0) factor_diag(0, min(8, d), s_w[0]);
     __syncthreads();
