@@ -47,7 +47,8 @@ size_t issm_amis_run_workspace_bytes(int32_t d, int64_t total, int32_t rounds) {
 }
 
 int issm_amis_run(const issm_amis_run_desc *r, issm_stream_t stream) {
-    if (!r || !r->target || !r->round_sizes) return ISSM_E_NULL;
+    if (!r || (!r->target && !r->target_bank) || !r->round_sizes) return ISSM_E_NULL;
+    if (r->target_bank && !r->target_den) return ISSM_E_NULL;
     const issm_bank &h = r->history;
     const int d = h.dim, rounds = r->rounds;
     if (d < 1 || d > 64 || rounds < 1 || h.count < rounds) return ISSM_E_SIZE;
@@ -80,6 +81,10 @@ int issm_amis_run(const issm_amis_run_desc *r, issm_stream_t stream) {
     char *loc = (char *)h.locations, *fac = (char *)h.scales, *lnorm = (char *)h.lognormalizers;
     uint64_t *fail_all = (uint64_t *)r->round_failures;
 
+    // scratch reset: the sticky timeout words and last-block counters sit at
+    // offsets that depend on (rounds, d, total), so a workspace reused by
+    // runs of another shape must not keep the earlier run's bytes there
+    ISSM_TRY((int)cudaMemsetAsync(ws, 0, tc_bytes + mom_bytes + red_bytes, s));
     // slot 0 <- the committed proposal; state reset
     ISSM_TRY((int)cudaMemcpyAsync(loc, r->initial_location, d * es, cudaMemcpyDeviceToDevice, s));
     ISSM_TRY((int)cudaMemcpyAsync(fac, r->initial_factor, (size_t)d * d * es, cudaMemcpyDeviceToDevice, s));
@@ -100,7 +105,16 @@ int issm_amis_run(const issm_amis_run_desc *r, issm_stream_t stream) {
         ISSM_TRY(issm_draw_philox(&view, t, r->seed, r->counter, offset, nullptr, 0, nullptr, 0, n_new, x_new, fail, 0,
                                   stream));
         offset += (uint64_t)n_new * d + 8;
-        if (r->target_operand)  // X beta on the tensor cores, the likelihood in the epilogue
+        if (r->target_bank) {  // a radial-mixture target: the proposals' density kernels
+            if (r->target_bank_precision != ISSM_PREC_NATIVE)
+                ISSM_TRY(issm_mixture_logdensity_ws(r->target_bank, r->target_den, x_new, n_new, nullptr, 0,
+                                                    logtargets + (size_t)n_old * es, nullptr, nullptr, 0,
+                                                    r->target_bank_precision, ws_tc, tc_bytes, stream));
+            else
+                ISSM_TRY(issm_mixture_logdensity(r->target_bank, r->target_den, x_new, n_new, nullptr, 0,
+                                                 logtargets + (size_t)n_old * es, nullptr, nullptr, 0,
+                                                 ISSM_PREC_NATIVE, stream));
+        } else if (r->target_operand)  // X beta on the tensor cores, the likelihood in the epilogue
             ISSM_TRY(issm_glm_logdensity(r->target, r->target_precision, r->target_operand, (const float *)x_new, n_new,
                                          (float *)(logtargets + (size_t)n_old * es),
                                          (int32_t *)(ws_tc + tc_bytes - 64), stream));

@@ -69,7 +69,8 @@ class AmisRunDesc(C.Structure):
                 ("cov", C.c_void_p), ("shift", C.c_void_p), ("cand_location", C.c_void_p),
                 ("cand_factor", C.c_void_p), ("cand_lognormalizer", C.c_void_p), ("workspace", C.c_void_p),
                 ("workspace_bytes", C.c_size_t), ("target_operand", C.c_void_p), ("target_precision", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("reserved", C.c_int32), ("target_bank", C.c_void_p), ("target_den", C.c_void_p),
+                ("target_bank_precision", C.c_int32), ("reserved2", C.c_int32)]
 
 
 TARGET_GAUSS_MIX, TARGET_STUDENT_T, TARGET_LINREG, TARGET_LOGISTIC, TARGET_STD_NORMAL, TARGET_QUADRATIC = range(6)

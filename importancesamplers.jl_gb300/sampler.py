@@ -468,11 +468,12 @@ def _moment_body(s, is_npmc):
 def native_body_eligible(s):
     """issm_amis_run covers AMIS with a Gaussian factor history, a native
     target, generated normals and no per-span profiling."""
-    from .targets import _Bound
+    from .targets import _Bound, _BoundBank
 
     h = getattr(s, "history", None)
     return (isinstance(s.algorithm, AMIS) and h is not None and h.family == GAUSSIAN and h.d <= 64
-            and h.scale_kind == native.SCALE_FACTOR and isinstance(s.bound_target, _Bound) and s.profile is None
+            and h.scale_kind == native.SCALE_FACTOR and isinstance(s.bound_target, (_Bound, _BoundBank))
+            and s.profile is None
             and "normals" not in s.__dict__ and "uniforms" not in s.__dict__
             and (s.precision == native.PREC_NATIVE or h.dtype == torch.float32))
 
@@ -490,7 +491,11 @@ def _native_body(s):
     sizes = (ctypes.c_int64 * s.rounds)(*[int(v) for v in s.schedule])
     bank = h.view(h.count)._obj
     loc0, fac0, ln0 = s.committed
-    desc = native.AmisRunDesc(bank, ctypes.cast(ctypes.byref(s.bound_target.struct), ctypes.c_void_p), s.rounds,
+    from .targets import _BoundBank
+
+    radial = isinstance(s.bound_target, _BoundBank)
+    target_ptr = None if radial else ctypes.cast(ctypes.byref(s.bound_target.struct), ctypes.c_void_p)
+    desc = native.AmisRunDesc(bank, target_ptr, s.rounds,
                               int(s.precision), ctypes.cast(sizes, ctypes.c_void_p), float(h.logconstant), s.seed, 0,
                               native.ptr(s.counter), native.ptr(s.logcounts), native.ptr(s.round_ids_init),
                               native.ptr(loc0), native.ptr(fac0), native.ptr(ln0), native.ptr(s.samples),
@@ -499,9 +504,15 @@ def _native_body(s):
                               native.ptr(s.mean), native.ptr(s.cov), native.ptr(s.shift), native.ptr(s.cand_loc),
                               native.ptr(s.cand_factor), native.ptr(s.cand_lognorm), native.ptr(ws), ws.numel())
     # the same target form as the host round loop's evaluate()
-    operand = s.bound_target.tensor_operand(s.target_precision, h.dtype, s.device)
-    if operand is not None:
-        desc.target_operand, desc.target_precision = native.ptr(operand), int(s.target_precision)
+    if radial:
+        tb = s.bound_target
+        desc.target_bank = ctypes.addressof(tb.bank.struct)
+        desc.target_den = ctypes.addressof(tb.den)
+        desc.target_bank_precision = tb.effective_precision(s.target_precision, h.dtype)
+    else:
+        operand = s.bound_target.tensor_operand(s.target_precision, h.dtype, s.device)
+        if operand is not None:
+            desc.target_operand, desc.target_precision = native.ptr(operand), int(s.target_precision)
     native.call("issm_amis_run", ctypes.byref(desc), native.stream_ptr())
     s.offset = sum(int(v) * d + 8 for v in s.schedule)
 

@@ -90,10 +90,16 @@ class _BoundBank:
         kind = native.DENOM_GENERATING if coef is None else native.DENOM_FULL
         self.den = ops.denominator(kind, coef)
 
-    def evaluate(self, samples, out=None, precision=None):
-        prec = native.PREC_NATIVE if precision is None else precision
-        if prec != native.PREC_NATIVE and (self.bank.scale_kind != native.SCALE_FACTOR or samples.dtype != torch.float32):
+    def effective_precision(self, precision, dtype):
+        """The form the density kernels run in: a tensor-core form only for a
+        factor bank and FP32 samples, else the SIMT form."""
+        prec = native.PREC_NATIVE if precision is None else int(precision)
+        if prec != native.PREC_NATIVE and (self.bank.scale_kind != native.SCALE_FACTOR or dtype != torch.float32):
             prec = native.PREC_NATIVE
+        return prec
+
+    def evaluate(self, samples, out=None, precision=None):
+        prec = self.effective_precision(precision, samples.dtype)
         return ops.mixture_logdensity(self.bank, self.den, samples, fixed_slot=0, precision=prec, out=out)
 
 

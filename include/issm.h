@@ -584,7 +584,7 @@ int issm_glm_logdensity(const issm_target *target, int32_t precision,
  * for the tensor-core precisions. Sample t of round r takes normal stream
  * elements from normal_offset (+ *counter); *counter advances by the run's
  * total at the end. The workspace (issm_amis_run_workspace_bytes) is zeroed
- * once when created; it holds, in order, the tensor-core scratch
+ * by the run itself at its start; it holds, in order, the tensor-core scratch
  * (issm_tc_workspace_bytes(rounds, d), rounded up to 256 bytes), the moments
  * scratch (issm_moments_workspace_bytes(total, d), rounded up) and the
  * reduction scratch; the first two end in their sticky timeout words.
@@ -592,6 +592,10 @@ int issm_glm_logdensity(const issm_target *target, int32_t precision,
  * (issm_glm_prepare for target_precision) and the target runs through
  * issm_glm_logdensity, its timeout word shared with the tensor-core
  * scratch's; NULL runs issm_target_logdensity (SIMT, the target's type).
+ * target_bank, when not NULL, is a target that is itself a radial mixture
+ * (a normalised Student-t or Gaussian, one slot or several): it runs through
+ * issm_mixture_logdensity[_ws] with target_den at target_bank_precision, the
+ * tensor-core scratch shared, and `target` may then be NULL.
  * ISSM_E_UNSUPPORTED for Student-t or non-factor histories. */
 typedef struct issm_amis_run_desc {
     issm_bank history;
@@ -614,6 +618,9 @@ typedef struct issm_amis_run_desc {
     size_t workspace_bytes;
     const void *target_operand;      /* issm_glm_prepare output, or NULL */
     int32_t target_precision, reserved;
+    const issm_bank *target_bank;            /* a normalised radial target, or NULL */
+    const issm_denominator *target_den;      /* its denominator (slot 0 generating, or full) */
+    int32_t target_bank_precision, reserved2;
 } issm_amis_run_desc;
 size_t issm_amis_run_workspace_bytes(int32_t d, int64_t total, int32_t rounds);
 int issm_amis_run(const issm_amis_run_desc *run, issm_stream_t stream);

@@ -91,17 +91,23 @@ def test_tc_amis_far_start_completes(issm, cuda, d, n_obs, budget):
     assert np.isfinite(float(res.diagnostics["round_lognormalizers"][-1]))
 
 
+@pytest.mark.parametrize("kind", ["linreg", "student_t"])
 @pytest.mark.parametrize("precision", ["native", "bf16"])
 @pytest.mark.parametrize("d", [5, 33, 64])
-def test_native_run_matches_host_round_loop(issm, cuda, precision, d):
+def test_native_run_matches_host_round_loop(issm, cuda, precision, d, kind):
     """issm_amis_run issues the same library calls as the host round loop:
-    samples, log weights, summaries and the final proposal are bitwise equal."""
+    samples, log weights, summaries and the final proposal are bitwise equal,
+    for a target with its own kernel (linear regression: SIMT, or X beta on
+    the tensor cores in the bf16 form) and for a radial-mixture target (a
+    normalised Student-t, evaluated by the proposals' density kernels)."""
     rng = np.random.default_rng(d)
     X = rng.normal(size=(200, d))
     y = X @ rng.normal(size=d) + 0.5 * rng.normal(size=200)
     target = issm.LinearRegressionTarget(X, y, sigma=0.5, prior_var=1.0)
     mean, _ = target.analytic()
     L = np.linalg.cholesky(np.linalg.inv(X.T @ X / 0.25 + np.eye(d)))
+    if kind == "student_t":
+        target = issm.StudentTTarget(mean, L, 5.0)
     p = issm.FactorGaussian((mean + 0.1 * L @ rng.normal(size=d)).astype(np.float32), (1.2 * L).astype(np.float32))
     prec = issm.native.PREC_NATIVE if precision == "native" else issm.native.PREC_BF16
     out = []
