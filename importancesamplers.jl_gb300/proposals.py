@@ -66,19 +66,18 @@ def student_t_logconstant(dof, dimension):
 
 
 def factor_exponent_bound(factor):
-    """_factor_exponent_bound (src/student_t_range.jl:21-31)."""
-    bound = 0
-    d = factor.shape[0]
-    for c in range(d):
-        for r in range(c, d):
-            v = float(factor[r, c])
-            if v == 0.0:
-                continue
-            if not math.isfinite(v):
-                return 1 << 62
-            _, e = math.frexp(v)
-            bound = max(bound, abs(e), abs(e - 1))
-    return bound
+    """_factor_exponent_bound (src/student_t_range.jl:21-31): the largest
+    |e| or |e - 1| over the binary exponents e (v = m 2^e, m in [0.5, 1)) of
+    the nonzero lower-triangle entries; 2^62 when one is not finite."""
+    f = np.asarray(factor, dtype=np.float64)
+    v = f[np.tril_indices(f.shape[0])]
+    v = v[v != 0.0]
+    if v.size == 0:
+        return 0
+    if not np.all(np.isfinite(v)):
+        return 1 << 62
+    e = np.frexp(v)[1].astype(np.int64)
+    return int(max(np.abs(e).max(), np.abs(e - 1).max()))
 
 
 def factor_range_risk(bound, dt):
