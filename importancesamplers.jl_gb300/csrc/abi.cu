@@ -107,7 +107,7 @@ const char *issm_status_string(int status) {
     case ISSM_E_DTYPE: return "unsupported or mismatched dtype";
     case ISSM_E_KIND: return "unknown family, scale or denominator kind";
     case ISSM_E_ALL_ZERO: return "normalized weights are undefined because all raw weights are zero";
-    case ISSM_E_UNSUPPORTED: return "request not supported by this build";
+    case ISSM_E_UNSUPPORTED: return "request not supported by this library";
     case ISSM_E_WORKSPACE: return "workspace too small";
     case ISSM_E_NOT_POSDEF: return "covariance is not positive definite";
     case ISSM_E_SCRATCH_LIMIT: return "input larger than the fixed scratch of a no-allocation entry point allows";

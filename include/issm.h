@@ -45,7 +45,7 @@ typedef struct CUstream_st *issm_stream_t;
 #define ISSM_E_DTYPE          (-3)   /* unsupported dtype / dtype mismatch    */
 #define ISSM_E_KIND           (-4)   /* unknown family/scale/denominator kind */
 #define ISSM_E_ALL_ZERO       (-5)   /* every log weight is -Inf (AllZeroWeightsError, src/results.jl:133-144) */
-#define ISSM_E_UNSUPPORTED    (-6)   /* valid request this build does not run */
+#define ISSM_E_UNSUPPORTED    (-6)   /* valid request this library does not run */
 #define ISSM_E_WORKSPACE      (-7)   /* workspace too small                   */
 #define ISSM_E_NOT_POSDEF     (-8)   /* Cholesky met a non-positive pivot     */
 #define ISSM_E_SCRATCH_LIMIT  (-9)   /* input larger than a fixed scratch allows */

@@ -1,10 +1,11 @@
 """Generate tests/golden/reference_vectors.json.
 
-The reference (ImportanceSamplers.jl) is Julia and cannot run in this build
-environment, so its known-answer tests are read as specifications: each case
-below re-enters the literal inputs of one reference test (cited file:line) and
-its expected output, either the literal the test asserts or the closed form the
-test compares against, evaluated here in 120-bit mpmath arithmetic.
+The reference (ImportanceSamplers.jl) is Julia, and no Julia is installed
+where these fixtures are made, so its known-answer tests are read as
+specifications: each case below re-enters the literal inputs of one reference
+test (cited file:line) and its expected output, either the literal the test
+asserts or the closed form the test compares against, evaluated here in
+120-bit mpmath arithmetic.
 
 Run:  python tests/golden/make_golden.py [--check-source REFERENCE_ROOT]
 

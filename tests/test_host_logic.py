@@ -193,3 +193,91 @@ def test_grouped_table_offsets_and_layout(issm):
     assert np.all(t.view(np.float64)[:, col["t_const"]] == -1.5)
     # the fixed rows are not modified by building a table
     assert runs[1].row[col["round"]] == 0
+
+
+def test_grouped_run_preparation_layout(issm):
+    """A grouped run's host preparation: one allocation of 256-byte aligned,
+    non-overlapping slices in the issm_group_run order the step kernels read,
+    an admission head holding the target's mode and upper factor (column
+    major) and the history's slot 0, and the mode-centred target constant
+    equal to the log joint density at the mode."""
+    rng = np.random.default_rng(2)
+    d, n_obs = 7, 90
+    X = rng.normal(size=(n_obs, d))
+    y = X @ rng.normal(size=d) + 0.5 * rng.normal(size=n_obs)
+    tgt = issm.LinearRegressionTarget(X, y, sigma=0.5, prior_var=1.0)
+    p = issm.FactorGaussian(rng.normal(size=d).astype(np.float32), (0.3 * np.eye(d)).astype(np.float32))
+    req = issm.serving.ServeRequest(0, tgt, p, rounds=4, round_size=1000, seed=3)
+    prep = issm.serving._Prep(req)
+    offs = sorted(prep.off.items(), key=lambda kv: kv[1])
+    assert all(o % 256 == 0 for _, o in offs)
+    assert [k for k, _ in offs[:6]] == ["failures", "t_mode", "t_chol", "lognorm", "loc", "fac"]
+    assert offs[-1][1] < prep.nbytes
+    head = prep.head
+    assert head.size == prep.off["fac"] + 4 * d * d
+    f32 = head.view(np.float32)
+    # failure words are zero; the head's other slots hold what the kernels read
+    assert not head[prep.off["failures"]:prep.off["failures"] + 24 * 4].any()
+    A = X.T @ X / 0.25 + np.eye(d)
+    mode = np.linalg.solve(A, X.T @ y / 0.25)
+    o = prep.off["t_mode"] // 4
+    assert np.allclose(f32[o:o + d], mode, rtol=1e-6)
+    o = prep.off["t_chol"] // 4
+    U = f32[o:o + d * d].reshape(d, d).T  # column-major
+    assert np.allclose(U.T @ U, A, rtol=1e-5) and np.allclose(np.tril(U, -1), 0)
+    o = prep.off["loc"] // 4
+    assert np.array_equal(f32[o:o + d], p.location)
+    # t_const = log N(y | X mode, s2 I) + log N(mode | 0, I)
+    r = y - X @ mode
+    c0 = (-0.5 * n_obs * np.log(2 * np.pi * 0.25) - 0.5 * r @ r / 0.25 - 0.5 * d * np.log(2 * np.pi)
+          - 0.5 * mode @ mode)
+    assert prep.t_const == pytest.approx(c0, rel=1e-12)
+
+
+def test_factor_exponent_bound_matches_the_entrywise_rule(issm):
+    """The vectorised bound equals the entry-by-entry rule of
+    src/student_t_range.jl:21-31 (max |e|, |e - 1| over the nonzero
+    lower-triangle binary exponents; 2^62 for a non-finite entry; the upper
+    triangle ignored)."""
+    import math
+    import sys
+
+    bound = sys.modules["issm.proposals"].factor_exponent_bound
+
+    def entrywise(f):
+        b = 0
+        for c in range(f.shape[0]):
+            for r in range(c, f.shape[0]):
+                v = float(f[r, c])
+                if v == 0.0:
+                    continue
+                if not math.isfinite(v):
+                    return 1 << 62
+                e = math.frexp(v)[1]
+                b = max(b, abs(e), abs(e - 1))
+        return b
+
+    rng = np.random.default_rng(8)
+    cases = [np.tril(rng.normal(size=(k, k)) * 10.0 ** rng.integers(-60, 60)) for k in (1, 2, 9, 64)]
+    cases += [np.zeros((3, 3)), np.diag([1e-310, 1.0, 1e308]), np.tril(rng.normal(size=(6, 6))).astype(np.float32)]
+    bad = np.eye(4)
+    bad[2, 1] = np.inf
+    upper = np.eye(4)
+    upper[0, 3] = np.nan
+    cases += [bad, upper]
+    for f in cases:
+        assert bound(f) == entrywise(f)
+
+
+def test_linear_regression_evidence_in_d_dimensions(issm):
+    """The conjugate evidence in d x d form (determinant lemma and Woodbury)
+    equals the n-dimensional Gaussian marginal of y."""
+    rng = np.random.default_rng(9)
+    for n, d in ((40, 3), (300, 12)):
+        X = rng.normal(size=(n, d))
+        y = X @ rng.normal(size=d) + 0.7 * rng.normal(size=n)
+        t = issm.LinearRegressionTarget(X, y, sigma=0.7, prior_var=2.0)
+        _, logz = t.analytic()
+        C = 0.49 * np.eye(n) + 2.0 * X @ X.T
+        ref = -0.5 * (n * np.log(2 * np.pi) + np.linalg.slogdet(C)[1] + y @ np.linalg.solve(C, y))
+        assert logz == pytest.approx(ref, rel=1e-11, abs=1e-9)
