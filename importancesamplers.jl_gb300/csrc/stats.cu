@@ -3,8 +3,10 @@
 //   weighted_sum      sum_i w_i x_i per coordinate with the self-normalised
 //                     weights w_i = e^{l_i - m} / S of the result's summary
 //                     (Statistics.mean(result) and, on f's values,
-//                     Statistics.mean(f, result), :11-33): FP64 sums, per-block
-//                     partials reduced in a fixed order (bitwise reproducible);
+//                     Statistics.mean(f, result), :11-33): FP64 sums for FP64
+//                     data, compensated FP32 sums merged in FP64 for FP32 data,
+//                     per-block partials reduced in a fixed order (bitwise
+//                     reproducible);
 //   weighted_quantile component-wise weighted quantiles with the StatsBase
 //                     generic-weight interpolation rule of _weighted_quantile
 //                     (:114-154), which the reference evaluates on the host
@@ -57,6 +59,52 @@ __global__ void weighted_sum_partial_kernel(const T *__restrict__ x, int d, int6
     if (threadIdx.x < dc) partial[((size_t)blockIdx.x * gridDim.y + blockIdx.y) * 64 + threadIdx.x] = acc;
 }
 
+// FP32 samples: per-thread compensated FP32 (Kahan) sums of w x with w in
+// FP32 (expf of the FP32 log weight less the summary's max, times 1/S), four
+// row groups per coordinate merged in FP64 in a fixed order. In FP64 the pass
+// ran on this GPU's narrow FP64 pipe (a conversion and an FMA per element)
+// at several times its memory time. Thread t owns coordinate t % 64 of every
+// fourth row, so a warp reads consecutive coordinates of one row.
+__global__ void __launch_bounds__(kSumThreads) weighted_sum_partial_f32_kernel(const float *__restrict__ x, int d,
+                                                                              int64_t n,
+                                                                              const float *__restrict__ lw,
+                                                                              const double *__restrict__ summary,
+                                                                              double *__restrict__ partial) {
+    __shared__ float ws[kSumTile];
+    __shared__ double s4[4][64];
+    const float m = (float)summary[0], inv = (float)(1.0 / summary[1]);
+    const int c0 = blockIdx.y * 64, dc = min(64, d - c0);
+    const int c = threadIdx.x & 63, rg = threadIdx.x >> 6;
+    float s = 0.f, k = 0.f;
+    const int64_t tiles = (n + kSumTile - 1) / kSumTile;
+    for (int64_t tt = blockIdx.x; tt < tiles; tt += gridDim.x) {
+        const int64_t r0 = tt * kSumTile;
+        const int rows = (int)min((int64_t)kSumTile, n - r0);
+        __syncthreads();
+        if (threadIdx.x < rows) {
+            const float l = lw[r0 + threadIdx.x];
+            ws[threadIdx.x] = l == -INFINITY ? 0.f : expf(l - m) * inv;
+        }
+        __syncthreads();
+        if (c < dc) {
+#pragma unroll 4
+            for (int r = rg; r < rows; r += 4) {
+                const float w = ws[r];
+                if (w == 0.f) continue;  // a zero weight contributes nothing (not even a NaN)
+                const float y = fmaf(w, x[(r0 + r) * d + c0 + c], -k);
+                const float t = s + y;
+                k = (t - s) - y;
+                s = t;
+            }
+        }
+    }
+    s4[rg][c] = (double)s - (double)k;
+    __syncthreads();
+    if (threadIdx.x < dc)
+        partial[((size_t)blockIdx.x * gridDim.y + blockIdx.y) * 64 + threadIdx.x] =
+            ((s4[0][threadIdx.x] + s4[1][threadIdx.x]) + s4[2][threadIdx.x]) + s4[3][threadIdx.x];
+}
+
 __global__ void weighted_sum_finish_kernel(const double *__restrict__ partial, int blocks, int d, double *out) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= d) return;
@@ -66,14 +114,16 @@ __global__ void weighted_sum_finish_kernel(const double *__restrict__ partial, i
     out[c] = s;
 }
 
+constexpr int kSumBlocksPerSm = 8;  // enough loads in flight to stream the samples
+
 static int sum_blocks(int64_t n) {
     const int64_t t = (n + kSumTile - 1) / kSumTile;
-    const int64_t cap = (int64_t)device_sms() * 2;
+    const int64_t cap = (int64_t)device_sms() * kSumBlocksPerSm;
     return (int)(t < cap ? (t < 1 ? 1 : t) : cap);
 }
 
 size_t weighted_sum_workspace_bytes(int64_t n, int d) {
-    return sizeof(double) * (size_t)kSMs * 2 * (size_t)((d + 63) / 64) * 64;
+    return sizeof(double) * (size_t)kSMs * kSumBlocksPerSm * (size_t)((d + 63) / 64) * 64;
 }
 
 int weighted_sum(const void *x, int d, int64_t n, const void *lw, int dtype, const double *summary, double *out,
@@ -82,8 +132,8 @@ int weighted_sum(const void *x, int d, int64_t n, const void *lw, int dtype, con
     const dim3 grid(blocks, (d + 63) / 64);
     double *partial = (double *)ws;
     if (dtype == ISSM_F32)
-        weighted_sum_partial_kernel<float><<<grid, kSumThreads, 0, stream>>>((const float *)x, d, n,
-                                                                            (const float *)lw, summary, partial);
+        weighted_sum_partial_f32_kernel<<<grid, kSumThreads, 0, stream>>>((const float *)x, d, n,
+                                                                         (const float *)lw, summary, partial);
     else
         weighted_sum_partial_kernel<double><<<grid, kSumThreads, 0, stream>>>((const double *)x, d, n,
                                                                              (const double *)lw, summary, partial);

@@ -134,8 +134,9 @@ def _functional_values(f, result):
 def mean(result, f=None):
     """Self-normalised weighted mean (Statistics.mean(result),
     src/statistics.jl:11-16), or the weighted expectation of the scalar
-    function f (mean(f, result), :18-33): one device pass, FP64 sums. Named
-    (dict) samples give a dict of means."""
+    function f (mean(f, result), :18-33): one device pass, FP64 sums for FP64
+    data and compensated FP32 sums merged in FP64 for FP32 data. Named (dict)
+    samples give a dict of means."""
     sm = _checked_summary(result)
     if f is not None:
         v = _functional_values(f, result)
