@@ -273,3 +273,55 @@ def test_fixed_cdf_properties(orc):
     w /= w.sum()
     counts = np.bincount(sys_anc - 1, minlength=lw.size)
     assert np.all(np.abs(counts - w * lw.size) <= 1.0 + 1e-9)
+
+
+def _quantile_rule(values, weights, probabilities):
+    """The StatsBase generic-weight interpolation rule as
+    src/statistics.jl:247-283 states it, restated with numpy for one
+    coordinate: NaN anywhere gives NaN; positive weights only, sorted by value
+    (stable); threshold p (W - w_first) + w_first against the cumulative
+    weights; linear interpolation between the bracketing values."""
+    if np.any(np.isnan(values)):
+        return np.full(len(probabilities), np.nan)
+    keep = np.flatnonzero(weights != 0)
+    order = keep[np.argsort(values[keep], kind="stable")]
+    v, w = values[order], weights[order]
+    cw = np.cumsum(w)
+    total, first = cw[-1], w[0]
+    out = []
+    for p in probabilities:
+        threshold = p * (total - first) + first
+        upper = int(np.searchsorted(cw, threshold, side="right"))  # 0-based index of the first cw > threshold
+        if upper >= len(v):
+            out.append(v[-1])
+            continue
+        lower = upper - 1
+        frac = (threshold - cw[lower]) / (cw[upper] - cw[lower])
+        if frac == 0:
+            out.append(v[lower])
+            continue
+        diff = v[upper] - v[lower]
+        out.append(v[lower] + frac * diff if np.isfinite(diff) else (1 - frac) * v[lower] + frac * v[upper])
+    return np.array(out)
+
+
+def test_weighted_quantile_matches_the_rule(orc):
+    """The oracle's weighted quantile (sort-based, FP64) equals an
+    independent numpy restatement of the reference's rule: random weights,
+    zero weights, ties, a NaN coordinate and the end probabilities."""
+    rng = np.random.default_rng(12)
+    n, d = 3000, 4
+    x = rng.normal(size=(n, d))
+    x[:, 1] = np.round(x[:, 1], 1)  # many ties
+    x[5, 3] = np.nan
+    w = rng.exponential(size=n)
+    w[rng.random(n) < 0.2] = 0.0
+    w /= w.sum()
+    probs = [0.0, 0.01, 0.25, 0.5, 0.9, 0.999, 1.0]
+    got = orc.weighted_quantile(x.reshape(-1), d, w, probs)
+    for c in range(d):
+        exp = _quantile_rule(x[:, c], w, probs)
+        if c == 3:
+            assert np.all(np.isnan(got[:, c]))
+        else:
+            assert np.allclose(got[:, c], exp, rtol=1e-12, atol=1e-12), (c, got[:, c], exp)
